@@ -1,0 +1,190 @@
+/*
+ * qsim_gb300.h — C ABI of the GB300 state-vector engine.
+ *
+ * Every entry point is plain C: opaque context handle, raw device pointers
+ * to complex64 state vectors, host pointers for matrices and results, and an
+ * int status (QSG_OK == 0).  No entry point exits the process; the last
+ * error message of the calling thread is available from qsg_last_error().
+ *
+ * State layout: amplitude i of an n-qubit state is the float pair
+ * (state[2i], state[2i+1]) = (re, im), i.e. normal (interleaved) order.  A
+ * state buffer holds qsg_min_size(n) floats; amplitudes past 2^n are padding
+ * and are kept at zero.  Bit q of an amplitude index is qubit q.
+ *
+ * Gate matrices are row-major interleaved complex float arrays of
+ * 2 * 4^k floats for k target qubits; row/column bit j corresponds to qs[j]
+ * and qs is sorted ascending (the convention of the reference's
+ * lib/matrix.h:26-33 and lib/simulator_basic.h:172-232).
+ *
+ * Work is issued on the context's CUDA stream.  Calls that return a value to
+ * the host synchronise that stream; the others are asynchronous.
+ *
+ * Each declaration names the reference member it replaces (file:line within
+ * quantumlib/qsim).
+ */
+#ifndef QSIM_GB300_H_
+#define QSIM_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  QSG_OK = 0,
+  QSG_ERR_INVALID = 1,       /* bad argument (qubit index, size, null ptr) */
+  QSG_ERR_OOM = 2,           /* device or pinned-host allocation failed    */
+  QSG_ERR_CUDA = 3,          /* CUDA runtime error                         */
+  QSG_ERR_UNSUPPORTED = 4,   /* e.g. more target qubits than supported     */
+  QSG_ERR_SIZE_MISMATCH = 5, /* states with different qubit counts         */
+  QSG_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up         */
+};
+
+typedef struct qsg_ctx qsg_ctx;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* qsg_last_error(void);
+/* Library version string. */
+const char* qsg_version(void);
+
+/* ---- context ------------------------------------------------------------
+ * Replaces the per-object device workspace of SimulatorCUDA
+ * (lib/simulator_cuda.h:52-54, d_ws/h_ws) and StateSpaceCUDA's scratch
+ * (lib/statespace_cuda.h:378-390).  `stream` may be NULL: the context then
+ * creates its own non-blocking stream.  One context per host thread. */
+int qsg_ctx_create(int device, void* stream, qsg_ctx** out);
+int qsg_ctx_destroy(qsg_ctx* ctx);
+int qsg_ctx_sync(qsg_ctx* ctx);     /* VectorSpaceCUDA::DeviceSync :162 */
+int qsg_ctx_num_sms(qsg_ctx* ctx, int* out);
+void* qsg_ctx_stream(qsg_ctx* ctx);
+
+/* ---- vector space (lib/vectorspace_cuda.h) ----------------------------- */
+/* StateSpaceCUDA::MinSize (lib/statespace_cuda.h:81-83), in floats. */
+uint64_t qsg_min_size(unsigned num_qubits);
+/* VectorSpaceCUDA::Create(n) (lib/vectorspace_cuda.h:87-96).  On OOM returns
+ * QSG_ERR_OOM and *out = NULL (the reference returns Null()). */
+int qsg_state_create(qsg_ctx* ctx, unsigned num_qubits, float** out);
+/* VectorSpaceCUDA::Free / detail::free (lib/vectorspace_cuda.h:108-110). */
+int qsg_state_free(qsg_ctx* ctx, float* state);
+/* Copy overloads (lib/vectorspace_cuda.h:116-160); sizes are MinSize(n). */
+int qsg_copy_d2d(qsg_ctx* ctx, float* dest, const float* src, unsigned n);
+int qsg_copy_d2h(qsg_ctx* ctx, float* host_dest, const float* src, unsigned n);
+int qsg_copy_h2d(qsg_ctx* ctx, float* dest, const float* host_src, unsigned n);
+/* Copy(src, size, dest) (:152-160): copies min(size, MinSize(n)) floats. */
+int qsg_copy_h2d_partial(qsg_ctx* ctx, float* dest, const float* host_src,
+                         uint64_t size, unsigned n);
+
+/* ---- state space (lib/statespace_cuda.h) ------------------------------- */
+/* InternalToNormalOrder / NormalToInternalOrder (:85-107).  The internal
+ * order of this engine is the normal order, so both only validate. */
+int qsg_internal_to_normal(qsg_ctx* ctx, float* state, unsigned n);
+int qsg_normal_to_internal(qsg_ctx* ctx, float* state, unsigned n);
+int qsg_set_all_zeros(qsg_ctx* ctx, float* state, unsigned n);   /* :109 */
+int qsg_set_state_uniform(qsg_ctx* ctx, float* state, unsigned n); /* :115 */
+int qsg_set_state_zero(qsg_ctx* ctx, float* state, unsigned n);  /* :130 */
+int qsg_get_ampl(qsg_ctx* ctx, const float* state, unsigned n, uint64_t i,
+                 float* re_im);                                    /* :138 */
+int qsg_set_ampl(qsg_ctx* ctx, float* state, unsigned n, uint64_t i,
+                 float re, float im);                              /* :150 */
+/* BulkSetAmpl (:168-187): state[i] = re+i*im where ((i & mask) == bits)
+ * XOR exclude. */
+int qsg_bulk_set_ampl(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                      uint64_t bits, float re, float im, int exclude);
+/* Add (:190-205): dest += src. */
+int qsg_add(qsg_ctx* ctx, const float* src, float* dest, unsigned n);
+/* Multiply (:208-217): state *= a. */
+int qsg_multiply(qsg_ctx* ctx, float a, float* state, unsigned n);
+/* InnerProduct (:219-229): sum conj(s1[i]) * s2[i] in FP64 -> out[2]. */
+int qsg_inner_product(qsg_ctx* ctx, const float* s1, const float* s2,
+                      unsigned n, double* out_re_im);
+/* RealInnerProduct (:231-237). */
+int qsg_real_inner_product(qsg_ctx* ctx, const float* s1, const float* s2,
+                           unsigned n, double* out);
+/* Norm (:239-241): sum |s[i]|^2 in FP64. */
+int qsg_norm(qsg_ctx* ctx, const float* state, unsigned n, double* out);
+/* PartialNorms (:331-355).  The state is cut into qsg_num_chunks(n) equal
+ * chunks of consecutive amplitudes; out[m] = sum of |s[i]|^2 over chunk m.
+ * `out` must hold qsg_num_chunks(n) doubles. */
+uint64_t qsg_num_chunks(unsigned n);
+int qsg_partial_norms(qsg_ctx* ctx, const float* state, unsigned n,
+                      double* out);
+/* FindMeasuredBits (:357-373): first index k of chunk m at which the running
+ * sum of |s|^2 inside the chunk exceeds r, masked by `mask` (last index of
+ * the chunk if none). */
+int qsg_find_measured_bits(qsg_ctx* ctx, const float* state, unsigned n,
+                           uint64_t m, double r, uint64_t mask,
+                           uint64_t* out);
+/* Sample (:243-312).  `sorted_u` holds num_samples uniforms in [0,1), sorted
+ * ascending (the host-side mt19937 draws of GenerateRandomValues,
+ * lib/util.h:67-85, divided by their max_value).  The device forms
+ * r_j = u_j * Norm and returns, per j, the first index k whose inclusive
+ * running sum of |s|^2 exceeds r_j (2^n - 1 if none, as
+ * lib/statespace_basic.h:222-224). */
+int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
+                      uint64_t num_samples, const double* sorted_u,
+                      uint64_t* out_bitstrings);
+/* Sample with the reference's RNG convention: std::mt19937(seed) +
+ * uniform_real_distribution<double>(0, norm), sorted (lib/util.h:67-85). */
+int qsg_sample(qsg_ctx* ctx, const float* state, unsigned n,
+               uint64_t num_samples, unsigned seed, uint64_t* out_bitstrings);
+/* Collapse (:316-329): zero amplitudes with (i & mask) != bits and scale the
+ * rest by (float)(1/sqrt(masked norm)). */
+int qsg_collapse(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                 uint64_t bits);
+/* VirtualMeasure + Collapse (lib/statespace.h:84-140) fused on the device:
+ * r = u * Norm, the index k found as in FindMeasuredBits over the whole
+ * state, bits = k & mask; when `collapse` is set the state is collapsed on
+ * bits.  `u` is the uniform in [0,1) the caller's generator produced. */
+int qsg_measure(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                double u, int collapse, uint64_t* out_bits);
+
+/* ---- simulator (lib/simulator_cuda.h) ---------------------------------- */
+/* ApplyGate (:70-125): in-place v <- M v on target qubits qs[0..k), k <= 6. */
+int qsg_apply_gate(qsg_ctx* ctx, float* state, unsigned n,
+                   const unsigned* qs, unsigned k, const float* matrix);
+/* ApplyControlledGate (:135-207): apply M on qs where the control qubits
+ * cqs[0..c) (sorted) take the values of cvals (bit i <-> cqs[i]); k <= 6. */
+int qsg_apply_controlled_gate(qsg_ctx* ctx, float* state, unsigned n,
+                              const unsigned* qs, unsigned k,
+                              const unsigned* cqs, unsigned c, uint64_t cvals,
+                              const float* matrix);
+/* ExpectationValue (:216-260): <s| M_qs |s> in FP64 -> out_re_im[2]. */
+int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
+                          const unsigned* qs, unsigned k, const float* matrix,
+                          double* out_re_im);
+/* SIMDRegisterSize (:265-267). */
+unsigned qsg_simd_register_size(void);
+
+/* ---- host random numbers ------------------------------------------------
+ * std::mt19937 + uniform_real_distribution<double>, the generators of
+ * lib/util.h:61-85 (RandomValue, GenerateRandomValues) and of
+ * QuantumTrajectorySimulator (lib/qtrajectory.h:268-302). */
+typedef struct qsg_rng qsg_rng;
+qsg_rng* qsg_rng_create(unsigned seed);
+void qsg_rng_destroy(qsg_rng* rng);
+uint32_t qsg_rng_next_u32(qsg_rng* rng);
+/* uniform_real_distribution<double>(0, max_value)(rng) */
+double qsg_rng_uniform(qsg_rng* rng, double max_value);
+/* GenerateRandomValues (lib/util.h:67-85) without the sentinel: `num` sorted
+ * draws of uniform_real_distribution<double>(0, max_value) from
+ * std::mt19937(seed). */
+void qsg_generate_random_values(uint64_t num, unsigned seed, double max_value,
+                                double* out);
+
+/* ---- timing ------------------------------------------------------------ */
+/* CUDA-event timing on the context stream: qsg_timer_start records an event,
+ * qsg_timer_stop records a second one, synchronises and returns the elapsed
+ * milliseconds. */
+int qsg_timer_start(qsg_ctx* ctx);
+int qsg_timer_stop(qsg_ctx* ctx, float* ms);
+/* Number of kernels this library launched on the context so far. */
+uint64_t qsg_ctx_launch_count(qsg_ctx* ctx);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* QSIM_GB300_H_ */

@@ -1,0 +1,273 @@
+// ref_driver.cc — TEST INFRASTRUCTURE ONLY (builds into oracle/_ref/).
+//
+// Runs the reference implementation (quantumlib/qsim, header-only C++) on
+// gate lists written by tests/golden/make_golden.py and writes its outputs
+// as raw binary files, which become the golden fixtures under tests/golden/.
+// Compiled against the reference headers where they lie (-I<qsim>/lib); no
+// reference source is copied.
+//
+// Gate-list format (one op per line, matrices as C99 hex floats, qubits
+// sorted ascending and the matrix already in that order):
+//   n <num_qubits>
+//   g <time> <k> <q...> <2*4^k floats>                 matrix gate
+//   c <time> <k> <q...> <c> <cq...> <cvals> <floats>   controlled gate
+//   m <time> <k> <q...>                                measurement
+//
+// Commands:
+//   mt <seed> <count> <out>
+//       raw std::mt19937 outputs (uint32) then `count` draws of
+//       uniform_real_distribution<double>(0,1) from a fresh mt19937(seed).
+//   run <gates> <out-prefix> <max_fused_size> <num_samples> <sample_seed>
+//       [<ev-file>]
+//       .f64  : final state of SimulatorBasic<For,double>, ops unfused
+//       .f32  : final state of QSimRunner + MultiQubitGateFuser +
+//               the host's SIMD simulator (float)
+//       .s32  : Sample(f32 state, num_samples, seed)
+//       .s64  : Sample(f64 state, num_samples, seed)
+//       .ev   : per EV line: <k> <q...> <floats> -> complex<double> on the
+//               f32 state (SIMD) then on the f64 state (basic)
+//       .meta : norm, number of fused ops
+//   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
+//       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
+//       with one std::mt19937(seed); writes bits per round (.bits) and the
+//       collapsed state after the last round (.f64).
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <random>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "circuit.h"
+#include "formux.h"
+#include "fuser_mqubit.h"
+#include "gate.h"
+#include "gate_appl.h"
+#include "gates_qsim.h"
+#include "io.h"
+#include "operation.h"
+#include "run_qsim.h"
+#include "simmux.h"
+#include "simulator_basic.h"
+#include "statespace_basic.h"
+
+using namespace qsim;
+
+struct GateSpec {
+  char kind;
+  unsigned time;
+  std::vector<unsigned> qs, cqs;
+  uint64_t cvals = 0;
+  std::vector<float> m;
+};
+
+static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
+  std::ifstream f(path);
+  std::string line;
+  std::vector<GateSpec> out;
+  while (std::getline(f, line)) {
+    std::istringstream ss(line);
+    std::string tag;
+    ss >> tag;
+    if (tag == "n") {
+      ss >> n;
+      continue;
+    }
+    GateSpec g;
+    g.kind = tag[0];
+    unsigned k;
+    ss >> g.time >> k;
+    g.qs.resize(k);
+    for (auto& q : g.qs) ss >> q;
+    if (g.kind == 'c') {
+      unsigned c;
+      ss >> c;
+      g.cqs.resize(c);
+      for (auto& q : g.cqs) ss >> q;
+      ss >> g.cvals;
+    }
+    if (g.kind != 'm') {
+      size_t cnt = 2u << (2 * k);
+      g.m.resize(cnt);
+      for (auto& x : g.m) {
+        std::string t;
+        ss >> t;
+        x = std::strtof(t.c_str(), nullptr);
+      }
+    }
+    out.push_back(std::move(g));
+  }
+  return out;
+}
+
+template <typename FP>
+static Operation<FP> ToOp(const GateSpec& g) {
+  if (g.kind == 'm') return CreateMeasurement(g.time, g.qs);
+  Gate<FP> gate;
+  gate.kind = kGateMatrix1;
+  gate.time = g.time;
+  gate.qubits = g.qs;
+  gate.matrix.assign(g.m.begin(), g.m.end());
+  gate.swapped = false;
+  if (g.kind == 'c') {
+    return ControlledGate<FP>{gate, g.cqs, g.cvals};
+  }
+  return gate;
+}
+
+static void WriteRaw(const std::string& path, const void* p, size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  std::fwrite(p, 1, bytes, f);
+  std::fclose(f);
+}
+
+static int CmdMt(int argc, char** argv) {
+  unsigned seed = std::atoi(argv[2]);
+  unsigned count = std::atoi(argv[3]);
+  std::mt19937 g(seed);
+  std::vector<uint32_t> raw(count);
+  for (auto& x : raw) x = g();
+  std::mt19937 g2(seed);
+  std::uniform_real_distribution<double> d(0.0, 1.0);
+  std::vector<double> u(count);
+  for (auto& x : u) x = d(g2);
+  std::string out = argv[4];
+  WriteRaw(out + ".raw", raw.data(), raw.size() * 4);
+  WriteRaw(out + ".u01", u.data(), u.size() * 8);
+  return 0;
+}
+
+struct Factory32 {
+  using Simulator = qsim::Simulator<For>;
+  using StateSpace = Simulator::StateSpace;
+  StateSpace CreateStateSpace() const { return StateSpace(1); }
+  Simulator CreateSimulator() const { return Simulator(1); }
+};
+
+static int CmdRun(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  std::string out = argv[3];
+  unsigned fsize = std::atoi(argv[4]);
+  uint64_t nsamples = std::strtoull(argv[5], nullptr, 10);
+  unsigned sseed = std::atoi(argv[6]);
+
+  // FP64, unfused: the reference's own FP64 oracle.
+  using Sim64 = SimulatorBasic<For, double>;
+  using SS64 = Sim64::StateSpace;
+  SS64 ss64(1);
+  Sim64 sim64(1);
+  auto s64 = ss64.Create(n);
+  ss64.SetStateZero(s64);
+  for (const auto& g : specs) {
+    auto op = ToOp<double>(g);
+    ApplyGate(sim64, op, s64);
+  }
+  WriteRaw(out + ".f64", s64.get(), sizeof(double) * SS64::MinSize(n));
+
+  // FP32 through QSimRunner + MultiQubitGateFuser + SIMD simulator.
+  Circuit<Operation<float>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<float>(g));
+  using Runner = QSimRunner<IO, MultiQubitGateFuser<IO>, Factory32>;
+  Runner::Parameter param;
+  param.max_fused_size = fsize;
+  param.seed = 1;
+  param.verbosity = 0;
+  Factory32 factory;
+  auto ss32 = factory.CreateStateSpace();
+  auto sim32 = factory.CreateSimulator();
+  auto s32 = ss32.Create(n);
+  ss32.SetStateZero(s32);
+  if (!Runner::Run(param, factory, circuit, s32)) {
+    std::fprintf(stderr, "run failed\n");
+    return 1;
+  }
+  ss32.InternalToNormalOrder(s32);
+  WriteRaw(out + ".f32", s32.get(), sizeof(float) * 2 * (uint64_t{1} << n));
+  ss32.NormalToInternalOrder(s32);
+
+  auto fused = MultiQubitGateFuser<IO>::FuseGates(
+      MultiQubitGateFuser<IO>::Parameter{fsize, 0}, n, circuit.ops);
+
+  if (nsamples > 0) {
+    auto b32 = ss32.Sample(s32, nsamples, sseed);
+    WriteRaw(out + ".s32", b32.data(), b32.size() * 8);
+    auto b64 = ss64.Sample(s64, nsamples, sseed);
+    WriteRaw(out + ".s64", b64.data(), b64.size() * 8);
+  }
+
+  if (argc > 7) {
+    std::ifstream f(argv[7]);
+    std::string line;
+    std::vector<double> evs;
+    while (std::getline(f, line)) {
+      std::istringstream ss(line);
+      unsigned k;
+      if (!(ss >> k)) continue;
+      std::vector<unsigned> qs(k);
+      for (auto& q : qs) ss >> q;
+      std::vector<float> m32(2u << (2 * k));
+      for (auto& x : m32) {
+        std::string t;
+        ss >> t;
+        x = std::strtof(t.c_str(), nullptr);
+      }
+      std::vector<double> m64(m32.begin(), m32.end());
+      auto e32 = sim32.ExpectationValue(qs, m32.data(), s32);
+      auto e64 = sim64.ExpectationValue(qs, m64.data(), s64);
+      evs.push_back(e32.real());
+      evs.push_back(e32.imag());
+      evs.push_back(e64.real());
+      evs.push_back(e64.imag());
+    }
+    WriteRaw(out + ".ev", evs.data(), evs.size() * 8);
+  }
+
+  double meta[2] = {ss64.Norm(s64), double(fused.size())};
+  WriteRaw(out + ".meta", meta, sizeof(meta));
+  return 0;
+}
+
+static int CmdMeasure(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  std::string out = argv[3];
+  unsigned seed = std::atoi(argv[4]);
+  unsigned reps = std::atoi(argv[5]);
+  unsigned k = std::atoi(argv[6]);
+  std::vector<unsigned> qs(k);
+  for (unsigned i = 0; i < k; ++i) qs[i] = std::atoi(argv[7 + i]);
+
+  using Sim64 = SimulatorBasic<For, double>;
+  using SS64 = Sim64::StateSpace;
+  SS64 ss64(1);
+  Sim64 sim64(1);
+  auto s64 = ss64.Create(n);
+  ss64.SetStateZero(s64);
+  for (const auto& g : specs) {
+    auto op = ToOp<double>(g);
+    ApplyGate(sim64, op, s64);
+  }
+  std::mt19937 rgen(seed);
+  std::vector<uint64_t> bits;
+  for (unsigned r = 0; r < reps; ++r) {
+    auto res = ss64.Measure(qs, rgen, s64);
+    bits.push_back(res.valid ? res.bits : ~uint64_t{0});
+  }
+  WriteRaw(out + ".bits", bits.data(), bits.size() * 8);
+  WriteRaw(out + ".f64", s64.get(), sizeof(double) * SS64::MinSize(n));
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2) return 2;
+  std::string cmd = argv[1];
+  if (cmd == "mt") return CmdMt(argc, argv);
+  if (cmd == "run") return CmdRun(argc, argv);
+  if (cmd == "measure") return CmdMeasure(argc, argv);
+  return 2;
+}

@@ -1,0 +1,99 @@
+"""ctypes binding of libqsim_gb300.so (the C ABI declared in
+include/qsim_gb300.h).  There is no fallback: if the library is missing,
+importing this module raises."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libqsim_gb300.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with `python -m qsim_gb300.build` "
+        "(nvcc, sm_103a). The engine has no CPU fallback.")
+
+lib = C.CDLL(LIB_PATH)
+
+u32, u64, i32 = C.c_uint, C.c_uint64, C.c_int
+f32, f64 = C.c_float, C.c_double
+vp = C.c_void_p
+P_u32 = C.POINTER(C.c_uint)
+P_u64 = C.POINTER(C.c_uint64)
+P_f32 = C.POINTER(C.c_float)
+P_f64 = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "qsg_last_error": (C.c_char_p, []),
+    "qsg_version": (C.c_char_p, []),
+    "qsg_ctx_create": (i32, [i32, vp, C.POINTER(vp)]),
+    "qsg_ctx_destroy": (i32, [vp]),
+    "qsg_ctx_sync": (i32, [vp]),
+    "qsg_ctx_num_sms": (i32, [vp, C.POINTER(C.c_int)]),
+    "qsg_ctx_stream": (vp, [vp]),
+    "qsg_ctx_launch_count": (u64, [vp]),
+    "qsg_min_size": (u64, [u32]),
+    "qsg_state_create": (i32, [vp, u32, C.POINTER(vp)]),
+    "qsg_state_free": (i32, [vp, vp]),
+    "qsg_copy_d2d": (i32, [vp, vp, vp, u32]),
+    "qsg_copy_d2h": (i32, [vp, vp, vp, u32]),
+    "qsg_copy_h2d": (i32, [vp, vp, vp, u32]),
+    "qsg_copy_h2d_partial": (i32, [vp, vp, vp, u64, u32]),
+    "qsg_internal_to_normal": (i32, [vp, vp, u32]),
+    "qsg_normal_to_internal": (i32, [vp, vp, u32]),
+    "qsg_set_all_zeros": (i32, [vp, vp, u32]),
+    "qsg_set_state_uniform": (i32, [vp, vp, u32]),
+    "qsg_set_state_zero": (i32, [vp, vp, u32]),
+    "qsg_get_ampl": (i32, [vp, vp, u32, u64, P_f32]),
+    "qsg_set_ampl": (i32, [vp, vp, u32, u64, f32, f32]),
+    "qsg_bulk_set_ampl": (i32, [vp, vp, u32, u64, u64, f32, f32, i32]),
+    "qsg_add": (i32, [vp, vp, vp, u32]),
+    "qsg_multiply": (i32, [vp, f32, vp, u32]),
+    "qsg_inner_product": (i32, [vp, vp, vp, u32, P_f64]),
+    "qsg_real_inner_product": (i32, [vp, vp, vp, u32, P_f64]),
+    "qsg_norm": (i32, [vp, vp, u32, P_f64]),
+    "qsg_num_chunks": (u64, [u32]),
+    "qsg_partial_norms": (i32, [vp, vp, u32, P_f64]),
+    "qsg_find_measured_bits": (i32, [vp, vp, u32, u64, f64, u64, P_u64]),
+    "qsg_sample_sorted": (i32, [vp, vp, u32, u64, P_f64, P_u64]),
+    "qsg_sample": (i32, [vp, vp, u32, u64, u32, P_u64]),
+    "qsg_collapse": (i32, [vp, vp, u32, u64, u64]),
+    "qsg_measure": (i32, [vp, vp, u32, u64, f64, i32, P_u64]),
+    "qsg_apply_gate": (i32, [vp, vp, u32, P_u32, u32, P_f32]),
+    "qsg_apply_controlled_gate": (i32, [vp, vp, u32, P_u32, u32, P_u32, u32,
+                                        u64, P_f32]),
+    "qsg_expectation_value": (i32, [vp, vp, u32, P_u32, u32, P_f32, P_f64]),
+    "qsg_simd_register_size": (u32, []),
+    "qsg_rng_create": (vp, [u32]),
+    "qsg_rng_destroy": (None, [vp]),
+    "qsg_rng_next_u32": (u32, [vp]),
+    "qsg_rng_uniform": (f64, [vp, f64]),
+    "qsg_generate_random_values": (None, [u64, u32, f64, P_f64]),
+    "qsg_timer_start": (i32, [vp]),
+    "qsg_timer_stop": (i32, [vp, P_f32]),
+}
+
+for _name, (_res, _args) in SIGNATURES.items():
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+class QsgError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise QsgError(status, lib.qsg_last_error().decode())
+
+
+def u32_array(xs):
+    xs = list(xs)
+    return (C.c_uint * max(1, len(xs)))(*xs)

@@ -1,0 +1,788 @@
+// State-space kernels: initialisation, elementwise ops, FP64 reductions,
+// chunked CDF scans for Sample / Measure, and Collapse.
+//
+// Replaces StateSpaceCUDA (lib/statespace_cuda.h:109-373) and its kernels
+// (lib/statespace_cuda_kernels.h:181-351).  The reference samples with a
+// single thread scanning all 2^n amplitudes (SampleKernel, :301-326); here
+// the state is cut into chunks of 2^13 amplitudes, chunk sums are scanned on
+// the device, and one CTA per chunk that holds samples resolves them with a
+// block-wide scan and binary searches.  Every reduction runs in FP64 with a
+// fixed partition, so results are deterministic for a given n and GPU.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "common.cuh"
+#include "matring.cuh"
+
+namespace qsg {
+
+constexpr int kRedThreads = 256;
+constexpr unsigned kChunkBits = 13;              // amplitudes per chunk 2^13
+constexpr int kScanThreads = 256;
+constexpr int kAmpsPerScanThread = 32;           // 256 * 32 = 8192
+
+inline unsigned chunk_bits(unsigned n) { return n < kChunkBits ? n : kChunkBits; }
+inline uint64_t num_chunks(unsigned n) { return uint64_t{1} << (n - chunk_bits(n)); }
+
+// ---------------------------------------------------------------------------
+// Elementwise kernels (grid-stride over float4 units = two amplitudes).
+
+__global__ void fill_zero_kernel(float4* s, uint64_t units) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x)
+    s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void set_one_kernel(float* s) { s[0] = 1.f; s[1] = 0.f; }
+
+__global__ void uniform_kernel(float4* s, uint64_t units, uint64_t namps,
+                               float v) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float a0 = 2 * i < namps ? v : 0.f;
+    float a1 = 2 * i + 1 < namps ? v : 0.f;
+    s[i] = make_float4(a0, 0.f, a1, 0.f);
+  }
+}
+
+__global__ void bulk_set_kernel(float2* s, uint64_t namps, uint64_t mask,
+                                uint64_t bits, float re, float im,
+                                bool exclude) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < namps;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    bool set = ((i & mask) == bits) ^ exclude;
+    if (set) s[i] = make_float2(re, im);
+  }
+}
+
+__global__ void add_kernel(const float4* __restrict__ a, float4* __restrict__ b,
+                           uint64_t units) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float4 x = a[i], y = b[i];
+    b[i] = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+  }
+}
+
+__global__ void multiply_kernel(float4* s, uint64_t units, float a) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float4 x = s[i];
+    s[i] = make_float4(x.x * a, x.y * a, x.z * a, x.w * a);
+  }
+}
+
+__global__ void collapse_kernel(float4* s, uint64_t units, uint64_t mask,
+                                uint64_t bits, float renorm) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float4 x = s[i];
+    bool k0 = ((2 * i) & mask) == bits;
+    bool k1 = ((2 * i + 1) & mask) == bits;
+    s[i] = make_float4(k0 ? x.x * renorm : 0.f, k0 ? x.y * renorm : 0.f,
+                       k1 ? x.z * renorm : 0.f, k1 ? x.w * renorm : 0.f);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 reductions.  OP 0: sum |s1|^2 (masked), 1: Re<s1|s2>, 2: <s1|s2>.
+
+template <int OP>
+__global__ void __launch_bounds__(kRedThreads)
+    reduce_kernel(const float4* __restrict__ s1, const float4* __restrict__ s2,
+                  uint64_t units, uint64_t mask, uint64_t bits,
+                  double2* __restrict__ partial) {
+  double ar = 0, ai = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(kRedThreads) + threadIdx.x;
+       i < units; i += uint64_t(gridDim.x) * kRedThreads) {
+    float4 x = s1[i];
+    if constexpr (OP == 0) {
+      double p0 = double(x.x) * x.x + double(x.y) * x.y;
+      double p1 = double(x.z) * x.z + double(x.w) * x.w;
+      if (mask == 0) {
+        ar += p0 + p1;
+      } else {
+        if (((2 * i) & mask) == bits) ar += p0;
+        if (((2 * i + 1) & mask) == bits) ar += p1;
+      }
+    } else {
+      float4 y = s2[i];
+      ar += double(x.x) * y.x + double(x.y) * y.y + double(x.z) * y.z +
+            double(x.w) * y.w;
+      if constexpr (OP == 2) {
+        ai += double(x.x) * y.y - double(x.y) * y.x + double(x.z) * y.w -
+              double(x.w) * y.z;
+      }
+    }
+  }
+  __shared__ double red[2][kRedThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, o);
+    ai += __shfl_down_sync(0xffffffffu, ai, o);
+  }
+  if (threadIdx.x % 32 == 0) {
+    red[0][threadIdx.x / 32] = ar;
+    red[1][threadIdx.x / 32] = ai;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sr = 0, si = 0;
+    for (int i = 0; i < kRedThreads / 32; ++i) {
+      sr += red[0][i];
+      si += red[1][i];
+    }
+    partial[blockIdx.x] = make_double2(sr, si);
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+    final_reduce_kernel(const double2* __restrict__ partial, uint64_t count,
+                        double2* __restrict__ out) {
+  double ar = 0, ai = 0;
+  for (uint64_t i = threadIdx.x; i < count; i += blockDim.x) {
+    ar += partial[i].x;
+    ai += partial[i].y;
+  }
+  __shared__ double red[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, o);
+    ai += __shfl_down_sync(0xffffffffu, ai, o);
+  }
+  if (threadIdx.x % 32 == 0) {
+    red[0][threadIdx.x / 32] = ar;
+    red[1][threadIdx.x / 32] = ai;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sr = 0, si = 0;
+    for (unsigned i = 0; i < blockDim.x / 32; ++i) {
+      sr += red[0][i];
+      si += red[1][i];
+    }
+    *out = make_double2(sr, si);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Chunk scans.  A chunk is 2^cb consecutive amplitudes; thread t of the CTA
+// owns amplitudes [t*32, t*32+32) of it.  chunk_scan() computes, in a fixed
+// order, the per-thread sequential sums and the block-exclusive prefix of
+// those sums; the chunk total it returns is bit-identical in every kernel
+// that calls it, so CDF positions found in different kernels agree.
+
+struct ChunkScan {
+  double thread_prefix;  // sum of all earlier threads' amplitudes
+  double total;          // chunk total
+};
+
+__device__ __forceinline__ double prob(float2 a) {
+  return double(a.x) * a.x + double(a.y) * a.y;
+}
+
+__device__ ChunkScan chunk_scan(const float2* __restrict__ chunk,
+                                uint32_t camps, double* local /*[32] or null*/) {
+  __shared__ double wsum[kScanThreads / 32];
+  __shared__ double tot;
+  const uint32_t t = threadIdx.x;
+  double s = 0;
+  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
+  for (uint32_t j = 0; j < per; ++j) {
+    uint32_t i = t * per + j;
+    double p = i < camps ? prob(chunk[i]) : 0.0;
+    s += p;
+    if (local) local[j] = s;
+  }
+  // Inclusive warp scan of s, then the exclusive value by a shuffle.
+  double x = s;
+  const int lane = t % 32, w = t / 32;
+  for (int o = 1; o < 32; o <<= 1) {
+    double y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  double xe = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane == 0) xe = 0.0;
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (t == 0) {
+    double acc = 0;
+    for (int i = 0; i < kScanThreads / 32; ++i) {
+      double v = wsum[i];
+      wsum[i] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  ChunkScan r;
+  r.thread_prefix = wsum[w] + xe;
+  // The chunk total is the last element of the scan as the search kernels
+  // form it (prefix + own running sum), so both agree to the bit.
+  if (t == kScanThreads - 1) tot = r.thread_prefix + s;
+  __syncthreads();
+  r.total = tot;
+  __syncthreads();
+  return r;
+}
+
+// out[m] = total of chunk m.
+__global__ void __launch_bounds__(kScanThreads)
+    chunk_sum_kernel(const float2* __restrict__ s, uint32_t cb,
+                     uint64_t nchunks, double* __restrict__ out) {
+  for (uint64_t m = blockIdx.x; m < nchunks; m += gridDim.x) {
+    ChunkScan cs = chunk_scan(s + (m << cb), 1u << cb, nullptr);
+    if (threadIdx.x == 0) out[m] = cs.total;
+  }
+}
+
+// Inclusive prefix over chunk totals (one CTA, fixed order):
+// incl[m] = sum_{j<=m} sums[j].
+__global__ void __launch_bounds__(1024)
+    chunk_prefix_kernel(const double* __restrict__ sums, uint64_t nchunks,
+                        double* __restrict__ incl) {
+  __shared__ double ws[32];
+  const uint64_t per = (nchunks + blockDim.x - 1) / blockDim.x;
+  const uint64_t beg = threadIdx.x * per;
+  double s = 0;
+  for (uint64_t j = 0; j < per; ++j) {
+    uint64_t i = beg + j;
+    if (i < nchunks) s += sums[i];
+  }
+  double x = s;
+  const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+  for (int o = 1; o < 32; o <<= 1) {
+    double y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double acc = 0;
+    for (unsigned i = 0; i < blockDim.x / 32; ++i) {
+      double v = ws[i];
+      ws[i] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  double run = ws[w] + (x - s);
+  for (uint64_t j = 0; j < per; ++j) {
+    uint64_t i = beg + j;
+    if (i < nchunks) {
+      run += sums[i];
+      incl[i] = run;
+    }
+  }
+}
+
+// r[j] = u[j] * total, total = incl[nchunks-1].
+__global__ void scale_uniforms_kernel(const double* __restrict__ u,
+                                      uint64_t m, const double* __restrict__ incl,
+                                      uint64_t nchunks, double* __restrict__ r) {
+  const double total = incl[nchunks - 1];
+  for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < m;
+       j += uint64_t(gridDim.x) * blockDim.x)
+    r[j] = u[j] * total;
+}
+
+// First j in [0, m) with r[j] >= x (r sorted ascending).
+__device__ __forceinline__ uint64_t lower_bound_d(const double* r, uint64_t m,
+                                                  double x) {
+  uint64_t lo = 0, hi = m;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) / 2;
+    if (r[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Resolves the samples that fall into each chunk.  Sample j belongs to
+// chunk m iff incl[m-1] <= r[j] < incl[m]; inside the chunk its index is the
+// first k with r[j] < incl[m-1] + (inclusive scan at k).  Samples with
+// r[j] >= incl[last] get 2^n - 1.
+__global__ void __launch_bounds__(kScanThreads)
+    sample_chunk_kernel(const float2* __restrict__ s, uint32_t cb,
+                        uint64_t nchunks, const double* __restrict__ incl,
+                        const double* __restrict__ r, uint64_t m,
+                        uint64_t last_index, uint64_t* __restrict__ out) {
+  extern __shared__ double scan[];  // 2^cb inclusive in-chunk scan
+  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const double lo_v = c == 0 ? -1.0 : incl[c - 1];
+    const double hi_v = incl[c];
+    const uint64_t lo = c == 0 ? 0 : lower_bound_d(r, m, lo_v);
+    const uint64_t hi = lower_bound_d(r, m, hi_v);
+    if (c == nchunks - 1) {
+      for (uint64_t j = hi + threadIdx.x; j < m; j += blockDim.x)
+        out[j] = last_index;
+    }
+    if (lo >= hi) continue;  // uniform across the block
+    const uint32_t camps = 1u << cb;
+    double local[kAmpsPerScanThread];
+    ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
+    const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
+    const double base = c == 0 ? 0.0 : incl[c - 1];
+    for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
+      uint32_t i = threadIdx.x * per + j;
+      if (i < camps) scan[i] = base + (cs.thread_prefix + local[j]);
+    }
+    __syncthreads();
+    for (uint64_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
+      const double x = r[j];
+      uint32_t a = 0, b = camps;  // first k with x < scan[k]
+      while (a < b) {
+        uint32_t mid = (a + b) / 2;
+        if (!(x < scan[mid])) a = mid + 1; else b = mid;
+      }
+      if (a >= camps) a = camps - 1;
+      out[j] = (c << cb) + a;
+    }
+    __syncthreads();
+  }
+}
+
+// FindMeasuredBits: first k of chunk c with r < in-chunk inclusive scan[k]
+// (last index of the chunk if none); masked.
+__global__ void __launch_bounds__(kScanThreads)
+    find_in_chunk_kernel(const float2* __restrict__ s, uint32_t cb, uint64_t c,
+                         double r, uint64_t mask, uint64_t* __restrict__ out) {
+  const uint32_t camps = 1u << cb;
+  double local[kAmpsPerScanThread];
+  ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
+  __shared__ unsigned long long best;
+  if (threadIdx.x == 0) best = ~0ull;
+  __syncthreads();
+  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
+  for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
+    uint32_t i = threadIdx.x * per + j;
+    if (i < camps && r < cs.thread_prefix + local[j]) {
+      atomicMin(&best, (unsigned long long)i);
+      break;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t k = best == ~0ull ? camps - 1 : best;
+    *out = ((c << cb) + k) & mask;
+  }
+}
+
+// Measure on the device: r = u * total; chunk c = first with r <= incl[c]
+// (the reference's `while (r > partial_norms[m]) ++m`), r -= incl[c-1], then
+// the in-chunk search of FindMeasuredBits.
+__global__ void __launch_bounds__(kScanThreads)
+    measure_kernel(const float2* __restrict__ s, uint32_t cb, uint64_t nchunks,
+                   const double* __restrict__ incl, double u, uint64_t mask,
+                   uint64_t* __restrict__ out) {
+  __shared__ uint64_t sc;
+  __shared__ double sr;
+  if (threadIdx.x == 0) {
+    double total = incl[nchunks - 1];
+    double r = u * total;
+    uint64_t lo = 0, hi = nchunks - 1;  // first c with r <= incl[c]
+    while (lo < hi) {
+      uint64_t mid = (lo + hi) / 2;
+      if (r > incl[mid]) lo = mid + 1; else hi = mid;
+    }
+    sc = lo;
+    sr = lo > 0 ? r - incl[lo - 1] : r;
+  }
+  __syncthreads();
+  const uint64_t c = sc;
+  const double r = sr;
+  const uint32_t camps = 1u << cb;
+  double local[kAmpsPerScanThread];
+  ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
+  __shared__ unsigned long long best;
+  if (threadIdx.x == 0) best = ~0ull;
+  __syncthreads();
+  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
+  for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
+    uint32_t i = threadIdx.x * per + j;
+    if (i < camps && r < cs.thread_prefix + local[j]) {
+      atomicMin(&best, (unsigned long long)i);
+      break;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t k = best == ~0ull ? camps - 1 : best;
+    *out = ((c << cb) + k) & mask;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host helpers.
+
+static unsigned grid_for(qsg_ctx* ctx, uint64_t work, int threads) {
+  uint64_t g = (work + threads - 1) / threads;
+  uint64_t cap = uint64_t(ctx->num_sms) * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+static inline uint64_t units_of(unsigned n) {
+  return n == 0 ? 1 : (uint64_t{1} << (n - 1));
+}
+
+int reduce_partials_d2(qsg_ctx* ctx, const double2* partial, uint64_t count,
+                       double* out_re_im) {
+  double2* dres = const_cast<double2*>(partial) + count;  // scratch tail
+  final_reduce_kernel<<<1, 1024, 0, ctx->stream>>>(partial, count, dres);
+  QSG_LAUNCHED(ctx);
+  void* h = nullptr;
+  int rc = get_hscratch(ctx, sizeof(double2), &h);
+  if (rc) return rc;
+  QSG_CUDA(cudaMemcpyAsync(h, dres, sizeof(double2), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(out_re_im, h, sizeof(double2));
+  return QSG_OK;
+}
+
+template <int OP>
+static int reduce(qsg_ctx* ctx, const float* s1, const float* s2, unsigned n,
+                  uint64_t mask, uint64_t bits, double* out) {
+  const uint64_t units = units_of(n);
+  const unsigned grid = grid_for(ctx, units, kRedThreads * 4);
+  void* p = nullptr;
+  int rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
+  if (rc) return rc;
+  double2* partial = static_cast<double2*>(p);
+  reduce_kernel<OP><<<grid, kRedThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float4*>(s1), reinterpret_cast<const float4*>(s2),
+      units, mask, bits, partial);
+  QSG_LAUNCHED(ctx);
+  return reduce_partials_d2(ctx, partial, grid, out);
+}
+
+// Chunk sums + inclusive prefix into scratch: returns pointers.
+static int chunk_prefix(qsg_ctx* ctx, const float* s, unsigned n,
+                        size_t extra_bytes, double** sums, double** incl,
+                        void** extra) {
+  const uint64_t nc = num_chunks(n);
+  void* p = nullptr;
+  size_t bytes = 2 * nc * sizeof(double) + extra_bytes + 256;
+  int rc = get_scratch(ctx, bytes, &p);
+  if (rc) return rc;
+  *sums = static_cast<double*>(p);
+  *incl = *sums + nc;
+  if (extra) *extra = reinterpret_cast<char*>(*incl + nc);
+  const unsigned grid = (unsigned)std::min<uint64_t>(nc, 65535ull * 16);
+  chunk_sum_kernel<<<grid, kScanThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float2*>(s), chunk_bits(n), nc, *sums);
+  QSG_LAUNCHED(ctx);
+  chunk_prefix_kernel<<<1, 1024, 0, ctx->stream>>>(*sums, nc, *incl);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+void matring_release(qsg_ctx* ctx) {
+  for (int i = 0; i < qsg_ctx::kRingSlots; ++i) {
+    if (ctx->ring_ev[i]) cudaEventDestroy(ctx->ring_ev[i]);
+    ctx->ring_ev[i] = nullptr;
+  }
+  if (ctx->ring_dev) cudaFree(ctx->ring_dev);
+  if (ctx->ring_host) cudaFreeHost(ctx->ring_host);
+  ctx->ring_dev = nullptr;
+  ctx->ring_host = nullptr;
+}
+
+int matring_upload(qsg_ctx* ctx, const float* host_matrix, size_t nfloats,
+                   const float** dev) {
+  if (nfloats > qsg_ctx::kRingSlotFloats) {
+    set_error("matrix too large for the upload ring");
+    return QSG_ERR_INVALID;
+  }
+  if (!ctx->ring_dev) {
+    const size_t bytes =
+        qsg_ctx::kRingSlots * qsg_ctx::kRingSlotFloats * sizeof(float);
+    QSG_CUDA(cudaMalloc(&ctx->ring_dev, bytes));
+    QSG_CUDA(cudaMallocHost(&ctx->ring_host, bytes));
+    for (int i = 0; i < qsg_ctx::kRingSlots; ++i) {
+      QSG_CUDA(cudaEventCreateWithFlags(&ctx->ring_ev[i],
+                                        cudaEventDisableTiming));
+    }
+  }
+  const int slot = ctx->ring_next;
+  ctx->ring_next = (slot + 1) % qsg_ctx::kRingSlots;
+  if (ctx->ring_used[slot]) QSG_CUDA(cudaEventSynchronize(ctx->ring_ev[slot]));
+  float* h = ctx->ring_host + slot * qsg_ctx::kRingSlotFloats;
+  float* d = ctx->ring_dev + slot * qsg_ctx::kRingSlotFloats;
+  std::memcpy(h, host_matrix, nfloats * sizeof(float));
+  QSG_CUDA(cudaMemcpyAsync(d, h, nfloats * sizeof(float),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  QSG_CUDA(cudaEventRecord(ctx->ring_ev[slot], ctx->stream));
+  ctx->ring_used[slot] = true;
+  *dev = d;
+  return QSG_OK;
+}
+
+// libstdc++'s std::generate_canonical<double, 53>(std::mt19937&) and
+// uniform_real_distribution<double>(0, 1): two 32-bit draws
+// (lo + hi * 2^32) / 2^64, clamped below 1.
+static double canonical_u01(std::mt19937& g) {
+  std::uniform_real_distribution<double> d(0.0, 1.0);
+  return d(g);
+}
+
+}  // namespace qsg
+
+using namespace qsg;
+
+extern "C" {
+
+int qsg_internal_to_normal(qsg_ctx* ctx, float* state, unsigned n) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "bad argument");
+  return QSG_OK;
+}
+
+int qsg_normal_to_internal(qsg_ctx* ctx, float* state, unsigned n) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "bad argument");
+  return QSG_OK;
+}
+
+int qsg_set_all_zeros(qsg_ctx* ctx, float* state, unsigned n) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_set_all_zeros: bad arg");
+  const uint64_t units = min_size(n) / 4;
+  fill_zero_kernel<<<grid_for(ctx, units, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<float4*>(state), units);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_set_state_zero(qsg_ctx* ctx, float* state, unsigned n) {
+  int rc = qsg_set_all_zeros(ctx, state, n);
+  if (rc) return rc;
+  set_one_kernel<<<1, 1, 0, ctx->stream>>>(state);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_set_state_uniform(qsg_ctx* ctx, float* state, unsigned n) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_set_state_uniform");
+  const uint64_t units = min_size(n) / 4;
+  const float v = float(1.0 / std::sqrt(double(uint64_t{1} << n)));
+  uniform_kernel<<<grid_for(ctx, units, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<float4*>(state), units, uint64_t{1} << n, v);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_get_ampl(qsg_ctx* ctx, const float* state, unsigned n, uint64_t i,
+                 float* re_im) {
+  QSG_CHECK_ARG(ctx && state && re_im, "qsg_get_ampl: null argument");
+  QSG_CHECK_ARG(n <= kMaxQubits && i < (uint64_t{1} << n),
+                "qsg_get_ampl: index out of range");
+  void* h = nullptr;
+  int rc = get_hscratch(ctx, 8, &h);
+  if (rc) return rc;
+  QSG_CUDA(cudaMemcpyAsync(h, state + 2 * i, 8, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(re_im, h, 8);
+  return QSG_OK;
+}
+
+int qsg_set_ampl(qsg_ctx* ctx, float* state, unsigned n, uint64_t i, float re,
+                 float im) {
+  QSG_CHECK_ARG(ctx && state, "qsg_set_ampl: null argument");
+  QSG_CHECK_ARG(n <= kMaxQubits && i < (uint64_t{1} << n),
+                "qsg_set_ampl: index out of range");
+  float v[2] = {re, im};
+  // Pageable source: the runtime stages it before returning.
+  QSG_CUDA(cudaMemcpyAsync(state + 2 * i, v, 8, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return QSG_OK;
+}
+
+int qsg_bulk_set_ampl(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                      uint64_t bits, float re, float im, int exclude) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_bulk_set_ampl");
+  const uint64_t namps = uint64_t{1} << n;
+  bulk_set_kernel<<<grid_for(ctx, namps, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<float2*>(state), namps, mask, bits, re, im,
+      exclude != 0);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_add(qsg_ctx* ctx, const float* src, float* dest, unsigned n) {
+  QSG_CHECK_ARG(ctx && src && dest && n <= kMaxQubits, "qsg_add");
+  const uint64_t units = units_of(n);
+  add_kernel<<<grid_for(ctx, units, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<const float4*>(src), reinterpret_cast<float4*>(dest),
+      units);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_multiply(qsg_ctx* ctx, float a, float* state, unsigned n) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_multiply");
+  const uint64_t units = units_of(n);
+  multiply_kernel<<<grid_for(ctx, units, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<float4*>(state), units, a);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_inner_product(qsg_ctx* ctx, const float* s1, const float* s2,
+                      unsigned n, double* out_re_im) {
+  QSG_CHECK_ARG(ctx && s1 && s2 && out_re_im && n <= kMaxQubits,
+                "qsg_inner_product");
+  return reduce<2>(ctx, s1, s2, n, 0, 0, out_re_im);
+}
+
+int qsg_real_inner_product(qsg_ctx* ctx, const float* s1, const float* s2,
+                           unsigned n, double* out) {
+  QSG_CHECK_ARG(ctx && s1 && s2 && out && n <= kMaxQubits,
+                "qsg_real_inner_product");
+  double r[2];
+  int rc = reduce<1>(ctx, s1, s2, n, 0, 0, r);
+  *out = r[0];
+  return rc;
+}
+
+int qsg_norm(qsg_ctx* ctx, const float* state, unsigned n, double* out) {
+  QSG_CHECK_ARG(ctx && state && out && n <= kMaxQubits, "qsg_norm");
+  double r[2];
+  int rc = reduce<0>(ctx, state, nullptr, n, 0, 0, r);
+  *out = r[0];
+  return rc;
+}
+
+uint64_t qsg_num_chunks(unsigned n) { return num_chunks(n); }
+
+int qsg_partial_norms(qsg_ctx* ctx, const float* state, unsigned n,
+                      double* out) {
+  QSG_CHECK_ARG(ctx && state && out && n <= kMaxQubits, "qsg_partial_norms");
+  double *sums, *incl;
+  int rc = chunk_prefix(ctx, state, n, 0, &sums, &incl, nullptr);
+  if (rc) return rc;
+  QSG_CUDA(cudaMemcpyAsync(out, sums, num_chunks(n) * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return QSG_OK;
+}
+
+int qsg_find_measured_bits(qsg_ctx* ctx, const float* state, unsigned n,
+                           uint64_t m, double r, uint64_t mask,
+                           uint64_t* out) {
+  QSG_CHECK_ARG(ctx && state && out && n <= kMaxQubits,
+                "qsg_find_measured_bits");
+  QSG_CHECK_ARG(m < num_chunks(n), "qsg_find_measured_bits: chunk %llu out "
+                "of range", (unsigned long long)m);
+  void* p = nullptr;
+  int rc = get_scratch(ctx, 64, &p);
+  if (rc) return rc;
+  uint64_t* d = static_cast<uint64_t*>(p);
+  find_in_chunk_kernel<<<1, kScanThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float2*>(state), chunk_bits(n), m, r, mask, d);
+  QSG_LAUNCHED(ctx);
+  void* h = nullptr;
+  rc = get_hscratch(ctx, 8, &h);
+  if (rc) return rc;
+  QSG_CUDA(cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(out, h, 8);
+  return QSG_OK;
+}
+
+int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
+                      uint64_t num_samples, const double* sorted_u,
+                      uint64_t* out_bitstrings) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_sample_sorted");
+  if (num_samples == 0) return QSG_OK;
+  QSG_CHECK_ARG(sorted_u && out_bitstrings, "qsg_sample_sorted: null");
+  const uint64_t nc = num_chunks(n);
+  const uint32_t cb = chunk_bits(n);
+  const size_t ubytes = num_samples * sizeof(double);
+  double *sums, *incl;
+  void* extra = nullptr;
+  int rc = chunk_prefix(ctx, state, n, 2 * ubytes + num_samples * 8 + 64,
+                        &sums, &incl, &extra);
+  if (rc) return rc;
+  double* du = static_cast<double*>(extra);
+  double* dr = du + num_samples;
+  uint64_t* dout = reinterpret_cast<uint64_t*>(dr + num_samples);
+  QSG_CUDA(cudaMemcpyAsync(du, sorted_u, ubytes, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  scale_uniforms_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
+                          ctx->stream>>>(du, num_samples, incl, nc, dr);
+  QSG_LAUNCHED(ctx);
+  const size_t smem = (size_t{1} << cb) * sizeof(double);
+  static bool attr = false;
+  if (!attr) {
+    QSG_CUDA(cudaFuncSetAttribute(sample_chunk_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(sizeof(double) << kChunkBits)));
+    attr = true;
+  }
+  const unsigned grid = (unsigned)std::min<uint64_t>(nc, ctx->num_sms * 8ull);
+  sample_chunk_kernel<<<grid, kScanThreads, smem, ctx->stream>>>(
+      reinterpret_cast<const float2*>(state), cb, nc, incl, dr, num_samples,
+      (uint64_t{1} << n) - 1, dout);
+  QSG_LAUNCHED(ctx);
+  QSG_CUDA(cudaMemcpyAsync(out_bitstrings, dout, num_samples * 8,
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return QSG_OK;
+}
+
+int qsg_sample(qsg_ctx* ctx, const float* state, unsigned n,
+               uint64_t num_samples, unsigned seed, uint64_t* out_bitstrings) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_sample");
+  if (num_samples == 0) return QSG_OK;
+  std::vector<double> u(num_samples);
+  std::mt19937 g(seed);
+  for (auto& x : u) x = canonical_u01(g);
+  std::sort(u.begin(), u.end());
+  return qsg_sample_sorted(ctx, state, n, num_samples, u.data(),
+                           out_bitstrings);
+}
+
+int qsg_collapse(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                 uint64_t bits) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_collapse");
+  double r[2];
+  int rc = reduce<0>(ctx, state, nullptr, n, mask, bits, r);
+  if (rc) return rc;
+  if (mask == 0) {
+    // The reference's masked reduce degenerates to the plain norm.
+  }
+  const float renorm = float(1.0 / std::sqrt(r[0]));
+  const uint64_t units = units_of(n);
+  collapse_kernel<<<grid_for(ctx, units, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<float4*>(state), units, mask, bits, renorm);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int qsg_measure(qsg_ctx* ctx, float* state, unsigned n, uint64_t mask,
+                double u, int collapse, uint64_t* out_bits) {
+  QSG_CHECK_ARG(ctx && state && out_bits && n <= kMaxQubits, "qsg_measure");
+  QSG_CHECK_ARG(u >= 0.0 && u < 1.0, "qsg_measure: u must be in [0,1)");
+  double *sums, *incl;
+  void* extra = nullptr;
+  int rc = chunk_prefix(ctx, state, n, 64, &sums, &incl, &extra);
+  if (rc) return rc;
+  uint64_t* d = static_cast<uint64_t*>(extra);
+  measure_kernel<<<1, kScanThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float2*>(state), chunk_bits(n), num_chunks(n),
+      incl, u, mask, d);
+  QSG_LAUNCHED(ctx);
+  void* h = nullptr;
+  rc = get_hscratch(ctx, 8, &h);
+  if (rc) return rc;
+  QSG_CUDA(cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(out_bits, h, 8);
+  if (collapse) return qsg_collapse(ctx, state, n, mask, *out_bits);
+  return QSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference
+implementation (quantumlib/qsim) through oracle/_ref/ref_driver.
+
+Run in a container where the reference checkout exists:
+
+    make -C oracle ref REF=<qsim checkout>
+    python tests/golden/make_golden.py
+
+Each case is a seeded gate list (written in the driver's text format) plus
+the reference's outputs: the FP64 final state of SimulatorBasic<double>
+(unfused), the FP32 final state of QSimRunner + MultiQubitGateFuser + the
+SIMD simulator, samples, expectation values and measurement outcomes.
+Everything is saved to one compressed .npz per case.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+PAULI = {
+    "I": np.eye(2, dtype=np.complex128),
+    "X": np.array([[0, 1], [1, 0]], dtype=np.complex128),
+    "Y": np.array([[0, -1j], [1j, 0]], dtype=np.complex128),
+    "Z": np.array([[1, 0], [0, -1]], dtype=np.complex128),
+}
+
+
+def random_unitary(rng: np.random.Generator, k: int) -> np.ndarray:
+    d = 1 << k
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def interleave(m: np.ndarray) -> np.ndarray:
+    """Row-major interleaved float32 (re, im) of a complex matrix."""
+    return np.ascontiguousarray(m.astype(np.complex64)).view(np.float32).ravel()
+
+
+def hexf(xs) -> str:
+    return " ".join(float(x).hex() for x in np.asarray(xs, dtype=np.float32))
+
+
+def pauli_matrix(ops: str) -> np.ndarray:
+    """Matrix of a Pauli string on sorted qubits; ops[j] acts on qs[j], and
+    bit j of the matrix index is qs[j] (so qs[0] is the least significant
+    factor of the Kronecker product)."""
+    m = np.array([[1.0 + 0j]])
+    for p in ops:
+        m = np.kron(PAULI[p], m)
+    return m
+
+
+def random_gate_list(rng, n, ngates, kmax, ctrl_frac=0.0, meas_at=None):
+    """Returns list of dicts: kind g/c/m, qs, cqs, cvals, matrix (complex)."""
+    ops = []
+    for t in range(ngates):
+        if meas_at is not None and t in meas_at:
+            k = int(rng.integers(1, 4))
+            qs = sorted(rng.choice(n, size=k, replace=False).tolist())
+            ops.append(dict(kind="m", time=t, qs=qs))
+            continue
+        k = int(rng.integers(1, kmax + 1))
+        if ctrl_frac > 0 and rng.random() < ctrl_frac:
+            k = min(k, 3)
+            c = int(rng.integers(1, 4))
+            picks = rng.choice(n, size=k + c, replace=False).tolist()
+            qs, cqs = sorted(picks[:k]), sorted(picks[k:])
+            cvals = int(rng.integers(0, 1 << c))
+            ops.append(dict(kind="c", time=t, qs=qs, cqs=cqs, cvals=cvals,
+                            m=random_unitary(rng, k)))
+        else:
+            qs = sorted(rng.choice(n, size=k, replace=False).tolist())
+            ops.append(dict(kind="g", time=t, qs=qs, m=random_unitary(rng, k)))
+    return ops
+
+
+def write_gate_list(path, n, ops):
+    with open(path, "w") as f:
+        f.write(f"n {n}\n")
+        for o in ops:
+            k = len(o["qs"])
+            q = " ".join(map(str, o["qs"]))
+            if o["kind"] == "g":
+                f.write(f"g {o['time']} {k} {q} {hexf(interleave(o['m']))}\n")
+            elif o["kind"] == "c":
+                cq = " ".join(map(str, o["cqs"]))
+                f.write(f"c {o['time']} {k} {q} {len(o['cqs'])} {cq} "
+                        f"{o['cvals']} {hexf(interleave(o['m']))}\n")
+            else:
+                f.write(f"m {o['time']} {k} {q}\n")
+
+
+def pack_ops(ops):
+    """Flat arrays for the fixture: kinds, offsets into qubit/matrix pools."""
+    kinds, qoff, qpool, coff, cpool, cvals, moff, mpool = [], [0], [], [0], [], [], [0], []
+    for o in ops:
+        kinds.append({"g": 0, "c": 1, "m": 2}[o["kind"]])
+        qpool += o["qs"]
+        qoff.append(len(qpool))
+        cpool += o.get("cqs", [])
+        coff.append(len(cpool))
+        cvals.append(o.get("cvals", 0))
+        if "m" in o:
+            mpool += interleave(o["m"]).tolist()
+        moff.append(len(mpool))
+    return dict(kinds=np.array(kinds, np.int32), qoff=np.array(qoff, np.int64),
+                qpool=np.array(qpool, np.int32), coff=np.array(coff, np.int64),
+                cpool=np.array(cpool, np.int32), cvals=np.array(cvals, np.uint64),
+                moff=np.array(moff, np.int64), mpool=np.array(mpool, np.float32))
+
+
+def random_pauli_evs(rng, n, count, wmax):
+    evs = []
+    for _ in range(count):
+        w = int(rng.integers(1, wmax + 1))
+        qs = sorted(rng.choice(n, size=w, replace=False).tolist())
+        ops = "".join(rng.choice(list("XYZ"), size=w).tolist())
+        evs.append((qs, ops, pauli_matrix(ops)))
+    return evs
+
+
+def run_case(name, n, ops, fsize, nsamples, sseed, evs=None, measure=None):
+    with tempfile.TemporaryDirectory() as td:
+        gl = os.path.join(td, "gates.txt")
+        write_gate_list(gl, n, ops)
+        out = os.path.join(td, "out")
+        cmd = [DRIVER, "run", gl, out, str(fsize), str(nsamples), str(sseed)]
+        if evs:
+            evf = os.path.join(td, "ev.txt")
+            with open(evf, "w") as f:
+                for qs, _, m in evs:
+                    f.write(f"{len(qs)} {' '.join(map(str, qs))} "
+                            f"{hexf(interleave(m))}\n")
+            cmd.append(evf)
+        subprocess.run(cmd, check=True)
+        rd = lambda ext, dt: np.fromfile(out + ext, dtype=dt)
+        data = dict(n=np.int32(n), fsize=np.int32(fsize),
+                    sample_seed=np.uint32(sseed),
+                    f64=rd(".f64", np.float64)[: 2 << n].view(np.complex128),
+                    f32=rd(".f32", np.float32).view(np.complex64),
+                    meta=rd(".meta", np.float64))
+        if nsamples:
+            data["s32"] = rd(".s32", np.uint64)
+            data["s64"] = rd(".s64", np.uint64)
+        if evs:
+            ev = rd(".ev", np.float64).reshape(-1, 4)
+            data["ev32"] = ev[:, 0] + 1j * ev[:, 1]
+            data["ev64"] = ev[:, 2] + 1j * ev[:, 3]
+            data["ev_qoff"] = np.cumsum([0] + [len(q) for q, _, _ in evs])
+            data["ev_qpool"] = np.array(sum([q for q, _, _ in evs], []), np.int32)
+            data["ev_ops"] = np.array([o for _, o, _ in evs])
+        if measure:
+            mseed, reps, mqs = measure
+            mo = os.path.join(td, "meas")
+            subprocess.run([DRIVER, "measure", gl, mo, str(mseed), str(reps),
+                            str(len(mqs))] + [str(q) for q in mqs], check=True)
+            data["meas_seed"] = np.uint32(mseed)
+            data["meas_qs"] = np.array(mqs, np.int32)
+            data["meas_bits"] = np.fromfile(mo + ".bits", dtype=np.uint64)
+            data["meas_state"] = np.fromfile(mo + ".f64", np.float64)[: 2 << n].view(np.complex128)
+        data.update(pack_ops(ops))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+        print(name, "written")
+
+
+def mt_case():
+    with tempfile.TemporaryDirectory() as td:
+        out = {}
+        for seed in (0, 1, 5489, 123456789, 4294967295):
+            p = os.path.join(td, f"mt{seed}")
+            subprocess.run([DRIVER, "mt", str(seed), "2000", p], check=True)
+            out[f"raw_{seed}"] = np.fromfile(p + ".raw", np.uint32)
+            out[f"u01_{seed}"] = np.fromfile(p + ".u01", np.float64)
+        np.savez_compressed(os.path.join(HERE, "mt19937.npz"), **out)
+        print("mt19937 written")
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
+    mt_case()
+    rng = np.random.default_rng(20261204)
+    # k = 1..6 gates at random positions (covers low/high targets, pair and
+    # non-pair layouts), FP32 fused at f=4, EVs of Pauli strings up to 6.
+    ops = random_gate_list(rng, 12, 48, 6)
+    run_case("rand12_k6", 12, ops, 4, 2000, 7,
+             evs=random_pauli_evs(rng, 12, 24, 6))
+    # Controlled gates with 1..3 controls and 1..3 targets.
+    ops = random_gate_list(rng, 11, 40, 3, ctrl_frac=0.5)
+    run_case("ctrl11", 11, ops, 3, 1000, 11)
+    # Small states (n = 1..6) with gates up to k = n.
+    for n in (1, 3, 6):
+        ops = random_gate_list(rng, n, 12, min(n, 4))
+        run_case(f"small{n}", n, ops, 2, 500, 3,
+                 evs=random_pauli_evs(rng, n, 4, min(n, 3)))
+    # Larger state, depth typical of the configs, measurement golden.
+    ops = random_gate_list(rng, 14, 60, 2)
+    run_case("rand14_k2", 14, ops, 2, 4000, 1,
+             measure=(17, 6, [0, 5, 13]))
+
+
+if __name__ == "__main__":
+    main()
