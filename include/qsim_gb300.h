@@ -174,6 +174,84 @@ double qsg_rng_uniform(qsg_rng* rng, double max_value);
 void qsg_generate_random_values(uint64_t num, unsigned seed, double max_value,
                                 double* out);
 
+/* ---- circuits ----------------------------------------------------------
+ * The operation list of lib/circuit.h:20-31 with the operation kinds of
+ * lib/operation.h:35-37 (matrix gate, controlled gate, measurement).
+ * Matrices are interleaved complex double, row-major, 2 * 4^k values, bit j
+ * of the row/column index <-> qs[j] as given (qubits are sorted on entry and
+ * the matrix permuted to match, as CreateGate, lib/gate.h:266-290). */
+typedef struct qsg_circuit qsg_circuit;
+int qsg_circuit_create(unsigned num_qubits, qsg_circuit** out);
+int qsg_circuit_destroy(qsg_circuit* c);
+int qsg_circuit_info(const qsg_circuit* c, unsigned* num_qubits,
+                     uint64_t* num_ops);
+int qsg_circuit_add_gate(qsg_circuit* c, unsigned time, const unsigned* qs,
+                         unsigned k, const double* matrix);
+/* ControlledGate (lib/gate.h:37-70): cvals bit i <-> cqs[i] as given. */
+int qsg_circuit_add_controlled_gate(qsg_circuit* c, unsigned time,
+                                    const unsigned* qs, unsigned k,
+                                    const unsigned* cqs, unsigned nc,
+                                    uint64_t cvals, const double* matrix);
+int qsg_circuit_add_measurement(qsg_circuit* c, unsigned time,
+                                const unsigned* qs, unsigned k);
+/* Gates of lib/gates_qsim.h by their text-format names (docs/input_format.md)
+ * plus "u3" (theta, phi, lambda). */
+int qsg_circuit_add_named_gate(qsg_circuit* c, unsigned time, const char* name,
+                               const unsigned* qs, unsigned nq,
+                               const double* params, unsigned np);
+/* CircuitQsimParser::FromStream (lib/circuit_qsim_parser.h:52-153). */
+int qsg_circuit_parse(const char* text, unsigned maxtime, qsg_circuit** out);
+/* Seeded synthetic workloads: grid random circuits (rows x cols plus a
+ * ragged last row of `extra` qubits), linear-chain random circuits, and
+ * layered U3 + CZ/CNOT circuits with controlled U3 gates. */
+int qsg_circuit_grid(unsigned rows, unsigned cols, unsigned extra,
+                     unsigned cycles, uint64_t seed, qsg_circuit** out);
+int qsg_circuit_chain(unsigned n, unsigned cycles, uint64_t seed,
+                      qsg_circuit** out);
+int qsg_circuit_layered_u3(unsigned n, unsigned layers,
+                           unsigned num_controlled, uint64_t seed,
+                           qsg_circuit** out);
+/* Reads back op i (qs/cqs arrays must hold the op's counts; matrix 2*4^k). */
+int qsg_circuit_get_op(const qsg_circuit* c, uint64_t i, int* kind,
+                       unsigned* time, unsigned* k, unsigned* qs, unsigned* nc,
+                       unsigned* cqs, uint64_t* cvals, double* matrix);
+/* Random Pauli strings (weight 1..max_weight, coefficients U[-1,1]); row i of
+ * qubits/letters has max_weight slots, the first weights[i] used. */
+int qsg_pauli_sum(unsigned n, unsigned count, unsigned max_weight,
+                  uint64_t seed, unsigned* weights, unsigned* qubits,
+                  char* letters, double* coeffs);
+
+/* ---- fusion plans and runs ---------------------------------------------
+ * MultiQubitGateFuser::FuseGates (lib/fuser_mqubit.h:282-526) +
+ * QSimRunner::Run (lib/run_qsim.h:225-289). */
+typedef struct qsg_plan qsg_plan;
+typedef struct qsg_fuse_options {
+  unsigned max_fused_size;  /* 1..6 */
+  unsigned seeds;           /* front gates tried per block (0: default) */
+  int tensor_path;          /* route blocks of >= tc_min_k qubits to tcgen05 */
+  unsigned tc_min_k;        /* 0: default 5 */
+  const void* cost_model;   /* engine cost model (NULL: gate-count rule) */
+} qsg_fuse_options;
+int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* opts,
+                    qsg_plan** out);
+/* One plan op per circuit op (no fusion). */
+int qsg_plan_create_unfused(const qsg_circuit* c, qsg_plan** out);
+int qsg_plan_destroy(qsg_plan* p);
+int qsg_plan_info(const qsg_plan* p, uint64_t* num_ops, unsigned* max_k,
+                  uint64_t* num_tensor_ops);
+int qsg_plan_get_op(const qsg_plan* p, uint64_t i, int* kind, unsigned* k,
+                    unsigned* qs, unsigned* nc, unsigned* cqs,
+                    uint64_t* cvals, int* path, uint64_t* num_members,
+                    double* matrix);
+/* Applies the plan to `state`; measurements draw from std::mt19937(seed)
+ * and their masked bits are written to mbits (up to mbits_cap). */
+int qsg_plan_run(qsg_ctx* ctx, qsg_plan* p, float* state, unsigned seed,
+                 uint64_t* mbits, uint64_t mbits_cap, uint64_t* num_meas);
+/* Records the plan applied to `state` as a CUDA graph (no measurements);
+ * qsg_plan_replay launches it on the context stream. */
+int qsg_plan_capture(qsg_ctx* ctx, qsg_plan* p, float* state);
+int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p);
+
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,
  * qsg_timer_stop records a second one, synchronises and returns the elapsed

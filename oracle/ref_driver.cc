@@ -27,6 +27,10 @@
 //       .ev   : per EV line: <k> <q...> <floats> -> complex<double> on the
 //               f32 state (SIMD) then on the f64 state (basic)
 //       .meta : norm, number of fused ops
+//   text <circuit.txt> <out-prefix>
+//       reference text format through CircuitQsimParser, FP64 state (.f64)
+//   fuse <gates> <max_fused_size>
+//       number of fused ops of MultiQubitGateFuser and their size histogram
 //   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
 //       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
 //       with one std::mt19937(seed); writes bits per round (.bits) and the
@@ -42,6 +46,8 @@
 #include <vector>
 
 #include "circuit.h"
+#include "circuit_qsim_parser.h"
+#include "io_file.h"
 #include "formux.h"
 #include "fuser_mqubit.h"
 #include "gate.h"
@@ -263,9 +269,53 @@ static int CmdMeasure(int argc, char** argv) {
   return 0;
 }
 
+// fuse <gates> <max_fused_size>: prints the number of fused operations
+// MultiQubitGateFuser produces and the size histogram.
+static int CmdFuse(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  unsigned fsize = std::atoi(argv[3]);
+  Circuit<Operation<float>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<float>(g));
+  auto fused = MultiQubitGateFuser<IO>::FuseGates(
+      MultiQubitGateFuser<IO>::Parameter{fsize, 0}, n, circuit.ops);
+  unsigned hist[8] = {0};
+  for (const auto& op : fused) {
+    if (const auto* pg = OpGetAlternative<FusedGate<float>>(op)) {
+      ++hist[std::min<size_t>(pg->qubits.size(), 7)];
+    }
+  }
+  std::printf("%zu", fused.size());
+  for (unsigned k = 0; k < 8; ++k) std::printf(" %u", hist[k]);
+  std::printf("\n");
+  return 0;
+}
+
+// text <circuit.txt> <out-prefix>: parses the reference text format with
+// CircuitQsimParser (FP64 gates) and applies every gate, unfused, with
+// SimulatorBasic<For,double>; measurements are skipped.  Writes .f64.
+static int CmdText(int argc, char** argv) {
+  Circuit<Operation<double>> circuit;
+  if (!CircuitQsimParser<IOFile>::FromFile(~0u, argv[2], circuit)) return 1;
+  unsigned n = circuit.num_qubits;
+  using Sim64 = SimulatorBasic<For, double>;
+  using SS64 = Sim64::StateSpace;
+  SS64 ss64(1);
+  Sim64 sim64(1);
+  auto s64 = ss64.Create(n);
+  ss64.SetStateZero(s64);
+  for (const auto& op : circuit.ops) ApplyGate(sim64, op, s64);
+  WriteRaw(std::string(argv[3]) + ".f64", s64.get(),
+           sizeof(double) * SS64::MinSize(n));
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   std::string cmd = argv[1];
+  if (cmd == "text") return CmdText(argc, argv);
+  if (cmd == "fuse") return CmdFuse(argc, argv);
   if (cmd == "mt") return CmdMt(argc, argv);
   if (cmd == "run") return CmdRun(argc, argv);
   if (cmd == "measure") return CmdMeasure(argc, argv);

@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libqsim_gb300.so")
 
 if not os.path.exists(LIB_PATH):
     raise ImportError(
-        f"{LIB_PATH} is missing: build it with `python -m qsim_gb300.build` "
+        f"{LIB_PATH} is missing: build it with `python qsim_gb300/build.py` "
         "(nvcc, sm_103a). The engine has no CPU fallback.")
 
 lib = C.CDLL(LIB_PATH)
@@ -71,6 +71,33 @@ SIGNATURES = {
     "qsg_rng_next_u32": (u32, [vp]),
     "qsg_rng_uniform": (f64, [vp, f64]),
     "qsg_generate_random_values": (None, [u64, u32, f64, P_f64]),
+    "qsg_circuit_create": (i32, [u32, C.POINTER(vp)]),
+    "qsg_circuit_destroy": (i32, [vp]),
+    "qsg_circuit_info": (i32, [vp, P_u32, P_u64]),
+    "qsg_circuit_add_gate": (i32, [vp, u32, P_u32, u32, P_f64]),
+    "qsg_circuit_add_controlled_gate": (i32, [vp, u32, P_u32, u32, P_u32, u32,
+                                              u64, P_f64]),
+    "qsg_circuit_add_measurement": (i32, [vp, u32, P_u32, u32]),
+    "qsg_circuit_add_named_gate": (i32, [vp, u32, C.c_char_p, P_u32, u32,
+                                         P_f64, u32]),
+    "qsg_circuit_parse": (i32, [C.c_char_p, u32, C.POINTER(vp)]),
+    "qsg_circuit_grid": (i32, [u32, u32, u32, u32, u64, C.POINTER(vp)]),
+    "qsg_circuit_chain": (i32, [u32, u32, u64, C.POINTER(vp)]),
+    "qsg_circuit_layered_u3": (i32, [u32, u32, u32, u64, C.POINTER(vp)]),
+    "qsg_circuit_get_op": (i32, [vp, u64, C.POINTER(C.c_int), P_u32, P_u32,
+                                 P_u32, P_u32, P_u32, P_u64, P_f64]),
+    "qsg_pauli_sum": (i32, [u32, u32, u32, u64, P_u32, P_u32, C.c_char_p,
+                            P_f64]),
+    "qsg_plan_create": (i32, [vp, vp, C.POINTER(vp)]),
+    "qsg_plan_create_unfused": (i32, [vp, C.POINTER(vp)]),
+    "qsg_plan_destroy": (i32, [vp]),
+    "qsg_plan_info": (i32, [vp, P_u64, P_u32, P_u64]),
+    "qsg_plan_get_op": (i32, [vp, u64, C.POINTER(C.c_int), P_u32, P_u32,
+                              P_u32, P_u32, P_u64, C.POINTER(C.c_int), P_u64,
+                              P_f64]),
+    "qsg_plan_run": (i32, [vp, vp, vp, u32, P_u64, u64, P_u64]),
+    "qsg_plan_capture": (i32, [vp, vp, vp]),
+    "qsg_plan_replay": (i32, [vp, vp]),
     "qsg_timer_start": (i32, [vp]),
     "qsg_timer_stop": (i32, [vp, P_f32]),
 }
@@ -79,6 +106,13 @@ for _name, (_res, _args) in SIGNATURES.items():
     _f = getattr(lib, _name)
     _f.restype = _res
     _f.argtypes = _args
+
+
+class FuseOptions(C.Structure):
+    """qsg_fuse_options."""
+    _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
+                ("tensor_path", C.c_int), ("tc_min_k", C.c_uint),
+                ("cost_model", C.c_void_p)]
 
 
 class QsgError(RuntimeError):

@@ -57,8 +57,22 @@ def _compile(cmd):
     return cmd, r.returncode, r.stdout + r.stderr
 
 
+def _check_arch_stamp() -> None:
+    """Objects built on another host architecture are discarded."""
+    import platform
+    stamp = os.path.join(BUILD, "ARCH")
+    arch = platform.machine()
+    old = open(stamp).read().strip() if os.path.exists(stamp) else None
+    if old != arch:
+        shutil.rmtree(BUILD, ignore_errors=True)
+        os.makedirs(BUILD, exist_ok=True)
+        with open(stamp, "w") as f:
+            f.write(arch + "\n")
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    _check_arch_stamp()
     cu, cc = _sources()
     hdr = _headers()
     newest = max([os.path.getmtime(h) for h in hdr] + [0.0])

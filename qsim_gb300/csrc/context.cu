@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "internal.h"
 #include "matring.cuh"
 
 namespace qsg {
@@ -75,6 +76,33 @@ bool valid_qubits(const unsigned* qs, unsigned k, unsigned n) {
   }
   return true;
 }
+
+int dev_alloc(qsg_ctx* ctx, size_t bytes, void** out) {
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return cuda_status(e, "device allocation");
+  }
+  return QSG_OK;
+}
+
+int dev_free(qsg_ctx* ctx, void* p) {
+  if (!p) return QSG_OK;
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  QSG_CUDA(cudaFree(p));
+  return QSG_OK;
+}
+
+int dev_upload(qsg_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  QSG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return QSG_OK;
+}
+
+void* ctx_stream(qsg_ctx* ctx) { return ctx->stream; }
+int ctx_device(qsg_ctx* ctx) { return ctx->device; }
 
 }  // namespace qsg
 

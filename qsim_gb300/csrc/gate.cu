@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "gate_tile.cuh"
+#include "internal.h"
 #include "matring.cuh"
 
 namespace qsg {
@@ -100,20 +101,43 @@ static bool plan_tile(unsigned n, const unsigned* qs, unsigned k,
   return true;
 }
 
+// One-time set-up of a tile-kernel instantiation: the shared-memory opt-in
+// (static shared memory adds to the dynamic size, so it is raised for every
+// instantiation) and the occupancy that sizes the persistent grid.  Done
+// before any graph capture by apply_gate_prepare.
+template <int K, bool PAIR, int MODE>
+static int tile_setup(int* occupancy) {
+  static int o = 0;
+  if (o == 0) {
+    auto kern = gate_tile_kernel<K, PAIR, MODE>;
+    const size_t smem = TileShape<K, PAIR>::SMEM;
+    QSG_CUDA(cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int v = 0;
+    QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &v, kern, kTileThreads, smem));
+    o = v < 1 ? 1 : v;
+  }
+  *occupancy = o;
+  return QSG_OK;
+}
+
 template <int K, bool PAIR, int MODE>
 static int launch_tile(qsg_ctx* ctx, float* state, unsigned n,
                        const unsigned* qs, const unsigned* cqs, unsigned c,
                        uint64_t cvals, const float* matrix,
-                       double* out_re_im) {
+                       const float* dev_matrix, double* out_re_im) {
   using SH = TileShape<K, PAIR>;
   GateArgs<K> a;
   if (!plan_tile(n, qs, K, cqs, c, cvals, PAIR, SH::LOG_ITEMS, a.g)) {
     set_error("tile planning failed (n=%u, k=%d)", n, K);
     return QSG_ERR_INVALID;
   }
-  if constexpr (K <= 4) {
+  if constexpr (K <= 5) {
     std::memcpy(a.m, matrix, sizeof(a.m));
     a.mat = nullptr;
+  } else if (dev_matrix) {
+    a.mat = reinterpret_cast<const float2*>(dev_matrix);
   } else {
     const float* dm = nullptr;
     int rc = matring_upload(ctx, matrix, 2 * (1 << (2 * K)), &dm);
@@ -123,17 +147,9 @@ static int launch_tile(qsg_ctx* ctx, float* state, unsigned n,
 
   auto kern = gate_tile_kernel<K, PAIR, MODE>;
   const size_t smem = SH::SMEM;
-  static int occ[2] = {0, 0};  // per-instantiation cache (device 0 class)
-  int& o = occ[0];
-  if (o == 0) {
-    if (smem > 48 * 1024) {
-      QSG_CUDA(cudaFuncSetAttribute(
-          kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
-    QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &o, kern, kTileThreads, smem));
-    if (o < 1) o = 1;
-  }
+  int o = 0;
+  int rc0 = tile_setup<K, PAIR, MODE>(&o);
+  if (rc0) return rc0;
   uint64_t grid = std::min<uint64_t>(a.g.num_tiles,
                                      uint64_t(ctx->num_sms) * uint64_t(o));
   if (grid < 1) grid = 1;
@@ -159,7 +175,7 @@ template <int MODE>
 static int dispatch(qsg_ctx* ctx, float* state, unsigned n,
                     const unsigned* qs, unsigned k, const unsigned* cqs,
                     unsigned c, uint64_t cvals, const float* matrix,
-                    double* out) {
+                    double* out, const float* dev_matrix = nullptr) {
   // A 0-qubit state is handled as a 1-qubit state whose amplitude 1 is the
   // zero padding of the buffer.
   unsigned ne = n == 0 ? 1 : n;
@@ -168,10 +184,10 @@ static int dispatch(qsg_ctx* ctx, float* state, unsigned n,
   case KK:                                                                   \
     if (pair)                                                                \
       return launch_tile<KK, true, MODE>(ctx, state, ne, qs, cqs, c, cvals,  \
-                                         matrix, out);                       \
+                                         matrix, dev_matrix, out);           \
     if constexpr (KK > 0)                                                    \
       return launch_tile<KK, false, MODE>(ctx, state, ne, qs, cqs, c, cvals, \
-                                          matrix, out);                      \
+                                          matrix, dev_matrix, out);          \
     break;
   switch (k) {
     QSG_CASE(0)
@@ -187,6 +203,42 @@ static int dispatch(qsg_ctx* ctx, float* state, unsigned n,
 #undef QSG_CASE
   set_error("gates on %u qubits are not supported (maximum 6)", k);
   return QSG_ERR_UNSUPPORTED;
+}
+
+int apply_gate_prepare(unsigned k, bool pair, int mode) {
+  int o = 0;
+#define QSG_PREP(KK)                                                   \
+  case KK:                                                             \
+    if (pair)                                                          \
+      return mode ? tile_setup<KK, true, 1>(&o) : tile_setup<KK, true, 0>(&o); \
+    if constexpr (KK > 0)                                              \
+      return mode ? tile_setup<KK, false, 1>(&o)                       \
+                  : tile_setup<KK, false, 0>(&o);                      \
+    return QSG_OK;
+  switch (k) {
+    QSG_PREP(0)
+    QSG_PREP(1)
+    QSG_PREP(2)
+    QSG_PREP(3)
+    QSG_PREP(4)
+    QSG_PREP(5)
+    QSG_PREP(6)
+    default:
+      return QSG_ERR_UNSUPPORTED;
+  }
+#undef QSG_PREP
+}
+
+int apply_gate_ex(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
+                  unsigned k, const unsigned* cqs, unsigned c, uint64_t cvals,
+                  const float* host_matrix, const float* dev_matrix) {
+  if (k > kMaxTargets) {
+    set_error("gates on %u qubits are not supported (maximum 6)", k);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  uint64_t cv = c == 0 ? 0 : (c < 64 ? (cvals & ((uint64_t{1} << c) - 1)) : cvals);
+  return dispatch<0>(ctx, state, n, qs, k, c ? cqs : nullptr, c, cv,
+                     host_matrix, nullptr, dev_matrix);
 }
 
 }  // namespace qsg

@@ -9,18 +9,22 @@
 //    combinations of the targets that lie above bit b.  Tile index bit j < b
 //    is state bit j; tile bit b+i is the i-th high target.  Every group of
 //    2^k amplitudes that the gate mixes lies inside one tile.
-//  * A CTA streams its tiles HBM -> registers -> shared memory with 128-bit
-//    coalesced loads, computes on shared memory, and streams the tile back.
+//  * A persistent CTA walks its tiles with a two-stage cp.async pipeline:
+//    16-byte copies land directly in (swizzled) shared memory while the
+//    previous tile is being computed; results go from registers straight
+//    back to HBM with 128-bit stores.
 //  * Shared memory is addressed in 16-byte units (two amplitudes).  A per-gate
 //    XOR swizzle of unit bits 0..2 makes the 128-bit accesses of the compute
 //    phase bank-conflict free whatever the target positions are.
 //  * When qubit 0 is not a target ("pair" mode) one work item holds two
 //    groups that differ in bit 0, so each 16-byte unit feeds both.  When
 //    qubit 0 is a target, a unit holds members (2p, 2p+1) of one group.
-//  * For k <= 4 the matrix sits in kernel-parameter (constant) space and is
+//  * For k <= 3 the matrix sits in kernel-parameter (constant) space and is
 //    read with compile-time offsets, so FFMAs take it as a constant operand.
-//    For k = 5, 6 it is staged column-major in shared memory and 2^(k-4)
-//    threads split the rows of one work item.
+//    For k >= 4 it is staged column-major in shared memory (broadcast
+//    128-bit reads of two rows) and 2^(k-3) threads split the rows of one
+//    work item (8 rows each), which keeps the code small and the register
+//    count low enough for five or more CTAs per SM.
 #pragma once
 
 #include "common.cuh"
@@ -54,24 +58,29 @@ struct TileGeom {
 template <int K>
 struct GateArgs {
   TileGeom g;
-  // k <= 4: row-major interleaved complex matrix in parameter space.
-  float m[K <= 4 ? 2 * (1 << (2 * K)) : 2];
-  // k >= 5: device copy of the row-major matrix.
+  // k <= 5: row-major interleaved complex matrix in parameter space.
+  float m[K <= 5 ? 2 * (1 << (2 * K)) : 2];
+  // k == 6: device copy of the row-major matrix (32 KiB exceeds the
+  // kernel-parameter limit).
   const float2* mat;
 };
 
 template <int K, bool PAIR>
 struct TileShape {
   static constexpr int D = 1 << K;
-  static constexpr int S = K >= 5 ? (1 << (K - 4)) : 1;  // row split
+  static constexpr int LOG_S = K >= 4 ? K - 3 : 0;
+  static constexpr int S = 1 << LOG_S;                    // row split
   static constexpr int R = D / S;                         // rows per thread
   static constexpr int ITEMS = kTileThreads / S;
-  static constexpr int LOG_ITEMS = K >= 5 ? 11 - K : 7;
+  static constexpr int LOG_ITEMS = 7 - LOG_S;
+  static constexpr bool SMEM_MAT = K >= 4;
   static constexpr int TB = LOG_ITEMS + K + (PAIR ? 1 : 0);  // full tile
   static constexpr int UNITS = 1 << (TB - 1);
   static constexpr int LPT = UNITS / kTileThreads;  // 16-B units per thread
-  static constexpr int MAT_FLOAT2 = K >= 5 ? D * D : 0;
-  static constexpr size_t SMEM = size_t(UNITS) * 16 + size_t(MAT_FLOAT2) * 8;
+  static constexpr int MAT_FLOAT2 = SMEM_MAT ? D * D : 0;
+  static constexpr int STAGES = 2;
+  static constexpr size_t SMEM =
+      size_t(STAGES) * UNITS * 16 + size_t(MAT_FLOAT2) * 8;
 };
 
 __device__ __forceinline__ uint64_t expand_outer(uint64_t t,
@@ -105,58 +114,56 @@ __device__ __forceinline__ uint32_t swz(uint32_t u, const TileGeom& g) {
   return u ^ x;
 }
 
-template <int LPT>
-__device__ __forceinline__ void tile_load(const float4* __restrict__ st,
-                                          float4* tile, uint64_t base,
-                                          const TileGeom& g) {
-  const uint32_t nunits = 1u << (g.tb - 1);
-  const uint32_t rl = g.b - 1;
-  const uint32_t pmask = (1u << rl) - 1;
-  float4 buf[LPT];
-#pragma unroll
-  for (int j = 0; j < LPT; ++j) {
-    uint32_t u = threadIdx.x + j * kTileThreads;
-    if (u < nunits) {
-      uint64_t a = ((base + g.run_off[u >> rl]) >> 1) + (u & pmask);
-      buf[j] = st[a];
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < LPT; ++j) {
-    uint32_t u = threadIdx.x + j * kTileThreads;
-    if (u < nunits) tile[swz(u, g)] = buf[j];
-  }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Issues the 16-byte copies of tile `t` into `tile` (one commit group).
 template <int LPT>
-__device__ __forceinline__ void tile_store(float4* __restrict__ st,
-                                           const float4* tile, uint64_t base,
-                                           const TileGeom& g) {
-  const uint32_t nunits = 1u << (g.tb - 1);
-  const uint32_t rl = g.b - 1;
-  const uint32_t pmask = (1u << rl) - 1;
+__device__ __forceinline__ void tile_load_async(const float4* __restrict__ st,
+                                                float4* tile, uint64_t t,
+                                                const TileGeom& g) {
+  if (t < g.num_tiles) {
+    const uint64_t base = expand_outer(t, g);
+    const uint32_t nunits = 1u << (g.tb - 1);
+    const uint32_t rl = g.b - 1;
+    const uint32_t pmask = (1u << rl) - 1;
 #pragma unroll
-  for (int j = 0; j < LPT; ++j) {
-    uint32_t u = threadIdx.x + j * kTileThreads;
-    if (u < nunits) {
-      uint64_t a = ((base + g.run_off[u >> rl]) >> 1) + (u & pmask);
-      st[a] = tile[swz(u, g)];
+    for (int j = 0; j < LPT; ++j) {
+      const uint32_t u = threadIdx.x + j * kTileThreads;
+      if (u < nunits) {
+        const uint64_t a = ((base + g.run_off[u >> rl]) >> 1) + (u & pmask);
+        cp_async16(&tile[swz(u, g)], &st[a]);
+      }
     }
   }
+  cp_async_commit();
 }
 
-// Matrix element (row, col) as float2.
+// Global float4 index of tile unit u (u = logical, unswizzled unit index).
+__device__ __forceinline__ uint64_t unit_addr(uint64_t base, uint32_t u,
+                                              const TileGeom& g) {
+  const uint32_t rl = g.b - 1;
+  return ((base + g.run_off[u >> rl]) >> 1) + (u & ((1u << rl) - 1));
+}
+
+// Matrix element (row, col) as float2 (k <= 3: parameter space).
 template <int K>
 struct MatAccess {
   static constexpr int D = 1 << K;
   const GateArgs<K>& a;
-  const float2* smat;  // column-major copy for K >= 5
   __device__ __forceinline__ float2 operator()(int row, int col) const {
-    if constexpr (K <= 4) {
-      return make_float2(a.m[2 * (row * D + col)], a.m[2 * (row * D + col) + 1]);
-    } else {
-      return smat[col * D + row];
-    }
+    return make_float2(a.m[2 * (row * D + col)], a.m[2 * (row * D + col) + 1]);
   }
 };
 
@@ -170,7 +177,7 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float2 m, float vr,
 
 // MODE 0: apply, MODE 1: expectation value.
 template <int K, bool PAIR, int MODE>
-__global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : (K == 4 ? 3 : 2))
+__global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
     gate_tile_kernel(float4* __restrict__ st,
                      const __grid_constant__ GateArgs<K> a,
                      double2* __restrict__ partial) {
@@ -183,17 +190,21 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : (K == 4 ? 3 : 2))
   extern __shared__ float4 smem[];
   const TileGeom& g = a.g;
   float4* tile = smem;
-  float2* smat = reinterpret_cast<float2*>(smem + SH::UNITS);
+  float2* smat = reinterpret_cast<float2*>(smem + SH::STAGES * SH::UNITS);
 
-  if constexpr (K >= 5) {
+  if constexpr (SH::SMEM_MAT) {
     // Column-major copy: smat[c * D + r] = M[r][c].
     for (int i = threadIdx.x; i < D * D; i += kTileThreads) {
-      int r = i / D, c = i % D;
-      smat[c * D + r] = a.mat[i];
+      const int r = i / D, c = i % D;
+      if constexpr (K <= 5) {
+        smat[c * D + r] = make_float2(a.m[2 * i], a.m[2 * i + 1]);
+      } else {
+        smat[c * D + r] = a.mat[i];
+      }
     }
     __syncthreads();
   }
-  MatAccess<K> M{a, smat};
+  MatAccess<K> M{a};
 
   const uint32_t tid = threadIdx.x;
   const int rb = SH::S == 1 ? 0 : int(tid / ITEMS);
@@ -206,10 +217,17 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : (K == 4 ? 3 : 2))
 
   double er = 0, ei = 0;
 
-  for (uint64_t t = blockIdx.x; t < g.num_tiles; t += gridDim.x) {
-    const uint64_t base = expand_outer(t, g);
-    tile_load<SH::LPT>(st, tile, base, g);
+  // Two-stage pipeline: tiles t0 and t0 + grid are in flight on entry.
+  float4* buf[2] = {tile, tile + SH::UNITS};
+  uint64_t t = blockIdx.x;
+  tile_load_async<SH::LPT>(st, buf[0], t, g);
+  tile_load_async<SH::LPT>(st, buf[1], t + gridDim.x, g);
+
+  for (int stage = 0; t < g.num_tiles; t += gridDim.x, stage ^= 1) {
+    float4* cur = buf[stage];
+    cp_async_wait<1>();
     __syncthreads();
+    const uint64_t base = expand_outer(t, g);
 
     float acc[R][NACC];
 #pragma unroll
@@ -218,25 +236,60 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : (K == 4 ? 3 : 2))
       for (int j = 0; j < NACC; ++j) acc[r][j] = 0.f;
 
     if (active) {
-      if constexpr (PAIR) {
-#pragma unroll(K >= 5 ? 2 : D)
+      if constexpr (SH::SMEM_MAT) {
+        // Rows rb*R .. rb*R+R-1 of column c are contiguous in smat.
+        const float4* mbase = reinterpret_cast<const float4*>(smat + rb * R);
+        if constexpr (PAIR) {
+#pragma unroll 2
+          for (int c = 0; c < D; ++c) {
+            const float4 v = cur[((e | g.moff[c]) >> 1) ^ swe];
+            const float4* mc = mbase + c * (D / 2);
+#pragma unroll
+            for (int r2 = 0; r2 < R / 2; ++r2) {
+              const float4 mm = mc[r2];
+              const float2 m0 = make_float2(mm.x, mm.y);
+              const float2 m1 = make_float2(mm.z, mm.w);
+              cmac(acc[2 * r2][0], acc[2 * r2][1], m0, v.x, v.y);
+              cmac(acc[2 * r2][2], acc[2 * r2][3], m0, v.z, v.w);
+              cmac(acc[2 * r2 + 1][0], acc[2 * r2 + 1][1], m1, v.x, v.y);
+              cmac(acc[2 * r2 + 1][2], acc[2 * r2 + 1][3], m1, v.z, v.w);
+            }
+          }
+        } else {
+#pragma unroll 2
+          for (int p = 0; p < D / 2; ++p) {
+            const float4 v = cur[((e | g.moff[2 * p]) >> 1) ^ swe];
+            const float4* mc0 = mbase + (2 * p) * (D / 2);
+            const float4* mc1 = mbase + (2 * p + 1) * (D / 2);
+#pragma unroll
+            for (int r2 = 0; r2 < R / 2; ++r2) {
+              const float4 a0 = mc0[r2], a1 = mc1[r2];
+              cmac(acc[2 * r2][0], acc[2 * r2][1], make_float2(a0.x, a0.y), v.x, v.y);
+              cmac(acc[2 * r2][0], acc[2 * r2][1], make_float2(a1.x, a1.y), v.z, v.w);
+              cmac(acc[2 * r2 + 1][0], acc[2 * r2 + 1][1], make_float2(a0.z, a0.w), v.x, v.y);
+              cmac(acc[2 * r2 + 1][0], acc[2 * r2 + 1][1], make_float2(a1.z, a1.w), v.z, v.w);
+            }
+          }
+        }
+      } else if constexpr (PAIR) {
+#pragma unroll
         for (int c = 0; c < D; ++c) {
-          const float4 v = tile[((e | g.moff[c]) >> 1) ^ swe];
+          const float4 v = cur[((e | g.moff[c]) >> 1) ^ swe];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const float2 m = M(rb * R + r, c);
+            const float2 m = M(r, c);
             cmac(acc[r][0], acc[r][1], m, v.x, v.y);
             cmac(acc[r][2], acc[r][3], m, v.z, v.w);
           }
         }
       } else {
-#pragma unroll(K >= 5 ? 2 : D / 2)
+#pragma unroll
         for (int p = 0; p < D / 2; ++p) {
-          const float4 v = tile[((e | g.moff[2 * p]) >> 1) ^ swe];
+          const float4 v = cur[((e | g.moff[2 * p]) >> 1) ^ swe];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const float2 m0 = M(rb * R + r, 2 * p);
-            const float2 m1 = M(rb * R + r, 2 * p + 1);
+            const float2 m0 = M(r, 2 * p);
+            const float2 m1 = M(r, 2 * p + 1);
             cmac(acc[r][0], acc[r][1], m0, v.x, v.y);
             cmac(acc[r][0], acc[r][1], m1, v.z, v.w);
           }
@@ -245,60 +298,66 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : (K == 4 ? 3 : 2))
     }
 
     if constexpr (MODE == 1) {
+      // v^dagger (M v) over this item's rows: FP32 products and item sum,
+      // FP64 accumulation across items and tiles (FP64 issue is scarce on
+      // GB300).
       if (active) {
+        float fr = 0.f, fi = 0.f;
         if constexpr (PAIR) {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const float4 v = tile[((e | g.moff[rb * R + r]) >> 1) ^ swe];
-            er += double(v.x) * acc[r][0] + double(v.y) * acc[r][1];
-            ei += double(v.x) * acc[r][1] - double(v.y) * acc[r][0];
-            er += double(v.z) * acc[r][2] + double(v.w) * acc[r][3];
-            ei += double(v.z) * acc[r][3] - double(v.w) * acc[r][2];
+            const float4 v = cur[((e | g.moff[rb * R + r]) >> 1) ^ swe];
+            fr += fmaf(v.x, acc[r][0], v.y * acc[r][1]) +
+                  fmaf(v.z, acc[r][2], v.w * acc[r][3]);
+            fi += fmaf(v.x, acc[r][1], -v.y * acc[r][0]) +
+                  fmaf(v.z, acc[r][3], -v.w * acc[r][2]);
           }
         } else {
 #pragma unroll
           for (int r = 0; r < R; r += 2) {
-            const float4 v = tile[((e | g.moff[rb * R + r]) >> 1) ^ swe];
-            er += double(v.x) * acc[r][0] + double(v.y) * acc[r][1];
-            ei += double(v.x) * acc[r][1] - double(v.y) * acc[r][0];
-            er += double(v.z) * acc[r + 1][0] + double(v.w) * acc[r + 1][1];
-            ei += double(v.z) * acc[r + 1][1] - double(v.w) * acc[r + 1][0];
+            const float4 v = cur[((e | g.moff[rb * R + r]) >> 1) ^ swe];
+            fr += fmaf(v.x, acc[r][0], v.y * acc[r][1]) +
+                  fmaf(v.z, acc[r + 1][0], v.w * acc[r + 1][1]);
+            fi += fmaf(v.x, acc[r][1], -v.y * acc[r][0]) +
+                  fmaf(v.z, acc[r + 1][1], -v.w * acc[r + 1][0]);
           }
         }
+        er += double(fr);
+        ei += double(fi);
       }
-      __syncthreads();
-    } else {
-      __syncthreads();
-      if (active) {
-        if constexpr (PAIR) {
+    } else if (active) {
+      // Controlled rows keep their input where the control test fails, so
+      // those units are left untouched in HBM.
+      if constexpr (PAIR) {
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            float4* p = &tile[((e | g.moff[rb * R + r]) >> 1) ^ swe];
-            if (ok0 && ok1) {
-              *p = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
-            } else if (ok0) {
-              *reinterpret_cast<float2*>(&p->x) =
-                  make_float2(acc[r][0], acc[r][1]);
-            } else if (ok1) {
-              *reinterpret_cast<float2*>(&p->z) =
-                  make_float2(acc[r][2], acc[r][3]);
-            }
-          }
-        } else {
-          if (ok0) {
-#pragma unroll
-            for (int r = 0; r < R; r += 2) {
-              tile[((e | g.moff[rb * R + r]) >> 1) ^ swe] = make_float4(
-                  acc[r][0], acc[r][1], acc[r + 1][0], acc[r + 1][1]);
-            }
+        for (int r = 0; r < R; ++r) {
+          const uint32_t u = (e | g.moff[rb * R + r]) >> 1;
+          float4* gp = st + unit_addr(base, u, g);
+          if (ok0 && ok1) {
+            *gp = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+          } else if (ok0) {
+            *reinterpret_cast<float2*>(&gp->x) =
+                make_float2(acc[r][0], acc[r][1]);
+          } else if (ok1) {
+            *reinterpret_cast<float2*>(&gp->z) =
+                make_float2(acc[r][2], acc[r][3]);
           }
         }
+      } else if (ok0) {
+#pragma unroll
+        for (int r = 0; r < R; r += 2) {
+          const uint32_t u = (e | g.moff[rb * R + r]) >> 1;
+          st[unit_addr(base, u, g)] = make_float4(
+              acc[r][0], acc[r][1], acc[r + 1][0], acc[r + 1][1]);
+        }
       }
-      __syncthreads();
-      tile_store<SH::LPT>(st, tile, base, g);
-      __syncthreads();
     }
+    // Every thread is done reading `cur`: refill it with the tile two steps
+    // ahead.
+    __syncthreads();
+    tile_load_async<SH::LPT>(st, cur, t + 2 * uint64_t(gridDim.x), g);
   }
+  cp_async_wait<0>();
 
   if constexpr (MODE == 1) {
     // Block reduction of (er, ei) in FP64, fixed order.

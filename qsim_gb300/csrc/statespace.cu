@@ -6,8 +6,10 @@
 // single thread scanning all 2^n amplitudes (SampleKernel, :301-326); here
 // the state is cut into chunks of 2^13 amplitudes, chunk sums are scanned on
 // the device, and one CTA per chunk that holds samples resolves them with a
-// block-wide scan and binary searches.  Every reduction runs in FP64 with a
-// fixed partition, so results are deterministic for a given n and GPU.
+// block-wide scan and binary searches.  Products and short partial sums are
+// FP32 (GB300 issues FP64 at a small fraction of the FP32 rate), every
+// longer sum is FP64, and every partition is fixed, so results are
+// deterministic for a given n and GPU.
 
 #include <algorithm>
 #include <cmath>
@@ -89,7 +91,14 @@ __global__ void collapse_kernel(float4* s, uint64_t units, uint64_t mask,
 }
 
 // ---------------------------------------------------------------------------
-// FP64 reductions.  OP 0: sum |s1|^2 (masked), 1: Re<s1|s2>, 2: <s1|s2>.
+// Reductions.  OP 0: sum |s1|^2 (masked), 1: Re<s1|s2>, 2: <s1|s2>.
+// GB300's FP64 rate is a small fraction of its FP32 rate, so products and
+// short partial sums (8 float4 units = 16 amplitudes per thread) are FP32,
+// as the reference's CUDA kernels form products in FP32; every partial is
+// then accumulated in FP64 (lib/statespace_cuda_kernels.h:31-177 uses FP64
+// accumulation).
+
+constexpr int kRedUnroll = 8;
 
 template <int OP>
 __global__ void __launch_bounds__(kRedThreads)
@@ -97,27 +106,40 @@ __global__ void __launch_bounds__(kRedThreads)
                   uint64_t units, uint64_t mask, uint64_t bits,
                   double2* __restrict__ partial) {
   double ar = 0, ai = 0;
-  for (uint64_t i = blockIdx.x * uint64_t(kRedThreads) + threadIdx.x;
-       i < units; i += uint64_t(gridDim.x) * kRedThreads) {
-    float4 x = s1[i];
-    if constexpr (OP == 0) {
-      double p0 = double(x.x) * x.x + double(x.y) * x.y;
-      double p1 = double(x.z) * x.z + double(x.w) * x.w;
-      if (mask == 0) {
-        ar += p0 + p1;
+  const uint64_t tile = uint64_t(kRedThreads) * kRedUnroll;
+  for (uint64_t b0 = blockIdx.x * tile; b0 < units;
+       b0 += uint64_t(gridDim.x) * tile) {
+    float4 x[kRedUnroll], y[kRedUnroll];
+#pragma unroll
+    for (int j = 0; j < kRedUnroll; ++j) {
+      const uint64_t i = b0 + j * kRedThreads + threadIdx.x;
+      x[j] = i < units ? s1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if constexpr (OP != 0)
+        y[j] = i < units ? s2[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float fr = 0.f, fi = 0.f;
+#pragma unroll
+    for (int j = 0; j < kRedUnroll; ++j) {
+      const uint64_t i = b0 + j * kRedThreads + threadIdx.x;
+      if constexpr (OP == 0) {
+        float p0 = fmaf(x[j].x, x[j].x, x[j].y * x[j].y);
+        float p1 = fmaf(x[j].z, x[j].z, x[j].w * x[j].w);
+        if (mask != 0) {
+          if (((2 * i) & mask) != bits) p0 = 0.f;
+          if (((2 * i + 1) & mask) != bits) p1 = 0.f;
+        }
+        fr += p0 + p1;
       } else {
-        if (((2 * i) & mask) == bits) ar += p0;
-        if (((2 * i + 1) & mask) == bits) ar += p1;
-      }
-    } else {
-      float4 y = s2[i];
-      ar += double(x.x) * y.x + double(x.y) * y.y + double(x.z) * y.z +
-            double(x.w) * y.w;
-      if constexpr (OP == 2) {
-        ai += double(x.x) * y.y - double(x.y) * y.x + double(x.z) * y.w -
-              double(x.w) * y.z;
+        fr += fmaf(x[j].x, y[j].x, x[j].y * y[j].y) +
+              fmaf(x[j].z, y[j].z, x[j].w * y[j].w);
+        if constexpr (OP == 2) {
+          fi += fmaf(x[j].x, y[j].y, -x[j].y * y[j].x) +
+                fmaf(x[j].z, y[j].w, -x[j].w * y[j].z);
+        }
       }
     }
+    ar += double(fr);
+    if constexpr (OP == 2) ai += double(fi);
   }
   __shared__ double red[2][kRedThreads / 32];
 #pragma unroll
@@ -169,37 +191,77 @@ __global__ void __launch_bounds__(1024)
 }
 
 // ---------------------------------------------------------------------------
-// Chunk scans.  A chunk is 2^cb consecutive amplitudes; thread t of the CTA
-// owns amplitudes [t*32, t*32+32) of it.  chunk_scan() computes, in a fixed
-// order, the per-thread sequential sums and the block-exclusive prefix of
-// those sums; the chunk total it returns is bit-identical in every kernel
-// that calls it, so CDF positions found in different kernels agree.
+// Chunk scans.  A chunk is 2^cb consecutive amplitudes (cb <= 13).
+//
+// chunk_sum_kernel: coalesced float4 loads, FP32 products and per-thread
+// partial sums, FP64 block total.
+//
+// ChunkCdf (used by the sample, measure and find kernels): the chunk's
+// probabilities are staged in shared memory (FP32, padded so a thread's
+// 32-element segment is conflict-free); thread t owns segment
+// [t*32, t*32+32) and its FP32 running sum; the segment totals are scanned
+// in FP64.  The CDF at element i of segment t is
+//   base + seg_prefix[t] + (double)(running FP32 sum up to i).
+// A position is found by a binary search over segment prefixes followed by a
+// sequential walk of at most 32 elements.
 
-struct ChunkScan {
-  double thread_prefix;  // sum of all earlier threads' amplitudes
-  double total;          // chunk total
-};
+constexpr int kSeg = kAmpsPerScanThread;                   // 32
+constexpr int kChunkAmps = kScanThreads * kSeg;             // 8192
+constexpr int kPadAmps = kChunkAmps + kChunkAmps / 32;      // padded floats
 
-__device__ __forceinline__ double prob(float2 a) {
-  return double(a.x) * a.x + double(a.y) * a.y;
+__device__ __forceinline__ int pad_idx(int i) { return i + (i >> 5); }
+
+__global__ void __launch_bounds__(kScanThreads)
+    chunk_sum_kernel(const float2* __restrict__ s, uint32_t cb,
+                     uint64_t nchunks, double* __restrict__ out) {
+  __shared__ double red[kScanThreads / 32];
+  const uint32_t camps = 1u << cb;
+  for (uint64_t m = blockIdx.x; m < nchunks; m += gridDim.x) {
+    const float2* c = s + (m << cb);
+    float f = 0.f;
+    for (uint32_t i = threadIdx.x; i < camps; i += kScanThreads) {
+      float2 a = c[i];
+      f += fmaf(a.x, a.x, a.y * a.y);
+    }
+    double d = f;
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int i = 0; i < kScanThreads / 32; ++i) t += red[i];
+      out[m] = t;
+    }
+    __syncthreads();
+  }
 }
 
-__device__ ChunkScan chunk_scan(const float2* __restrict__ chunk,
-                                uint32_t camps, double* local /*[32] or null*/) {
-  __shared__ double wsum[kScanThreads / 32];
-  __shared__ double tot;
-  const uint32_t t = threadIdx.x;
-  double s = 0;
-  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
-  for (uint32_t j = 0; j < per; ++j) {
-    uint32_t i = t * per + j;
-    double p = i < camps ? prob(chunk[i]) : 0.0;
-    s += p;
-    if (local) local[j] = s;
+struct ChunkCdf {
+  float* p;          // padded FP32 probabilities
+  double* seg;       // [kScanThreads + 1] exclusive segment prefixes
+  uint32_t camps;
+};
+
+// Loads chunk c and builds the segment prefixes.  All threads must call it.
+__device__ void chunk_cdf_build(const float2* __restrict__ s, uint32_t cb,
+                                uint64_t c, float* p, double* seg) {
+  const uint32_t camps = 1u << cb;
+  const float2* ch = s + (c << cb);
+  for (uint32_t i = threadIdx.x; i < camps; i += kScanThreads) {
+    float2 a = ch[i];
+    p[pad_idx(i)] = fmaf(a.x, a.x, a.y * a.y);
   }
-  // Inclusive warp scan of s, then the exclusive value by a shuffle.
-  double x = s;
-  const int lane = t % 32, w = t / 32;
+  __syncthreads();
+  float f = 0.f;
+  const uint32_t beg = threadIdx.x * kSeg;
+  for (int j = 0; j < kSeg; ++j) {
+    uint32_t i = beg + j;
+    if (i < camps) f += p[pad_idx(i)];
+  }
+  // Block exclusive scan of the segment totals in FP64.
+  __shared__ double wsum[kScanThreads / 32];
+  double x = f;
+  const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
   for (int o = 1; o < 32; o <<= 1) {
     double y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
@@ -208,7 +270,7 @@ __device__ ChunkScan chunk_scan(const float2* __restrict__ chunk,
   if (lane == 0) xe = 0.0;
   if (lane == 31) wsum[w] = x;
   __syncthreads();
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     double acc = 0;
     for (int i = 0; i < kScanThreads / 32; ++i) {
       double v = wsum[i];
@@ -217,25 +279,34 @@ __device__ ChunkScan chunk_scan(const float2* __restrict__ chunk,
     }
   }
   __syncthreads();
-  ChunkScan r;
-  r.thread_prefix = wsum[w] + xe;
-  // The chunk total is the last element of the scan as the search kernels
-  // form it (prefix + own running sum), so both agree to the bit.
-  if (t == kScanThreads - 1) tot = r.thread_prefix + s;
+  seg[threadIdx.x] = wsum[w] + xe;
+  if (threadIdx.x == kScanThreads - 1) seg[kScanThreads] = wsum[w] + xe + f;
   __syncthreads();
-  r.total = tot;
-  __syncthreads();
-  return r;
 }
 
-// out[m] = total of chunk m.
-__global__ void __launch_bounds__(kScanThreads)
-    chunk_sum_kernel(const float2* __restrict__ s, uint32_t cb,
-                     uint64_t nchunks, double* __restrict__ out) {
-  for (uint64_t m = blockIdx.x; m < nchunks; m += gridDim.x) {
-    ChunkScan cs = chunk_scan(s + (m << cb), 1u << cb, nullptr);
-    if (threadIdx.x == 0) out[m] = cs.total;
+// First i in the chunk with x < base + CDF(i); camps-1 if none.  `strict`
+// false uses x <= CDF (the reference's `while (r > partial_norms[m])`).
+__device__ uint32_t chunk_cdf_find(const float* p, const double* seg,
+                                   uint32_t camps, double base, double x) {
+  uint32_t nseg = (camps + kSeg - 1) / kSeg;
+  // first segment t with x < base + seg[t+1]
+  uint32_t lo = 0, hi = nseg;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) / 2;
+    if (x < base + seg[mid + 1]) hi = mid; else lo = mid + 1;
   }
+  if (lo >= nseg) return camps - 1;
+  const double b = base + seg[lo];
+  float f = 0.f;
+  const uint32_t beg = lo * kSeg;
+  for (int j = 0; j < kSeg; ++j) {
+    uint32_t i = beg + j;
+    if (i >= camps) break;
+    f += p[pad_idx(i)];
+    if (x < b + double(f)) return i;
+  }
+  uint32_t last = beg + kSeg - 1;
+  return last < camps ? last : camps - 1;
 }
 
 // Inclusive prefix over chunk totals (one CTA, fixed order):
@@ -257,6 +328,8 @@ __global__ void __launch_bounds__(1024)
     double y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
+  double xe = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane == 0) xe = 0.0;
   if (lane == 31) ws[w] = x;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -268,7 +341,7 @@ __global__ void __launch_bounds__(1024)
     }
   }
   __syncthreads();
-  double run = ws[w] + (x - s);
+  double run = ws[w] + xe;
   for (uint64_t j = 0; j < per; ++j) {
     uint64_t i = beg + j;
     if (i < nchunks) {
@@ -300,73 +373,42 @@ __device__ __forceinline__ uint64_t lower_bound_d(const double* r, uint64_t m,
 }
 
 // Resolves the samples that fall into each chunk.  Sample j belongs to
-// chunk m iff incl[m-1] <= r[j] < incl[m]; inside the chunk its index is the
-// first k with r[j] < incl[m-1] + (inclusive scan at k).  Samples with
-// r[j] >= incl[last] get 2^n - 1.
+// chunk c iff incl[c-1] <= r[j] < incl[c]; inside the chunk its index is the
+// first k with r[j] < incl[c-1] + CDF(k).  Samples with r[j] >= incl[last]
+// get 2^n - 1 (lib/statespace_basic.h:222-224).
 __global__ void __launch_bounds__(kScanThreads)
     sample_chunk_kernel(const float2* __restrict__ s, uint32_t cb,
                         uint64_t nchunks, const double* __restrict__ incl,
                         const double* __restrict__ r, uint64_t m,
                         uint64_t last_index, uint64_t* __restrict__ out) {
-  extern __shared__ double scan[];  // 2^cb inclusive in-chunk scan
+  __shared__ float p[kPadAmps];
+  __shared__ double seg[kScanThreads + 1];
   for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const double lo_v = c == 0 ? -1.0 : incl[c - 1];
-    const double hi_v = incl[c];
-    const uint64_t lo = c == 0 ? 0 : lower_bound_d(r, m, lo_v);
-    const uint64_t hi = lower_bound_d(r, m, hi_v);
+    const uint64_t lo = c == 0 ? 0 : lower_bound_d(r, m, incl[c - 1]);
+    const uint64_t hi = lower_bound_d(r, m, incl[c]);
     if (c == nchunks - 1) {
       for (uint64_t j = hi + threadIdx.x; j < m; j += blockDim.x)
         out[j] = last_index;
     }
     if (lo >= hi) continue;  // uniform across the block
-    const uint32_t camps = 1u << cb;
-    double local[kAmpsPerScanThread];
-    ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
-    const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
+    chunk_cdf_build(s, cb, c, p, seg);
     const double base = c == 0 ? 0.0 : incl[c - 1];
-    for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
-      uint32_t i = threadIdx.x * per + j;
-      if (i < camps) scan[i] = base + (cs.thread_prefix + local[j]);
-    }
-    __syncthreads();
-    for (uint64_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
-      const double x = r[j];
-      uint32_t a = 0, b = camps;  // first k with x < scan[k]
-      while (a < b) {
-        uint32_t mid = (a + b) / 2;
-        if (!(x < scan[mid])) a = mid + 1; else b = mid;
-      }
-      if (a >= camps) a = camps - 1;
-      out[j] = (c << cb) + a;
-    }
+    for (uint64_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
+      out[j] = (c << cb) + chunk_cdf_find(p, seg, 1u << cb, base, r[j]);
     __syncthreads();
   }
 }
 
-// FindMeasuredBits: first k of chunk c with r < in-chunk inclusive scan[k]
-// (last index of the chunk if none); masked.
+// FindMeasuredBits: first k of chunk c with r < in-chunk CDF(k) (last index
+// of the chunk if none); masked.
 __global__ void __launch_bounds__(kScanThreads)
     find_in_chunk_kernel(const float2* __restrict__ s, uint32_t cb, uint64_t c,
                          double r, uint64_t mask, uint64_t* __restrict__ out) {
-  const uint32_t camps = 1u << cb;
-  double local[kAmpsPerScanThread];
-  ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
-  __shared__ unsigned long long best;
-  if (threadIdx.x == 0) best = ~0ull;
-  __syncthreads();
-  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
-  for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
-    uint32_t i = threadIdx.x * per + j;
-    if (i < camps && r < cs.thread_prefix + local[j]) {
-      atomicMin(&best, (unsigned long long)i);
-      break;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint64_t k = best == ~0ull ? camps - 1 : best;
-    *out = ((c << cb) + k) & mask;
-  }
+  __shared__ float p[kPadAmps];
+  __shared__ double seg[kScanThreads + 1];
+  chunk_cdf_build(s, cb, c, p, seg);
+  if (threadIdx.x == 0)
+    *out = ((c << cb) + chunk_cdf_find(p, seg, 1u << cb, 0.0, r)) & mask;
 }
 
 // Measure on the device: r = u * total; chunk c = first with r <= incl[c]
@@ -376,6 +418,8 @@ __global__ void __launch_bounds__(kScanThreads)
     measure_kernel(const float2* __restrict__ s, uint32_t cb, uint64_t nchunks,
                    const double* __restrict__ incl, double u, uint64_t mask,
                    uint64_t* __restrict__ out) {
+  __shared__ float p[kPadAmps];
+  __shared__ double seg[kScanThreads + 1];
   __shared__ uint64_t sc;
   __shared__ double sr;
   if (threadIdx.x == 0) {
@@ -391,26 +435,9 @@ __global__ void __launch_bounds__(kScanThreads)
   }
   __syncthreads();
   const uint64_t c = sc;
-  const double r = sr;
-  const uint32_t camps = 1u << cb;
-  double local[kAmpsPerScanThread];
-  ChunkScan cs = chunk_scan(s + (c << cb), camps, local);
-  __shared__ unsigned long long best;
-  if (threadIdx.x == 0) best = ~0ull;
-  __syncthreads();
-  const uint32_t per = (camps + kScanThreads - 1) / kScanThreads;
-  for (uint32_t j = 0; j < per && j < kAmpsPerScanThread; ++j) {
-    uint32_t i = threadIdx.x * per + j;
-    if (i < camps && r < cs.thread_prefix + local[j]) {
-      atomicMin(&best, (unsigned long long)i);
-      break;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint64_t k = best == ~0ull ? camps - 1 : best;
-    *out = ((c << cb) + k) & mask;
-  }
+  chunk_cdf_build(s, cb, c, p, seg);
+  if (threadIdx.x == 0)
+    *out = ((c << cb) + chunk_cdf_find(p, seg, 1u << cb, 0.0, sr)) & mask;
 }
 
 // ---------------------------------------------------------------------------
@@ -447,7 +474,7 @@ template <int OP>
 static int reduce(qsg_ctx* ctx, const float* s1, const float* s2, unsigned n,
                   uint64_t mask, uint64_t bits, double* out) {
   const uint64_t units = units_of(n);
-  const unsigned grid = grid_for(ctx, units, kRedThreads * 4);
+  const unsigned grid = grid_for(ctx, units, kRedThreads * kRedUnroll);
   void* p = nullptr;
   int rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
   if (rc) return rc;
@@ -714,16 +741,8 @@ int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
   scale_uniforms_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
                           ctx->stream>>>(du, num_samples, incl, nc, dr);
   QSG_LAUNCHED(ctx);
-  const size_t smem = (size_t{1} << cb) * sizeof(double);
-  static bool attr = false;
-  if (!attr) {
-    QSG_CUDA(cudaFuncSetAttribute(sample_chunk_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(sizeof(double) << kChunkBits)));
-    attr = true;
-  }
   const unsigned grid = (unsigned)std::min<uint64_t>(nc, ctx->num_sms * 8ull);
-  sample_chunk_kernel<<<grid, kScanThreads, smem, ctx->stream>>>(
+  sample_chunk_kernel<<<grid, kScanThreads, 0, ctx->stream>>>(
       reinterpret_cast<const float2*>(state), cb, nc, incl, dr, num_samples,
       (uint64_t{1} << n) - 1, dout);
   QSG_LAUNCHED(ctx);

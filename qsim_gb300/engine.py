@@ -33,3 +33,195 @@ def generate_random_values(num: int, seed: int, max_value: float) -> np.ndarray:
     N.lib.qsg_generate_random_values(num, seed & 0xFFFFFFFF, max_value,
                                      out.ctypes.data_as(N.P_f64))
     return out[:num]
+
+
+import ctypes as C
+
+from ._native import check
+
+KIND_GATE, KIND_CONTROLLED, KIND_MEASURE = 0, 1, 2
+
+
+def _u32(xs):
+    return N.u32_array(xs)
+
+
+def _c128(m):
+    a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+    return a, a.view(np.float64).ctypes.data_as(N.P_f64)
+
+
+class Circuit:
+    """Operation list (lib/circuit.h) built through the engine's C ABI."""
+
+    def __init__(self, num_qubits: int = 0, _handle=None):
+        if _handle is not None:
+            self.h = _handle
+        else:
+            h = C.c_void_p()
+            check(N.lib.qsg_circuit_create(num_qubits, C.byref(h)))
+            self.h = h
+
+    # ---- constructors ------------------------------------------------------
+    @classmethod
+    def parse(cls, text: str, maxtime: int = 0xFFFFFFFF) -> "Circuit":
+        h = C.c_void_p()
+        check(N.lib.qsg_circuit_parse(text.encode(), maxtime, C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
+    def grid(cls, rows, cols, extra, cycles, seed) -> "Circuit":
+        h = C.c_void_p()
+        check(N.lib.qsg_circuit_grid(rows, cols, extra, cycles, seed, C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
+    def chain(cls, n, cycles, seed) -> "Circuit":
+        h = C.c_void_p()
+        check(N.lib.qsg_circuit_chain(n, cycles, seed, C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
+    def layered_u3(cls, n, layers, num_controlled, seed) -> "Circuit":
+        h = C.c_void_p()
+        check(N.lib.qsg_circuit_layered_u3(n, layers, num_controlled, seed,
+                                           C.byref(h)))
+        return cls(_handle=h)
+
+    # ---- building ----------------------------------------------------------
+    def add_gate(self, time, qs, matrix):
+        _, mp = _c128(matrix)
+        check(N.lib.qsg_circuit_add_gate(self.h, time, _u32(qs), len(qs), mp))
+
+    def add_controlled_gate(self, time, qs, cqs, cvals, matrix):
+        _, mp = _c128(matrix)
+        check(N.lib.qsg_circuit_add_controlled_gate(
+            self.h, time, _u32(qs), len(qs), _u32(cqs), len(cqs), cvals, mp))
+
+    def add_measurement(self, time, qs):
+        check(N.lib.qsg_circuit_add_measurement(self.h, time, _u32(qs), len(qs)))
+
+    def add_named(self, time, name, qs, params=()):
+        p = (C.c_double * max(1, len(params)))(*params)
+        check(N.lib.qsg_circuit_add_named_gate(self.h, time, name.encode(),
+                                               _u32(qs), len(qs), p, len(params)))
+
+    # ---- inspection --------------------------------------------------------
+    @property
+    def num_qubits(self) -> int:
+        n = C.c_uint()
+        check(N.lib.qsg_circuit_info(self.h, C.byref(n), None))
+        return n.value
+
+    def __len__(self) -> int:
+        m = C.c_uint64()
+        check(N.lib.qsg_circuit_info(self.h, None, C.byref(m)))
+        return m.value
+
+    def op(self, i: int) -> dict:
+        kind, time, k, nc = C.c_int(), C.c_uint(), C.c_uint(), C.c_uint()
+        check(N.lib.qsg_circuit_get_op(self.h, i, C.byref(kind), C.byref(time),
+                                       C.byref(k), None, C.byref(nc), None,
+                                       None, None))
+        qs = (C.c_uint * 64)()
+        cqs = (C.c_uint * 64)()
+        cv = C.c_uint64()
+        d = 1 << k.value
+        m = np.zeros(d * d, dtype=np.complex128)
+        check(N.lib.qsg_circuit_get_op(self.h, i, None, None, None, qs, None,
+                                       cqs, C.byref(cv),
+                                       m.view(np.float64).ctypes.data_as(N.P_f64)))
+        return dict(kind=kind.value, time=time.value, qs=list(qs[:k.value]),
+                    cqs=list(cqs[:nc.value]), cvals=cv.value,
+                    m=m.reshape(d, d) if kind.value != KIND_MEASURE else None)
+
+    def ops(self):
+        return [self.op(i) for i in range(len(self))]
+
+    def __del__(self):
+        try:
+            N.lib.qsg_circuit_destroy(self.h)
+        except Exception:
+            pass
+
+
+def pauli_sum(n, count, max_weight, seed):
+    w = (C.c_uint * count)()
+    q = (C.c_uint * (count * max_weight))()
+    letters = C.create_string_buffer(count * max_weight + 1)
+    co = (C.c_double * count)()
+    check(N.lib.qsg_pauli_sum(n, count, max_weight, seed, w, q, letters, co))
+    raw = letters.raw
+    out = []
+    for i in range(count):
+        qs = list(q[i * max_weight:i * max_weight + w[i]])
+        ls = raw[i * max_weight:i * max_weight + w[i]].decode()
+        out.append((qs, ls, co[i]))
+    return out
+
+
+class Plan:
+    """Fused plan (MultiQubitGateFuser output) ready to run on the GPU."""
+
+    def __init__(self, circuit: Circuit, max_fused_size: int = 4,
+                 tensor_path: bool = False, tc_min_k: int = 5, seeds: int = 0,
+                 cost_model=None, unfused: bool = False):
+        self.circuit = circuit
+        h = C.c_void_p()
+        if unfused:
+            check(N.lib.qsg_plan_create_unfused(circuit.h, C.byref(h)))
+        else:
+            o = N.FuseOptions(max_fused_size, seeds, int(tensor_path), tc_min_k,
+                              cost_model)
+            check(N.lib.qsg_plan_create(circuit.h, C.byref(o), C.byref(h)))
+        self.h = h
+
+    def info(self):
+        n, k, t = C.c_uint64(), C.c_uint(), C.c_uint64()
+        check(N.lib.qsg_plan_info(self.h, C.byref(n), C.byref(k), C.byref(t)))
+        return dict(num_ops=n.value, max_k=k.value, num_tensor_ops=t.value)
+
+    def __len__(self):
+        return self.info()["num_ops"]
+
+    def op(self, i: int) -> dict:
+        kind, k, nc, path = C.c_int(), C.c_uint(), C.c_uint(), C.c_int()
+        nm = C.c_uint64()
+        check(N.lib.qsg_plan_get_op(self.h, i, C.byref(kind), C.byref(k), None,
+                                    C.byref(nc), None, None, C.byref(path),
+                                    C.byref(nm), None))
+        qs = (C.c_uint * 64)()
+        cqs = (C.c_uint * 64)()
+        cv = C.c_uint64()
+        d = 1 << k.value
+        m = np.zeros(d * d, dtype=np.complex128)
+        check(N.lib.qsg_plan_get_op(self.h, i, None, None, qs, None, cqs,
+                                    C.byref(cv), None, None,
+                                    m.view(np.float64).ctypes.data_as(N.P_f64)))
+        return dict(kind=kind.value, qs=list(qs[:k.value]),
+                    cqs=list(cqs[:nc.value]), cvals=cv.value, path=path.value,
+                    members=nm.value,
+                    m=m.reshape(d, d) if kind.value != KIND_MEASURE else None)
+
+    def ops(self):
+        return [self.op(i) for i in range(len(self))]
+
+    def run(self, ctx, state, seed: int = 1, max_meas: int = 1024):
+        bits = np.zeros(max_meas, dtype=np.uint64)
+        nm = C.c_uint64()
+        check(N.lib.qsg_plan_run(ctx.h, self.h, state.get(), seed,
+                                 bits.ctypes.data_as(N.P_u64), max_meas,
+                                 C.byref(nm)))
+        return bits[:nm.value]
+
+    def capture(self, ctx, state):
+        check(N.lib.qsg_plan_capture(ctx.h, self.h, state.get()))
+
+    def replay(self, ctx):
+        check(N.lib.qsg_plan_replay(ctx.h, self.h))
+
+    def __del__(self):
+        try:
+            N.lib.qsg_plan_destroy(self.h)
+        except Exception:
+            pass

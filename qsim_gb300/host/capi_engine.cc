@@ -1,0 +1,313 @@
+// C ABI of the host engine: circuits, workload generators, fusion plans,
+// plan runs and CUDA-graph capture.  Declared in include/qsim_gb300.h.
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+#include "internal.h"
+#include "runner.h"
+
+using namespace qsg;
+using namespace qsg::host;
+
+struct qsg_circuit {
+  Circuit c;
+};
+
+struct qsg_plan {
+  PlanRuntime rt;
+};
+
+namespace qsg {
+void set_error_msg(const char* msg);
+}
+
+namespace {
+
+int invalid(const char* msg) {
+  qsg::set_error_msg(msg);
+  return QSG_ERR_INVALID;
+}
+
+std::vector<cplx> to_cplx(const double* m, unsigned k) {
+  const size_t d = size_t(1) << k;
+  std::vector<cplx> out(d * d);
+  for (size_t i = 0; i < d * d; ++i) out[i] = cplx(m[2 * i], m[2 * i + 1]);
+  return out;
+}
+
+bool distinct_lt(const unsigned* qs, unsigned k, unsigned n) {
+  for (unsigned i = 0; i < k; ++i) {
+    if (qs[i] >= n) return false;
+    for (unsigned j = 0; j < i; ++j)
+      if (qs[i] == qs[j]) return false;
+  }
+  return true;
+}
+
+template <typename F>
+int make_circuit(F&& f, qsg_circuit** out) {
+  if (!out) return invalid("null output");
+  *out = nullptr;
+  auto* c = new (std::nothrow) qsg_circuit();
+  if (!c) return QSG_ERR_OOM;
+  f(c->c);
+  *out = c;
+  return QSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsg_circuit_create(unsigned num_qubits, qsg_circuit** out) {
+  if (num_qubits > 63) return invalid("too many qubits");
+  return make_circuit([&](Circuit& c) { c.num_qubits = num_qubits; }, out);
+}
+
+int qsg_circuit_destroy(qsg_circuit* c) {
+  delete c;
+  return QSG_OK;
+}
+
+int qsg_circuit_info(const qsg_circuit* c, unsigned* num_qubits,
+                     uint64_t* num_ops) {
+  if (!c) return invalid("null circuit");
+  if (num_qubits) *num_qubits = c->c.num_qubits;
+  if (num_ops) *num_ops = c->c.ops.size();
+  return QSG_OK;
+}
+
+int qsg_circuit_add_gate(qsg_circuit* c, unsigned time, const unsigned* qs,
+                         unsigned k, const double* matrix) {
+  if (!c || !matrix || (k && !qs)) return invalid("null argument");
+  if (k > 6) return invalid("gates act on at most 6 qubits");
+  if (!distinct_lt(qs, k, c->c.num_qubits)) return invalid("bad qubits");
+  c->c.ops.push_back(
+      make_gate(time, std::vector<unsigned>(qs, qs + k), to_cplx(matrix, k)));
+  return QSG_OK;
+}
+
+int qsg_circuit_add_controlled_gate(qsg_circuit* c, unsigned time,
+                                    const unsigned* qs, unsigned k,
+                                    const unsigned* cqs, unsigned nc,
+                                    uint64_t cvals, const double* matrix) {
+  if (!c || !matrix || (k && !qs) || (nc && !cqs))
+    return invalid("null argument");
+  if (k > 6) return invalid("gates act on at most 6 qubits");
+  std::vector<unsigned> all(qs, qs + k);
+  all.insert(all.end(), cqs, cqs + nc);
+  if (!distinct_lt(all.data(), all.size(), c->c.num_qubits))
+    return invalid("bad qubits");
+  Op op = make_gate(time, std::vector<unsigned>(qs, qs + k), to_cplx(matrix, k));
+  // Sort controls with their values (lib/gate.h:93-146).
+  std::vector<std::pair<unsigned, unsigned>> cp;
+  for (unsigned i = 0; i < nc; ++i) cp.push_back({cqs[i], unsigned((cvals >> i) & 1)});
+  std::sort(cp.begin(), cp.end());
+  op.kind = nc ? OpKind::kControlled : OpKind::kGate;
+  op.cvals = 0;
+  for (unsigned i = 0; i < nc; ++i) {
+    op.cqs.push_back(cp[i].first);
+    op.cvals |= uint64_t(cp[i].second) << i;
+  }
+  c->c.ops.push_back(std::move(op));
+  return QSG_OK;
+}
+
+int qsg_circuit_add_measurement(qsg_circuit* c, unsigned time,
+                                const unsigned* qs, unsigned k) {
+  if (!c || (k && !qs)) return invalid("null argument");
+  if (!distinct_lt(qs, k, c->c.num_qubits)) return invalid("bad qubits");
+  Op op;
+  op.kind = OpKind::kMeasure;
+  op.time = time;
+  op.qs.assign(qs, qs + k);
+  std::sort(op.qs.begin(), op.qs.end());
+  c->c.ops.push_back(std::move(op));
+  return QSG_OK;
+}
+
+int qsg_circuit_add_named_gate(qsg_circuit* c, unsigned time, const char* name,
+                               const unsigned* qs, unsigned nq,
+                               const double* params, unsigned np) {
+  if (!c || !name) return invalid("null argument");
+  if (!distinct_lt(qs, nq, c->c.num_qubits)) return invalid("bad qubits");
+  Op op;
+  if (!named_gate(name, time, std::vector<unsigned>(qs, qs + nq),
+                  std::vector<double>(params, params + np), &op))
+    return invalid("unknown gate or wrong arity");
+  c->c.ops.push_back(std::move(op));
+  return QSG_OK;
+}
+
+int qsg_circuit_parse(const char* text, unsigned maxtime, qsg_circuit** out) {
+  if (!text || !out) return invalid("null argument");
+  *out = nullptr;
+  auto* c = new qsg_circuit();
+  std::string err;
+  if (!parse_qsim_text(text, maxtime, &c->c, &err)) {
+    delete c;
+    return invalid(err.c_str());
+  }
+  *out = c;
+  return QSG_OK;
+}
+
+int qsg_circuit_grid(unsigned rows, unsigned cols, unsigned extra,
+                     unsigned cycles, uint64_t seed, qsg_circuit** out) {
+  if (rows * cols + extra > 63 || extra > cols) return invalid("bad grid");
+  return make_circuit(
+      [&](Circuit& c) { c = grid_random_circuit(rows, cols, extra, cycles, seed); },
+      out);
+}
+
+int qsg_circuit_chain(unsigned n, unsigned cycles, uint64_t seed,
+                      qsg_circuit** out) {
+  if (n == 0 || n > 63) return invalid("bad qubit count");
+  return make_circuit(
+      [&](Circuit& c) { c = chain_random_circuit(n, cycles, seed); }, out);
+}
+
+int qsg_circuit_layered_u3(unsigned n, unsigned layers,
+                           unsigned num_controlled, uint64_t seed,
+                           qsg_circuit** out) {
+  if (n < 3 || n > 63) return invalid("bad qubit count");
+  return make_circuit(
+      [&](Circuit& c) {
+        c = layered_u3_circuit(n, layers, num_controlled, seed);
+      },
+      out);
+}
+
+int qsg_circuit_get_op(const qsg_circuit* c, uint64_t i, int* kind,
+                       unsigned* time, unsigned* k, unsigned* qs, unsigned* nc,
+                       unsigned* cqs, uint64_t* cvals, double* matrix) {
+  if (!c || i >= c->c.ops.size()) return invalid("op index out of range");
+  const Op& op = c->c.ops[i];
+  if (kind) *kind = int(op.kind);
+  if (time) *time = op.time;
+  if (k) *k = op.qs.size();
+  if (qs) std::copy(op.qs.begin(), op.qs.end(), qs);
+  if (nc) *nc = op.cqs.size();
+  if (cqs) std::copy(op.cqs.begin(), op.cqs.end(), cqs);
+  if (cvals) *cvals = op.cvals;
+  if (matrix) {
+    for (size_t j = 0; j < op.m.size(); ++j) {
+      matrix[2 * j] = op.m[j].real();
+      matrix[2 * j + 1] = op.m[j].imag();
+    }
+  }
+  return QSG_OK;
+}
+
+int qsg_pauli_sum(unsigned n, unsigned count, unsigned max_weight,
+                  uint64_t seed, unsigned* weights, unsigned* qubits,
+                  char* letters, double* coeffs) {
+  if (!weights || !qubits || !letters || !coeffs) return invalid("null");
+  if (n == 0 || max_weight == 0 || max_weight > 6) return invalid("bad sizes");
+  auto terms = random_pauli_sum(n, count, max_weight, seed);
+  for (unsigned i = 0; i < count; ++i) {
+    weights[i] = terms[i].qs.size();
+    for (unsigned j = 0; j < max_weight; ++j) {
+      qubits[i * max_weight + j] = j < weights[i] ? terms[i].qs[j] : 0;
+      letters[i * max_weight + j] = j < weights[i] ? terms[i].letters[j] : 'I';
+    }
+    coeffs[i] = terms[i].coeff;
+  }
+  return QSG_OK;
+}
+
+int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* o,
+                    qsg_plan** out) {
+  if (!c || !out) return invalid("null argument");
+  *out = nullptr;
+  FuseOptions fo;
+  if (o) {
+    fo.max_fused_size = o->max_fused_size;
+    fo.seeds = o->seeds ? o->seeds : fo.seeds;
+    fo.tensor_path = o->tensor_path != 0;
+    fo.tc_min_k = o->tc_min_k ? o->tc_min_k : fo.tc_min_k;
+    fo.cost = static_cast<const CostModel*>(o->cost_model);
+  }
+  if (fo.max_fused_size < 1 || fo.max_fused_size > 6)
+    return invalid("max_fused_size must be 1..6");
+  auto* p = new qsg_plan();
+  p->rt.plan = fuse(c->c, fo);
+  *out = p;
+  return QSG_OK;
+}
+
+int qsg_plan_create_unfused(const qsg_circuit* c, qsg_plan** out) {
+  if (!c || !out) return invalid("null argument");
+  auto* p = new qsg_plan();
+  p->rt.plan = unfused(c->c);
+  *out = p;
+  return QSG_OK;
+}
+
+int qsg_plan_destroy(qsg_plan* p) {
+  delete p;
+  return QSG_OK;
+}
+
+int qsg_plan_info(const qsg_plan* p, uint64_t* num_ops, unsigned* max_k,
+                  uint64_t* num_tensor_ops) {
+  if (!p) return invalid("null plan");
+  if (num_ops) *num_ops = p->rt.plan.ops.size();
+  if (max_k) *max_k = p->rt.plan.max_k();
+  if (num_tensor_ops) {
+    uint64_t t = 0;
+    for (const auto& op : p->rt.plan.ops) t += op.path == Path::kTensor;
+    *num_tensor_ops = t;
+  }
+  return QSG_OK;
+}
+
+int qsg_plan_get_op(const qsg_plan* p, uint64_t i, int* kind, unsigned* k,
+                    unsigned* qs, unsigned* nc, unsigned* cqs,
+                    uint64_t* cvals, int* path, uint64_t* num_members,
+                    double* matrix) {
+  if (!p || i >= p->rt.plan.ops.size()) return invalid("op index out of range");
+  const PlanOp& op = p->rt.plan.ops[i];
+  if (kind) *kind = int(op.kind);
+  if (k) *k = op.qs.size();
+  if (qs) std::copy(op.qs.begin(), op.qs.end(), qs);
+  if (nc) *nc = op.cqs.size();
+  if (cqs) std::copy(op.cqs.begin(), op.cqs.end(), cqs);
+  if (cvals) *cvals = op.cvals;
+  if (path) *path = int(op.path);
+  if (num_members) *num_members = op.members.size();
+  if (matrix) {
+    for (size_t j = 0; j < op.m.size(); ++j) {
+      matrix[2 * j] = op.m[j].real();
+      matrix[2 * j + 1] = op.m[j].imag();
+    }
+  }
+  return QSG_OK;
+}
+
+int qsg_plan_run(qsg_ctx* ctx, qsg_plan* p, float* state, unsigned seed,
+                 uint64_t* mbits, uint64_t mbits_cap, uint64_t* num_meas) {
+  if (!ctx || !p || !state) return invalid("null argument");
+  std::vector<uint64_t> bits;
+  int rc = p->rt.run(ctx, state, seed, &bits);
+  if (num_meas) *num_meas = bits.size();
+  if (mbits)
+    std::copy(bits.begin(), bits.begin() + std::min<size_t>(bits.size(), mbits_cap),
+              mbits);
+  return rc;
+}
+
+int qsg_plan_capture(qsg_ctx* ctx, qsg_plan* p, float* state) {
+  if (!ctx || !p || !state) return invalid("null argument");
+  return p->rt.capture(ctx, state);
+}
+
+int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p) {
+  if (!ctx || !p) return invalid("null argument");
+  return p->rt.replay(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,306 @@
+// Fusion planner.
+//
+// The reference's MultiQubitGateFuser (lib/fuser_mqubit.h:185-526) groups
+// one- and two-qubit gates into blocks of at most max_fused_size qubits,
+// passes controlled gates through unfused (:408-421), splits at measurement
+// times, and multiplies each block's matrices on the host
+// (CalculateFusedMatrix, lib/fuser.h:149-179).  This planner keeps that
+// contract (same inputs, same kinds of outputs, blocks <= max_fused_size)
+// with its own search: a block grows from a seed gate by scanning the
+// remaining gates in order and absorbing every gate whose qubits fit and
+// whose unscheduled predecessors are already in the block.  Qubits touched by
+// a skipped gate are blocked for the rest of the scan, which keeps the block
+// order-preserving.  Several front gates are tried as seeds and the best
+// block is kept: by default the one absorbing the most gates; with a cost
+// model, the one with the largest (cost of its gates applied alone) minus
+// (cost of the block) per block, i.e. the most time saved.
+
+#include <algorithm>
+#include <cstring>
+
+#include "engine.h"
+
+namespace qsg {
+namespace host {
+
+unsigned Plan::max_k() const {
+  unsigned k = 0;
+  for (const auto& op : ops) k = std::max<unsigned>(k, op.qs.size());
+  return k;
+}
+
+std::vector<cplx> block_matrix(const Circuit& c, const std::vector<int>& members,
+                               const std::vector<unsigned>& qs) {
+  const unsigned k = qs.size();
+  const unsigned d = 1u << k;
+  // Columns of the block matrix evolve as k-qubit states.
+  std::vector<cplx> m(size_t(d) * d, 0.0);
+  for (unsigned i = 0; i < d; ++i) m[i * d + i] = 1.0;
+  std::vector<cplx> tmp(d);
+  for (int idx : members) {
+    const Op& op = c.ops[idx];
+    const unsigned gk = op.qs.size();
+    const unsigned gd = 1u << gk;
+    // Positions of the gate's qubits inside the block.
+    unsigned pos[6], gmask = 0;
+    for (unsigned j = 0; j < gk; ++j) {
+      pos[j] = unsigned(std::find(qs.begin(), qs.end(), op.qs[j]) - qs.begin());
+      gmask |= 1u << pos[j];
+    }
+    auto expand = [&](unsigned gi) {
+      unsigned r = 0;
+      for (unsigned j = 0; j < gk; ++j)
+        if ((gi >> j) & 1) r |= 1u << pos[j];
+      return r;
+    };
+    for (unsigned col = 0; col < d; ++col) {
+      // Row-space update of column `col`: m[:, col] <- G m[:, col].
+      for (unsigned base = 0; base < d; ++base) {
+        if (base & gmask) continue;
+        cplx in[64];
+        for (unsigned gi = 0; gi < gd; ++gi) in[gi] = m[(base | expand(gi)) * d + col];
+        for (unsigned go = 0; go < gd; ++go) {
+          cplx acc = 0.0;
+          for (unsigned gi = 0; gi < gd; ++gi) acc += op.m[go * gd + gi] * in[gi];
+          tmp[go] = acc;
+        }
+        for (unsigned go = 0; go < gd; ++go) m[(base | expand(go)) * d + col] = tmp[go];
+      }
+    }
+  }
+  return m;
+}
+
+namespace {
+
+uint64_t qmask(const std::vector<unsigned>& qs) {
+  uint64_t m = 0;
+  for (unsigned q : qs) m |= uint64_t{1} << q;
+  return m;
+}
+
+void finish(const Circuit& c, PlanOp& p) {
+  if (p.kind == OpKind::kGate) {
+    if (p.members.size() == 1 && c.ops[p.members[0]].qs == p.qs) {
+      p.m = c.ops[p.members[0]].m;
+    } else {
+      p.m = block_matrix(c, p.members, p.qs);
+    }
+  }
+  p.m32.resize(2 * p.m.size());
+  for (size_t i = 0; i < p.m.size(); ++i) {
+    p.m32[2 * i] = float(p.m[i].real());
+    p.m32[2 * i + 1] = float(p.m[i].imag());
+  }
+}
+
+struct Block {
+  std::vector<int> members;
+  uint64_t mask = 0;
+  double score = -1e300;
+};
+
+// One absorb scan over the unscheduled ops of [first, end): ops whose qubits
+// lie in `mask` and whose unscheduled predecessors are all in the block are
+// absorbed (in_block set, appended to `members` when `commit`).  Returns the
+// count absorbed and fills `cands` with expansion candidates: fusible ops
+// that are not blocked but need qubits outside `mask`, with
+// popcount(mask | q) <= f, in scan order.
+template <typename Fusible>
+size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
+                   std::vector<char>& in_block, size_t first, size_t end,
+                   uint64_t mask, unsigned f, Fusible&& fusible, bool commit,
+                   std::vector<int>* members, std::vector<size_t>* cands,
+                   size_t max_cands) {
+  uint64_t blocked = 0;
+  size_t absorbed = 0;
+  std::vector<size_t> taken;
+  for (size_t i = first; i < end; ++i) {
+    if (done[i]) continue;
+    const Op& op = c.ops[i];
+    const uint64_t m = qmask(op.qs) | qmask(op.cqs);
+    if (in_block[i]) continue;
+    if (m & blocked) {
+      blocked |= m;
+    } else if (fusible(op) && (m & ~mask) == 0) {
+      ++absorbed;
+      taken.push_back(i);
+      in_block[i] = 1;
+    } else {
+      if (cands && fusible(op) && cands->size() < max_cands &&
+          unsigned(__builtin_popcountll(mask | m)) <= f)
+        cands->push_back(i);
+      blocked |= m;
+    }
+    if ((mask & ~blocked) == 0 && (!cands || cands->size() >= max_cands))
+      break;
+  }
+  if (commit) {
+    for (size_t i : taken) members->push_back(int(i));
+  } else {
+    for (size_t i : taken) in_block[i] = 0;
+  }
+  return absorbed;
+}
+
+// Grows a block from `seed`: absorb everything inside the current qubit
+// set, then expand the set by the candidate whose expanded set absorbs the
+// most ops (one-step lookahead), until the set has f qubits or no
+// candidate fits.
+template <typename Fusible>
+Block grow_block(const Circuit& c, const std::vector<char>& done, size_t first,
+                 size_t end, size_t seed, unsigned f, Fusible&& fusible) {
+  static thread_local std::vector<char> in_block;
+  in_block.assign(c.ops.size(), 0);
+  Block b;
+  b.members.push_back(int(seed));
+  in_block[seed] = 1;
+  b.mask = qmask(c.ops[seed].qs);
+  constexpr size_t kMaxCands = 12;
+  for (;;) {
+    std::vector<size_t> cands;
+    absorb_scan(c, done, in_block, first, end, b.mask, f, fusible, true,
+                &b.members, &cands, kMaxCands);
+    if (unsigned(__builtin_popcountll(b.mask)) >= f || cands.empty()) break;
+    size_t best = cands[0];
+    long best_score = -1;
+    for (size_t cand : cands) {
+      const uint64_t m2 = b.mask | qmask(c.ops[cand].qs);
+      const size_t got = absorb_scan(c, done, in_block, first, end, m2, f,
+                                     fusible, false, nullptr, nullptr, 0);
+      // Prefer more absorbed ops, then fewer new qubits.
+      const long score =
+          long(got) * 8 - long(__builtin_popcountll(m2 & ~b.mask));
+      if (score > best_score) {
+        best_score = score;
+        best = cand;
+      }
+    }
+    b.mask |= qmask(c.ops[best].qs);
+  }
+  std::sort(b.members.begin(), b.members.end());
+  return b;
+}
+
+}  // namespace
+
+Plan unfused(const Circuit& c) {
+  Plan p;
+  p.num_qubits = c.num_qubits;
+  for (size_t i = 0; i < c.ops.size(); ++i) {
+    const Op& op = c.ops[i];
+    PlanOp po;
+    po.kind = op.kind;
+    po.time = op.time;
+    po.qs = op.qs;
+    po.cqs = op.cqs;
+    po.cvals = op.cvals;
+    po.m = op.m;
+    po.members = {int(i)};
+    finish(c, po);
+    p.ops.push_back(std::move(po));
+  }
+  return p;
+}
+
+Plan fuse(const Circuit& c, const FuseOptions& opt) {
+  const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
+  Plan plan;
+  plan.num_qubits = c.num_qubits;
+  const size_t nops = c.ops.size();
+  std::vector<char> done(nops, 0);
+
+  auto fusible = [&](const Op& op) {
+    return op.kind == OpKind::kGate && op.qs.size() <= f;
+  };
+  auto cost_of = [&](const std::vector<unsigned>& qs) {
+    return opt.cost->cost_us(c.num_qubits, qs, 0,
+                             (opt.tensor_path && qs.size() >= opt.tc_min_k)
+                                 ? Path::kTensor
+                                 : Path::kCudaCore);
+  };
+
+  size_t seg_begin = 0;
+  while (seg_begin < nops) {
+    // Segment: up to and including the next measurement (a full barrier).
+    size_t seg_end = seg_begin;
+    while (seg_end < nops && c.ops[seg_end].kind != OpKind::kMeasure) ++seg_end;
+
+    size_t first = seg_begin;
+    for (;;) {
+      while (first < seg_end && done[first]) ++first;
+      if (first >= seg_end) break;
+      const Op& op0 = c.ops[first];
+      if (!fusible(op0)) {
+        PlanOp po;
+        po.kind = op0.kind;
+        po.time = op0.time;
+        po.qs = op0.qs;
+        po.cqs = op0.cqs;
+        po.cvals = op0.cvals;
+        po.m = op0.m;
+        po.members = {int(first)};
+        finish(c, po);
+        plan.ops.push_back(std::move(po));
+        done[first] = 1;
+        continue;
+      }
+      // Seeds: front gates (no unscheduled predecessor) among the first few
+      // unscheduled fusible gates.
+      std::vector<size_t> seeds;
+      {
+        uint64_t touched = 0;
+        for (size_t i = first; i < seg_end && seeds.size() < opt.seeds; ++i) {
+          if (done[i]) continue;
+          const Op& op = c.ops[i];
+          const uint64_t m = qmask(op.qs) | qmask(op.cqs);
+          if (fusible(op) && (m & touched) == 0) seeds.push_back(i);
+          touched |= m;
+          if (touched == (c.num_qubits >= 64 ? ~uint64_t{0}
+                                             : (uint64_t{1} << c.num_qubits) - 1))
+            break;
+        }
+      }
+      Block best;
+      for (size_t seed : seeds) {
+        Block b = grow_block(c, done, first, seg_end, seed, f, fusible);
+        std::vector<unsigned> qs;
+        for (unsigned q = 0; q < c.num_qubits; ++q)
+          if ((b.mask >> q) & 1) qs.push_back(q);
+        if (opt.cost) {
+          double alone = 0;
+          for (int mi : b.members) alone += cost_of(c.ops[mi].qs);
+          b.score = alone - cost_of(qs);
+        } else {
+          b.score = double(b.members.size()) - 1e-3 * double(qs.size());
+        }
+        if (b.score > best.score) best = std::move(b);
+      }
+      PlanOp po;
+      po.kind = OpKind::kGate;
+      po.time = c.ops[best.members.front()].time;
+      for (unsigned q = 0; q < c.num_qubits; ++q)
+        if ((best.mask >> q) & 1) po.qs.push_back(q);
+      po.members = best.members;
+      for (int mi : best.members) done[mi] = 1;
+      finish(c, po);
+      if (opt.tensor_path && po.qs.size() >= opt.tc_min_k) po.path = Path::kTensor;
+      plan.ops.push_back(std::move(po));
+    }
+    if (seg_end < nops) {
+      const Op& m = c.ops[seg_end];
+      PlanOp po;
+      po.kind = OpKind::kMeasure;
+      po.time = m.time;
+      po.qs = m.qs;
+      po.members = {int(seg_end)};
+      plan.ops.push_back(std::move(po));
+      done[seg_end] = 1;
+    }
+    seg_begin = seg_end + 1;
+  }
+  return plan;
+}
+
+}  // namespace host
+}  // namespace qsg

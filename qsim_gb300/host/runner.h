@@ -1,0 +1,55 @@
+// Plan runtime: a fused plan plus the device resources that running or
+// capturing it needs.
+#pragma once
+
+#include <cstddef>
+#include <vector>
+
+#include "engine.h"
+
+namespace qsg {
+
+// Tensor-core (tcgen05) application of a k = 5, 6 fused gate; `operands` are
+// the device operands built by tc_build_operands.  Defined in tc_gate.cu.
+int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
+                  unsigned k, const float* m32, const void* operands);
+// Size in bytes of the device operands of a k-qubit tensor-core gate, and
+// their construction from the interleaved FP32 matrix.
+size_t tc_operand_bytes(unsigned k);
+void tc_build_operands(unsigned k, const float* m32, void* host_out);
+
+void set_error_msg(const char* msg);
+
+namespace host {
+
+struct PlanRuntime {
+  Plan plan;
+  qsg_ctx* ctx = nullptr;
+  float* dmat = nullptr;             // k = 6 matrices (CUDA-core path)
+  std::vector<size_t> dmat_off;
+  void* tc_buf = nullptr;            // tensor-core operands
+  std::vector<size_t> tc_off;
+  bool tc_ready = false;
+  void* graph = nullptr;             // cudaGraph_t
+  void* graph_exec = nullptr;        // cudaGraphExec_t
+  float* captured_state = nullptr;
+
+  PlanRuntime() = default;
+  PlanRuntime(const PlanRuntime&) = delete;
+  PlanRuntime& operator=(const PlanRuntime&) = delete;
+  ~PlanRuntime();
+
+  void release();
+  int upload(qsg_ctx* ctx);
+  int prepare_tc();
+  const void* tc_operands(size_t i) const;
+  int launch_op(size_t i, float* state);
+  // Runs every op; measurement bits are appended to `mbits`.
+  int run(qsg_ctx* ctx, float* state, unsigned seed,
+          std::vector<uint64_t>* mbits);
+  int capture(qsg_ctx* ctx, float* state);
+  int replay(qsg_ctx* ctx);
+};
+
+}  // namespace host
+}  // namespace qsg

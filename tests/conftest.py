@@ -162,9 +162,17 @@ def load_golden(name):
     return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
 
 
-GOLDEN_CASES = sorted(os.path.basename(p)[:-4]
-                      for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                      if not p.endswith("mt19937.npz"))
+def _gate_list_cases():
+    out = []
+    for p in glob.glob(os.path.join(GOLDEN, "*.npz")):
+        with np.load(p) as z:
+            if "kinds" in z.files:
+                out.append(os.path.basename(p)[:-4])
+    return sorted(out)
+
+
+# Golden cases that hold a gate list and the reference's outputs for it.
+GOLDEN_CASES = _gate_list_cases()
 
 
 PAULI = {

@@ -172,6 +172,87 @@ def run_case(name, n, ops, fsize, nsamples, sseed, evs=None, measure=None):
         print(name, "written")
 
 
+GATES_1Q = ["id1", "h", "t", "x", "y", "z", "x_1_2", "y_1_2", "hz_1_2", "s"]
+GATES_1Q_P = [("rx", 1), ("ry", 1), ("rz", 1), ("rxy", 2)]
+GATES_2Q = ["id2", "cz", "cnot", "cx", "sw", "is"]
+GATES_2Q_P = [("fs", 2), ("cp", 1)]
+
+
+def random_text_circuit(rng, n, layers):
+    """Every gate of the text format (docs/input_format.md), random qubits in
+    both orders, angles that are exact in float (multiples of 1/64, some
+    negative), controlled gates and a final measurement."""
+    lines = [str(n)]
+    for t in range(layers):
+        perm = rng.permutation(n).tolist()
+        i = 0
+        while i < n:
+            r = rng.random()
+            ang = lambda: f"{int(rng.integers(-400, 400)) / 64}"
+            if r < 0.35 or i == n - 1:
+                g = GATES_1Q[int(rng.integers(len(GATES_1Q)))]
+                lines.append(f"{t} {g} {perm[i]}")
+                i += 1
+            elif r < 0.5:
+                g, npar = GATES_1Q_P[int(rng.integers(len(GATES_1Q_P)))]
+                lines.append(f"{t} {g} {perm[i]} " + " ".join(ang() for _ in range(npar)))
+                i += 1
+            elif r < 0.8:
+                g = GATES_2Q[int(rng.integers(len(GATES_2Q)))]
+                lines.append(f"{t} {g} {perm[i]} {perm[i + 1]}")
+                i += 2
+            elif r < 0.93 or i + 2 >= n:
+                g, npar = GATES_2Q_P[int(rng.integers(len(GATES_2Q_P)))]
+                lines.append(f"{t} {g} {perm[i]} {perm[i + 1]} " + " ".join(ang() for _ in range(npar)))
+                i += 2
+            else:
+                lines.append(f"{t} c {perm[i]} {perm[i + 1]} rx {perm[i + 2]} {ang()}")
+                i += 3
+    lines.append(f"{layers} m " + " ".join(str(q) for q in range(n)))
+    return "\n".join(lines) + "\n"
+
+
+def text_case(name, n, layers, seed):
+    rng = np.random.default_rng(seed)
+    text = random_text_circuit(rng, n, layers)
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "c.txt")
+        with open(p, "w") as f:
+            f.write(text)
+        subprocess.run([DRIVER, "text", p, os.path.join(td, "out")], check=True)
+        f64 = np.fromfile(os.path.join(td, "out.f64"), np.float64)[: 2 << n]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), n=np.int32(n),
+                        text=np.array(text), f64=f64.view(np.complex128))
+    print(name, "written")
+
+
+def fuse_counts_case():
+    """Pass counts of the reference's MultiQubitGateFuser on the seeded grid
+    circuits, for comparison with this engine's planner."""
+    sys.path.insert(0, ROOT)
+    from qsim_gb300 import engine as E
+    out = {}
+    for name, args in [("grid5x6d20", (5, 6, 0, 20, 1)),
+                       ("grid4x5d14", (4, 5, 0, 14, 1)),
+                       ("grid5x6p2d24", (5, 6, 2, 24, 1))]:
+        c = E.Circuit.grid(*args)
+        ops = []
+        for o in c.ops():
+            ops.append(dict(kind="g", time=o["time"], qs=o["qs"], m=o["m"]))
+        with tempfile.TemporaryDirectory() as td:
+            gl = os.path.join(td, "g.txt")
+            write_gate_list(gl, c.num_qubits, ops)
+            counts = []
+            for f in (2, 3, 4, 5, 6):
+                r = subprocess.run([DRIVER, "fuse", gl, str(f)], check=True,
+                                   capture_output=True, text=True).stdout.split()
+                counts.append(int(r[0]))
+        out[name] = np.array(counts, np.int32)
+        out[name + "_args"] = np.array(args, np.int64)
+    np.savez_compressed(os.path.join(HERE, "fuser_mqubit_counts.npz"), **out)
+    print("fuser_mqubit_counts written")
+
+
 def mt_case():
     with tempfile.TemporaryDirectory() as td:
         out = {}
@@ -188,6 +269,8 @@ def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
     mt_case()
+    text_case("text_gates9", 9, 30, 5)
+    fuse_counts_case()
     rng = np.random.default_rng(20261204)
     # k = 1..6 gates at random positions (covers low/high targets, pair and
     # non-pair layouts), FP32 fused at f=4, EVs of Pauli strings up to 6.

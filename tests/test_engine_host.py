@@ -1,0 +1,187 @@
+"""CPU tests of the host engine: text parser and gate library against the
+reference, fusion plans against the unfused circuit (the plan may change
+speed, never the state), planner quality against the reference's
+MultiQubitGateFuser, and the synthetic workload generators."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+
+@pytest.fixture(scope="module")
+def E():
+    from qsim_gb300 import engine
+    return engine
+
+
+def oracle_run_circuit(oracle, n, ops):
+    s = oracle.zero_state(n)
+    for o in ops:
+        if o["kind"] == 0:
+            oracle.apply_gate(s, n, o["qs"], o["m"])
+        elif o["kind"] == 1:
+            oracle.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
+    return s
+
+
+def test_parser_and_gate_library_match_reference(E, oracle):
+    """Every gate of the text format, qubits in both orders, controlled
+    gates: parsed here and applied by the oracle, the state equals the
+    reference's CircuitQsimParser + SimulatorBasic<double> state."""
+    d = load_golden("text_gates9")
+    c = E.Circuit.parse(str(d["text"]))
+    n = int(d["n"])
+    assert c.num_qubits == n
+    s = oracle_run_circuit(oracle, n, c.ops())
+    assert rel_l2(s, d["f64"]) < 1e-12
+
+
+@pytest.mark.parametrize("text", [
+    "3\n0 foo 0\n",                 # unknown gate
+    "3\n0 h 3\n",                   # qubit out of range
+    "3\n0 cz 1 1\n",                # repeated qubit
+    "3\n1 h 0\n0 x 0\n",            # out of time order on qubit 0
+    "3\n0 h 0\n1 m 0\n0 x 1\n",     # crosses a measurement boundary
+    "3\n0 rx 0\n",                  # missing parameter
+    "3\n0 h 0 1\n",                 # trailing characters
+    "3\n0 c 1 m 0\n",               # controlled measurement
+    "0\n",                          # no qubits
+])
+def test_parser_rejects_invalid_input(E, text):
+    from qsim_gb300 import QsgError
+    with pytest.raises(QsgError):
+        E.Circuit.parse(text)
+
+
+def test_parser_maxtime(E):
+    c = E.Circuit.parse("2\n0 h 0\n1 cz 0 1\n2 x 1\n", maxtime=1)
+    assert len(c) == 2
+
+
+def test_named_gates_are_unitary(E):
+    c = E.Circuit(3)
+    for name, qs, ps in [("h", [0], []), ("t", [1], []), ("x_1_2", [2], []),
+                         ("y_1_2", [0], []), ("hz_1_2", [1], []),
+                         ("rxy", [0], [0.3, 1.1]), ("fs", [2, 0], [1.2, -0.4]),
+                         ("cp", [1, 2], [0.7]), ("is", [0, 2], []),
+                         ("cnot", [2, 1], []), ("u3", [1], [0.1, 0.2, 0.3])]:
+        c.add_named(0, name, qs, ps)
+    for o in c.ops():
+        m = o["m"]
+        assert np.allclose(m @ m.conj().T, np.eye(m.shape[0]), atol=1e-12)
+        assert o["qs"] == sorted(o["qs"])
+
+
+def test_cnot_control_order(E, oracle):
+    """cnot q0 q1 with q0 > q1: control stays on q0 after qubit sorting."""
+    c = E.Circuit(2)
+    c.add_named(0, "x", [1])
+    c.add_named(1, "cnot", [1, 0])
+    s = oracle_run_circuit(oracle, 2, c.ops())
+    assert abs(s[3]) == pytest.approx(1.0)
+
+
+def small_circuits(E):
+    yield "grid3x4", E.Circuit.grid(3, 4, 0, 14, 3)
+    yield "grid2x4p2", E.Circuit.grid(2, 4, 2, 10, 4)
+    yield "chain11", E.Circuit.chain(11, 12, 5)
+    yield "u3ctrl10", E.Circuit.layered_u3(10, 6, 3, 6)
+
+
+@pytest.mark.parametrize("f", [1, 2, 3, 4, 5, 6])
+def test_fused_plan_equals_unfused(E, oracle, f):
+    """The fused plan's matrices (FP64) reproduce the unfused circuit's
+    state to 1e-12 (reference test: tests/fuser_mqubit_test.cc:264-365)."""
+    for name, c in small_circuits(E):
+        n = c.num_qubits
+        want = oracle_run_circuit(oracle, n, c.ops())
+        plan = E.Plan(c, max_fused_size=f)
+        s = oracle.zero_state(n)
+        covered = 0
+        for o in plan.ops():
+            assert len(o["qs"]) <= max(f, 2) or o["kind"] != 0
+            covered += o["members"]
+            if o["kind"] == 0:
+                oracle.apply_gate(s, n, o["qs"], o["m"])
+            elif o["kind"] == 1:
+                oracle.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
+        assert covered == len(c)
+        assert rel_l2(s, want) < 1e-12, (name, f)
+
+
+def test_fused_plan_with_measurements_keeps_order(E):
+    c = E.Circuit.parse("3\n0 h 0\n0 h 1\n1 cz 0 1\n2 m 0 1\n3 h 2\n3 x 0\n4 m 2\n")
+    plan = E.Plan(c, max_fused_size=4)
+    kinds = [o["kind"] for o in plan.ops()]
+    assert kinds.count(2) == 2
+    first_m = kinds.index(2)
+    # Gates before the first measurement are fused into ops before it.
+    assert all(k == 0 for k in kinds[:first_m])
+    assert sum(o["members"] for o in plan.ops()) == len(c)
+
+
+def test_planner_pass_counts_vs_reference_fuser(E):
+    """Fused-op counts at max_fused_size 4, 5 and 6 on the seeded grid
+    circuits are within 10% of (or below) the reference fuser's counts."""
+    d = load_golden("fuser_mqubit_counts")
+    for name in ("grid5x6d20", "grid4x5d14", "grid5x6p2d24"):
+        c = E.Circuit.grid(*[int(x) for x in d[name + "_args"]])
+        ref = d[name]  # f = 2..6
+        for f in (4, 5, 6):
+            mine = len(E.Plan(c, max_fused_size=f))
+            assert mine <= 1.1 * ref[f - 2] + 1, (name, f, mine, ref[f - 2])
+
+
+def test_grid_generator_invariants(E):
+    rows, cols, cycles = 4, 5, 14
+    c = E.Circuit.grid(rows, cols, 0, cycles, 11)
+    ops = c.ops()
+    n = rows * cols
+    one = [o for o in ops if len(o["qs"]) == 1]
+    two = [o for o in ops if len(o["qs"]) == 2]
+    assert len(one) == n * cycles
+    # No qubit repeats its previous single-qubit gate.
+    last = {}
+    for o in one:
+        key = o["m"].round(12).tobytes()
+        assert last.get(o["qs"][0]) != key
+        last[o["qs"][0]] = key
+    # Each cycle's couplers are nearest neighbours and disjoint.
+    by_time = {}
+    for o in two:
+        by_time.setdefault(o["time"], []).append(o["qs"])
+        a, b = o["qs"]
+        ra, ca, rb, cb = a // cols, a % cols, b // cols, b % cols
+        assert abs(ra - rb) + abs(ca - cb) == 1
+    for t, pairs in by_time.items():
+        flat = [q for p in pairs for q in p]
+        assert len(flat) == len(set(flat))
+    # Deterministic by seed, different across seeds.
+    c2 = E.Circuit.grid(rows, cols, 0, cycles, 11)
+    assert all(np.array_equal(a["m"], b["m"]) for a, b in zip(ops, c2.ops()))
+    c3 = E.Circuit.grid(rows, cols, 0, cycles, 12)
+    assert not all(np.array_equal(a["m"], b["m"]) for a, b in zip(ops, c3.ops()))
+
+
+def test_layered_u3_generator(E):
+    c = E.Circuit.layered_u3(28, 40, 8, 3)
+    ops = c.ops()
+    ctrl = [o for o in ops if o["kind"] == 1]
+    assert len(ctrl) == 40 * 8
+    assert all(1 <= len(o["cqs"]) <= 2 and len(o["qs"]) == 1 for o in ctrl)
+    u3 = [o for o in ops if o["kind"] == 0 and len(o["qs"]) == 1]
+    assert len(u3) == 28 * 40
+    # Times are ordered per qubit.
+    last = {}
+    for o in ops:
+        for q in o["qs"] + o["cqs"]:
+            assert o["time"] >= last.get(q, -1)
+            last[q] = o["time"]
+
+
+def test_pauli_sum(E):
+    terms = E.pauli_sum(28, 64, 6, 9)
+    assert len(terms) == 64
+    for qs, letters, coeff in terms:
+        assert 1 <= len(qs) <= 6 and qs == sorted(qs) and len(set(qs)) == len(qs)
+        assert set(letters) <= set("XYZ") and -1 <= coeff <= 1

@@ -275,7 +275,8 @@ def test_partial_norms_and_find_measured_bits(eng, oracle):
     pn = ss.PartialNorms(st)
     chunk = (1 << n) // pn.size
     p = np.abs(s) ** 2
-    assert np.allclose(pn, p.reshape(pn.size, chunk).sum(1), rtol=1e-12, atol=1e-15)
+    # FP32 products and per-thread partial sums, FP64 accumulation.
+    assert np.allclose(pn, p.reshape(pn.size, chunk).sum(1), rtol=1e-6, atol=1e-12)
     for m in (0, pn.size // 2, pn.size - 1):
         r = 0.6 * pn[m]
         cs = np.cumsum(p[m * chunk:(m + 1) * chunk])
