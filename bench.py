@@ -1,0 +1,368 @@
+#!/usr/bin/env python3
+"""Headline benchmark: seconds per run of the 30-qubit depth-20 random grid
+circuit (5x6 grid, sqrt(X)/sqrt(Y)/sqrt(W) + fSim(pi/2, pi/6), coupler
+sequence A,B,C,D,C,D,A,B, seed 1) on one GB300, complex64 state (8 GiB)
+from |0...0>.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One step = SetStateZero + every fused op of the plan, replayed from a CUDA
+graph on a resident state (8 GiB > 129 MB L2, so no L2 flush is needed).
+The headline form is the fastest engine form (tensor-core path and learned
+planner when available); the plain CUDA-core f=4 form is timed beside it.
+`e2e` is the same run through the public API with host buffers: plan
+applied through the C ABI, 1000 samples and the full final state copied to
+pinned host memory inside each timed step.
+
+Multi-GPU: the path does not shard (one state per GPU), so N > 1 runs N
+independent replicas; value = total runs / max-over-ranks time.
+
+--impl reference times the reference's CPU algorithm on the host cores (the
+oracle's OpenMP FP32 port of SimulatorBasic; the reference's own code is not
+present on the GPU host), on a bounded sample of the same workload: the
+first fused ops of the same f=4 plan, extrapolated to the whole circuit.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "30q d20 circuit s/run: tensor-core+learned fusion vs plain, F>=1-1e-6; traj/s"
+UNIT = "s/run"
+GRID = dict(rows=5, cols=6, extra=0, cycles=20, seed=1)
+WORKLOAD = "grid5x6 (30 qubits) random circuit depth 20, seed 1, complex64, from |0>"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed
+    region (the process started here is the only one stopped)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != self.gpu:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s, p in zip(sm, power) if p > 0.3 * max(power)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def traffic_from_profiles(n: int):
+    """dram read+write bytes per launch of the dominant kernel, from the
+    committed ncu summary (scaled from its capture size to n qubits)."""
+    p = os.path.join(ROOT, "profiles", "gate_tile_k4_plain_pass.md")
+    if not os.path.exists(p):
+        return None
+    nq, tb = None, None
+    for line in open(p):
+        if line.startswith("capture_qubits:"):
+            nq = int(line.split(":")[1])
+        if line.startswith("dram_bytes_per_launch:"):
+            tb = float(line.split(":")[1])
+    if nq is None or tb is None:
+        return None
+    return tb * (2 ** (n - nq))
+
+
+# --------------------------------------------------------------------------
+def cpu_sample(n: int, plan_ops, max_ops: int, threads: int | None = None):
+    """Times the oracle's OpenMP FP32 port on the first fused ops of the
+    plan at full size; returns (seconds, ops timed, threads)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import Oracle
+    orc = Oracle()
+    if threads:
+        orc.L.orc_set_num_threads(threads)
+    nthreads = orc.L.orc_num_threads()
+    st = np.zeros(2 << n, dtype=np.float32)
+    st[0] = 1.0
+    P = C.POINTER
+    t_total, done = 0.0, 0
+    for o in plan_ops[:max_ops]:
+        m = np.ascontiguousarray(o["m"].astype(np.complex64)).view(np.float32)
+        qs = (C.c_uint * max(1, len(o["qs"])))(*o["qs"])
+        t0 = time.perf_counter()
+        orc.L.orc_apply_gate_f32(st.ctypes.data_as(P(C.c_float)), n, qs,
+                                 len(o["qs"]), m.ctypes.data_as(P(C.c_float)))
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > 20.0:
+            break
+    return t_total, done, nthreads
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    from qsim_gb300 import engine as E
+    c = E.Circuit.grid(GRID["rows"], GRID["cols"], GRID["extra"],
+                       GRID["cycles"], GRID["seed"])
+    n = c.num_qubits
+    plan = E.Plan(c, max_fused_size=4)
+    ops = plan.ops()
+    per_step = []
+    for _ in range(args.warmup + args.steps):
+        t, done, threads = cpu_sample(n, ops, args.cpu_ops)
+        per_step.append(t * len(ops) / done)
+    vals = per_step[args.warmup:]
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "max_fused_size": 4,
+                   "fused_ops": len(ops)},
+        "cpu_baseline": {
+            "value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {done} of {len(ops)} fused ops (f=4 plan) of "
+                      f"the 30-qubit circuit on an 8 GiB FP32 host state, "
+                      f"extrapolated by op count"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+def run_engine(args, world, rank, local, dist):
+    import numpy as np
+    import qsim_gb300 as q
+    from qsim_gb300 import engine as E
+    from qsim_gb300 import _native as N
+
+    hbm_peak, _, peak_kind = peaks()
+    ctx = q.Context(0)
+    ss = q.StateSpace(ctx=ctx)
+    c = E.Circuit.grid(GRID["rows"], GRID["cols"], GRID["extra"],
+                       GRID["cycles"], GRID["seed"] + (rank if args.distinct_replicas else 0))
+    n = c.num_qubits
+    nbytes_state = 8 << n
+    st = ss.Create(n)
+    if ss.IsNull(st):
+        raise RuntimeError("not enough device memory for the 30-qubit state")
+
+    forms = {}
+    forms["plain_f4"] = E.Plan(c, max_fused_size=4)
+    forms["plain_f5"] = E.Plan(c, max_fused_size=5)
+    forms["plain_f6"] = E.Plan(c, max_fused_size=6)
+
+    def time_form(plan, steps, warmup):
+        plan.capture(ctx, st)
+        for _ in range(warmup):
+            ss.SetStateZero(st)
+            plan.replay(ctx)
+        ctx.sync()
+        barrier(dist)
+        ctx.timer_start()
+        for _ in range(steps):
+            ss.SetStateZero(st)
+            plan.replay(ctx)
+        return ctx.timer_stop() / steps
+
+    results = {}
+    for name, plan in forms.items():
+        results[name] = time_form(plan, max(1, args.steps // 2), 1)
+    best = min(results, key=results.get)
+    head = forms[best]
+
+    # Headline timed region: K steps of the best form.
+    head.capture(ctx, st)
+    for _ in range(args.warmup):
+        ss.SetStateZero(st)
+        head.replay(ctx)
+    ctx.sync()
+    launches_per_step = len(head) + 2  # plan ops + fill + set-one kernels
+    barrier(dist)
+    clk = ClockSampler(local)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        ss.SetStateZero(st)
+        head.replay(ctx)
+    ms = ctx.timer_stop() / args.steps
+    clocks = clk.stop()
+    ms = max_over_ranks(dist, ms)
+    value = ms / 1e3
+
+    # Roofline of the dominant kernel: per-op CUDA-event times of the plain
+    # f=4 plan; algorithmic bytes per launch = 16 * 2^n (one read + one
+    # write of the state).
+    ss.SetStateZero(st)
+    prof = forms["plain_f4"].profile(ctx, st)
+    ops4 = forms["plain_f4"].ops()
+    ks = [len(o["qs"]) for o in ops4]
+    gate_ms = [t for t, k in zip(prof, ks)]
+    avg_launch_ms = float(np.mean(gate_ms))
+    achieved = 16.0 * (1 << n) / (avg_launch_ms * 1e-3) / 1e9
+    per_k = {}
+    for k in sorted(set(ks)):
+        ts = [t for t, kk in zip(prof, ks) if kk == k]
+        per_k[str(k)] = {"launches": len(ts), "avg_ms": float(np.mean(ts)),
+                         "gbs": 16.0 * (1 << n) / (float(np.mean(ts)) * 1e-3) / 1e9}
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": traffic_from_profiles(n),
+                "kernel": "gate_tile_kernel (plain f=4 plan, all launches)",
+                "peak_source": peak_kind, "per_k": per_k}
+
+    # End to end through the public API with host buffers.
+    hbuf = C.c_void_p()
+    N.check(N.lib.qsg_host_alloc(nbytes_state, C.byref(hbuf)))
+    samples = np.zeros(1000, dtype=np.uint64)
+    h2d = sum(8 * (1 << (2 * len(o["qs"]))) for o in head.ops())
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        ctx.sync()
+        barrier(dist)
+        t0 = time.perf_counter()
+        ss.SetStateZero(st)
+        head.run(ctx, st)
+        N.check(N.lib.qsg_sample(ctx.h, st.get(), n, 1000, 1,
+                                 samples.ctypes.data_as(N.P_u64)))
+        N.check(N.lib.qsg_copy_d2h(ctx.h, hbuf, st.get(), n))
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(dt)
+    N.lib.qsg_host_free(hbuf)
+    e2e = max_over_ranks(dist, statistics.median(e2e_times))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        t, done, threads = cpu_sample(n, ops4, args.cpu_ops)
+        cpu = {"value": t * len(ops4) / done, "unit": UNIT, "cores": threads,
+               "kind": "port",
+               "sample": f"first {done} of {len(ops4)} fused ops of the f=4 "
+                         f"plan on an 8 GiB FP32 host state (oracle OpenMP "
+                         f"port of SimulatorBasic), extrapolated by op count"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value / 1.0, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": best,
+                       "fused_ops": len(head), "max_k": head.info()["max_k"],
+                       "state_bytes": nbytes_state,
+                       "l2": "state 8 GiB > 129 MB L2, no flush needed",
+                       "parallelism": f"replicas x{world}",
+                       "forms_s": {k: v / 1e3 for k, v in results.items()},
+                       "passes": {k: len(v) for k, v in forms.items()}},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": nbytes_state + 8 * 1000},
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-ops", type=int, default=4,
+                    help="fused ops timed on the CPU for the baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--distinct-replicas", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, dist = dist_setup()
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, dist)
+        else:
+            run_engine(args, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

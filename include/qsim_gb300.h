@@ -77,6 +77,10 @@ int qsg_copy_h2d(qsg_ctx* ctx, float* dest, const float* host_src, unsigned n);
 int qsg_copy_h2d_partial(qsg_ctx* ctx, float* dest, const float* host_src,
                          uint64_t size, unsigned n);
 
+/* Page-locked host buffers for fast host<->device copies of whole states. */
+int qsg_host_alloc(size_t bytes, void** out);
+int qsg_host_free(void* p);
+
 /* ---- state space (lib/statespace_cuda.h) ------------------------------- */
 /* InternalToNormalOrder / NormalToInternalOrder (:85-107).  The internal
  * order of this engine is the normal order, so both only validate. */
@@ -155,6 +159,15 @@ int qsg_apply_controlled_gate(qsg_ctx* ctx, float* state, unsigned n,
 int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
                           const unsigned* qs, unsigned k, const float* matrix,
                           double* out_re_im);
+/* ApplyGate on the tensor cores (tcgen05, split-TF32, FP32 accumulation):
+ * k <= 6 targets, n >= 12; the gate is padded to 6 targets with the
+ * identity on the lowest free qubits.  No counterpart in the reference, which
+ * applies every gate on CUDA cores (lib/simulator_cuda.h:333-380). */
+int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
+                      const unsigned* qs, unsigned k, const float* matrix);
+/* Reads and clears the tensor-core kernels' error flag: 1 if a bounded
+ * device-side wait gave up (the kernel then skipped its remaining tiles). */
+int qsg_tc_error(qsg_ctx* ctx, int* out);
 /* SIMDRegisterSize (:265-267). */
 unsigned qsg_simd_register_size(void);
 
@@ -251,6 +264,10 @@ int qsg_plan_run(qsg_ctx* ctx, qsg_plan* p, float* state, unsigned seed,
  * qsg_plan_replay launches it on the context stream. */
 int qsg_plan_capture(qsg_ctx* ctx, qsg_plan* p, float* state);
 int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p);
+/* Applies the plan's gate ops with a CUDA event pair around each launch;
+ * op_ms[i] = milliseconds of op i (measurement ops are skipped, 0). */
+int qsg_plan_profile(qsg_ctx* ctx, qsg_plan* p, float* state, float* op_ms,
+                     uint64_t cap);
 
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,

@@ -37,6 +37,8 @@ SIGNATURES = {
     "qsg_min_size": (u64, [u32]),
     "qsg_state_create": (i32, [vp, u32, C.POINTER(vp)]),
     "qsg_state_free": (i32, [vp, vp]),
+    "qsg_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
+    "qsg_host_free": (i32, [vp]),
     "qsg_copy_d2d": (i32, [vp, vp, vp, u32]),
     "qsg_copy_d2h": (i32, [vp, vp, vp, u32]),
     "qsg_copy_h2d": (i32, [vp, vp, vp, u32]),
@@ -65,6 +67,8 @@ SIGNATURES = {
     "qsg_apply_controlled_gate": (i32, [vp, vp, u32, P_u32, u32, P_u32, u32,
                                         u64, P_f32]),
     "qsg_expectation_value": (i32, [vp, vp, u32, P_u32, u32, P_f32, P_f64]),
+    "qsg_apply_gate_tc": (i32, [vp, vp, u32, P_u32, u32, P_f32]),
+    "qsg_tc_error": (i32, [vp, C.POINTER(C.c_int)]),
     "qsg_simd_register_size": (u32, []),
     "qsg_rng_create": (vp, [u32]),
     "qsg_rng_destroy": (None, [vp]),
@@ -98,6 +102,7 @@ SIGNATURES = {
     "qsg_plan_run": (i32, [vp, vp, vp, u32, P_u64, u64, P_u64]),
     "qsg_plan_capture": (i32, [vp, vp, vp]),
     "qsg_plan_replay": (i32, [vp, vp]),
+    "qsg_plan_profile": (i32, [vp, vp, vp, P_f32, u64]),
     "qsg_timer_start": (i32, [vp]),
     "qsg_timer_stop": (i32, [vp, P_f32]),
 }

@@ -75,6 +75,10 @@ struct qsg_ctx {
   cudaEvent_t ring_ev[kRingSlots] = {};
   bool ring_used[kRingSlots] = {};
   int ring_next = 0;
+
+  // Device operands of single tensor-core gate calls.
+  void* tc_slot = nullptr;
+  size_t tc_slot_size = 0;
 };
 
 namespace qsg {
@@ -83,6 +87,7 @@ namespace qsg {
 // stream before replacing a smaller buffer).
 int get_scratch(qsg_ctx* ctx, size_t bytes, void** out);
 int get_hscratch(qsg_ctx* ctx, size_t bytes, void** out);
+int get_tc_operand_slot(qsg_ctx* ctx, size_t bytes, void** out);
 
 // Validates a qubit list: distinct, sorted ascending, < n.
 bool valid_qubits(const unsigned* qs, unsigned k, unsigned n);

@@ -68,6 +68,21 @@ int get_hscratch(qsg_ctx* ctx, size_t bytes, void** out) {
   return QSG_OK;
 }
 
+int get_tc_operand_slot(qsg_ctx* ctx, size_t bytes, void** out) {
+  if (bytes > ctx->tc_slot_size) {
+    if (ctx->tc_slot) {
+      QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+      QSG_CUDA(cudaFree(ctx->tc_slot));
+      ctx->tc_slot = nullptr;
+      ctx->tc_slot_size = 0;
+    }
+    QSG_CUDA(cudaMalloc(&ctx->tc_slot, bytes));
+    ctx->tc_slot_size = bytes;
+  }
+  *out = ctx->tc_slot;
+  return QSG_OK;
+}
+
 bool valid_qubits(const unsigned* qs, unsigned k, unsigned n) {
   if (k > 0 && qs == nullptr) return false;
   for (unsigned i = 0; i < k; ++i) {
@@ -153,6 +168,7 @@ int qsg_ctx_destroy(qsg_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   matring_release(ctx);
   if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->tc_slot) cudaFree(ctx->tc_slot);
   if (ctx->hscratch) cudaFreeHost(ctx->hscratch);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -201,6 +217,24 @@ int qsg_state_free(qsg_ctx* ctx, float* state) {
   if (!state) return QSG_OK;
   QSG_CUDA(cudaStreamSynchronize(ctx->stream));
   QSG_CUDA(cudaFree(state));
+  return QSG_OK;
+}
+
+int qsg_host_alloc(size_t bytes, void** out) {
+  QSG_CHECK_ARG(out, "qsg_host_alloc: null out");
+  *out = nullptr;
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    cudaGetLastError();
+    set_error("pinned host allocation of %zu bytes failed", bytes);
+    return QSG_ERR_OOM;
+  }
+  return QSG_OK;
+}
+
+int qsg_host_free(void* p) {
+  if (p) QSG_CUDA(cudaFreeHost(p));
   return QSG_OK;
 }
 

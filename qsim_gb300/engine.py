@@ -217,6 +217,14 @@ class Plan:
     def capture(self, ctx, state):
         check(N.lib.qsg_plan_capture(ctx.h, self.h, state.get()))
 
+    def profile(self, ctx, state):
+        """Per-op milliseconds (CUDA events around each launch)."""
+        n = len(self)
+        ms = np.zeros(max(1, n), dtype=np.float32)
+        check(N.lib.qsg_plan_profile(ctx.h, self.h, state.get(),
+                                     ms.ctypes.data_as(N.P_f32), n))
+        return ms[:n]
+
     def replay(self, ctx):
         check(N.lib.qsg_plan_replay(ctx.h, self.h))
 

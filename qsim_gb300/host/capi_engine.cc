@@ -305,6 +305,15 @@ int qsg_plan_capture(qsg_ctx* ctx, qsg_plan* p, float* state) {
   return p->rt.capture(ctx, state);
 }
 
+int qsg_plan_profile(qsg_ctx* ctx, qsg_plan* p, float* state, float* op_ms,
+                     uint64_t cap) {
+  if (!ctx || !p || !state || !op_ms) return invalid("null argument");
+  std::vector<float> ms;
+  int rc = p->rt.profile(ctx, state, &ms);
+  std::copy(ms.begin(), ms.begin() + std::min<size_t>(ms.size(), cap), op_ms);
+  return rc;
+}
+
 int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p) {
   if (!ctx || !p) return invalid("null argument");
   return p->rt.replay(ctx);

@@ -184,6 +184,40 @@ Block grow_block(const Circuit& c, const std::vector<char>& done, size_t first,
 
 }  // namespace
 
+// Pads a block to 6 targets with the identity on the lowest free qubits
+// (the tensor-core kernel's fixed shape).
+void pad_block_to_6(unsigned n, PlanOp& po) {
+  const unsigned k = po.qs.size();
+  if (k >= 6 || n < 6) return;
+  std::vector<unsigned> all = po.qs;
+  for (unsigned q = 0; all.size() < 6 && q < n; ++q)
+    if (std::find(all.begin(), all.end(), q) == all.end()) all.push_back(q);
+  std::sort(all.begin(), all.end());
+  unsigned pos[6];
+  unsigned tmask = 0;
+  for (unsigned j = 0; j < k; ++j) {
+    pos[j] = unsigned(std::find(all.begin(), all.end(), po.qs[j]) - all.begin());
+    tmask |= 1u << pos[j];
+  }
+  auto sub = [&](unsigned i) {
+    unsigned r = 0;
+    for (unsigned j = 0; j < k; ++j) r |= ((i >> pos[j]) & 1) << j;
+    return r;
+  };
+  const unsigned d = 1u << k;
+  std::vector<cplx> m6(64 * 64, 0.0);
+  for (unsigned r = 0; r < 64; ++r)
+    for (unsigned cc = 0; cc < 64; ++cc)
+      if ((r & ~tmask) == (cc & ~tmask)) m6[r * 64 + cc] = po.m[sub(r) * d + sub(cc)];
+  po.qs = all;
+  po.m = std::move(m6);
+  po.m32.resize(2 * po.m.size());
+  for (size_t i = 0; i < po.m.size(); ++i) {
+    po.m32[2 * i] = float(po.m[i].real());
+    po.m32[2 * i + 1] = float(po.m[i].imag());
+  }
+}
+
 Plan unfused(const Circuit& c) {
   Plan p;
   p.num_qubits = c.num_qubits;
@@ -284,7 +318,11 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
       po.members = best.members;
       for (int mi : best.members) done[mi] = 1;
       finish(c, po);
-      if (opt.tensor_path && po.qs.size() >= opt.tc_min_k) po.path = Path::kTensor;
+      if (opt.tensor_path && po.qs.size() >= opt.tc_min_k &&
+          c.num_qubits >= 12) {
+        pad_block_to_6(c.num_qubits, po);
+        po.path = Path::kTensor;
+      }
       plan.ops.push_back(std::move(po));
     }
     if (seg_end < nops) {

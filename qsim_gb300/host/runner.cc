@@ -195,6 +195,32 @@ int PlanRuntime::capture(qsg_ctx* c, float* state) {
   return QSG_OK;
 }
 
+int PlanRuntime::profile(qsg_ctx* c, float* state, std::vector<float>* ms) {
+  ctx = c;
+  int rc = upload(ctx);
+  if (rc) return rc;
+  rc = prepare_tc();
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(ctx_stream(ctx));
+  const size_t nops = plan.ops.size();
+  std::vector<cudaEvent_t> ev(nops + 1);
+  for (auto& e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], s);
+  for (size_t i = 0; i < nops; ++i) {
+    if (plan.ops[i].kind != OpKind::kMeasure) {
+      rc = launch_op(i, state);
+      if (rc) break;
+    }
+    cudaEventRecord(ev[i + 1], s);
+  }
+  cudaEventSynchronize(ev[nops]);
+  ms->assign(nops, 0.f);
+  for (size_t i = 0; rc == QSG_OK && i < nops; ++i)
+    cudaEventElapsedTime(&(*ms)[i], ev[i], ev[i + 1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
 int PlanRuntime::replay(qsg_ctx* c) {
   if (!graph_exec) {
     set_error_msg("plan has no captured graph");

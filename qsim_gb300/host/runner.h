@@ -19,6 +19,11 @@ size_t tc_operand_bytes(unsigned k);
 void tc_build_operands(unsigned k, const float* m32, void* host_out);
 
 void set_error_msg(const char* msg);
+// Pads a gate to 6 targets (identity on the lowest free qubits) for the
+// tensor-core path; m6_out holds 2 * 64 * 64 floats.
+void tc_pad_gate(unsigned n, const unsigned* qs, unsigned k, const float* m32,
+                 unsigned* qs6, float* m6_out);
+int tc_check_error(qsg_ctx* ctx, int* out);
 
 namespace host {
 
@@ -48,6 +53,9 @@ struct PlanRuntime {
   int run(qsg_ctx* ctx, float* state, unsigned seed,
           std::vector<uint64_t>* mbits);
   int capture(qsg_ctx* ctx, float* state);
+  // Runs the gate ops with a CUDA event around each; per-op milliseconds
+  // (measurements are skipped and get 0).
+  int profile(qsg_ctx* ctx, float* state, std::vector<float>* ms);
   int replay(qsg_ctx* ctx);
 };
 

@@ -253,6 +253,35 @@ def fuse_counts_case():
     print("fuser_mqubit_counts written")
 
 
+def config1_case():
+    """The 20-qubit 4x5 grid workload (depth 14, seed 1) through the
+    reference at max_fused_size 2 with 1000 samples (seed 1).  The full
+    state is too large to commit; the fixture keeps the reference's FP64
+    amplitudes at 4096 fixed indices, its norm, its samples from the FP32
+    (SIMD, fused) and FP64 states, and its fused-op count."""
+    sys.path.insert(0, ROOT)
+    from qsim_gb300 import engine as E
+    c = E.Circuit.grid(4, 5, 0, 14, 1)
+    n = c.num_qubits
+    ops = [dict(kind="g", time=o["time"], qs=o["qs"], m=o["m"]) for o in c.ops()]
+    with tempfile.TemporaryDirectory() as td:
+        gl = os.path.join(td, "g.txt")
+        write_gate_list(gl, n, ops)
+        out = os.path.join(td, "out")
+        subprocess.run([DRIVER, "run", gl, out, "2", "1000", "1"], check=True)
+        f64 = np.fromfile(out + ".f64", np.float64)[: 2 << n].view(np.complex128)
+        f32 = np.fromfile(out + ".f32", np.float32).view(np.complex64)
+        idx = np.sort(np.random.default_rng(4).choice(1 << n, 4096, replace=False))
+        meta = np.fromfile(out + ".meta", np.float64)
+        np.savez_compressed(
+            os.path.join(HERE, "config1_grid4x5d14.npz"), n=np.int32(n),
+            idx=idx.astype(np.int64), amp64=f64[idx],
+            ref_f32_rel_l2=np.float64(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+            s32=np.fromfile(out + ".s32", np.uint64),
+            s64=np.fromfile(out + ".s64", np.uint64), meta=meta)
+    print("config1_grid4x5d14 written")
+
+
 def mt_case():
     with tempfile.TemporaryDirectory() as td:
         out = {}
@@ -271,6 +300,7 @@ def main():
     mt_case()
     text_case("text_gates9", 9, 30, 5)
     fuse_counts_case()
+    config1_case()
     rng = np.random.default_rng(20261204)
     # k = 1..6 gates at random positions (covers low/high targets, pair and
     # non-pair layouts), FP32 fused at f=4, EVs of Pauli strings up to 6.

@@ -1,0 +1,147 @@
+"""GPU tests of the engine above the state-vector calls: fused plans run on
+the device against the oracle and the reference's golden outputs, CUDA-graph
+replay, measurements inside plans, expectation values of Pauli sums.
+
+Tolerances: FP32 state vs FP64, relative L2 <= 1e-5.  Samples of a whole
+circuit: the reference's own FP32 path matches its FP64 samples on 99.8% of
+the config-1 samples (FP32 rounding moves CDF boundaries), so full-circuit
+sample parity is >= 99.5% against both of the reference's sample sets."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def eng():
+    import qsim_gb300 as q
+    from qsim_gb300 import engine as E
+    ctx = q.Context(0)
+    return q, E, ctx, q.StateSpace(ctx=ctx), q.Simulator(ctx=ctx)
+
+
+def oracle_state(oracle, c):
+    n = c.num_qubits
+    s = oracle.zero_state(n)
+    for o in c.ops():
+        if o["kind"] == 0:
+            oracle.apply_gate(s, n, o["qs"], o["m"])
+        elif o["kind"] == 1:
+            oracle.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
+    return s
+
+
+def test_config1_grid20_against_reference(eng, oracle):
+    """20-qubit 4x5 grid, depth 14, max_fused_size 2, 1000 samples (seed 1):
+    final state vs the oracle (full) and the reference's FP64 amplitudes,
+    samples vs the reference's samples."""
+    q, E, ctx, ss, sim = eng
+    d = load_golden("config1_grid4x5d14")
+    c = E.Circuit.grid(4, 5, 0, 14, 1)
+    n = c.num_qubits
+    plan = E.Plan(c, max_fused_size=2)
+    st = ss.Create(n)
+    ss.SetStateZero(st)
+    plan.run(ctx, st)
+    got = ss.to_numpy(st)
+    assert rel_l2(got[d["idx"]], d["amp64"]) < TOL
+    assert rel_l2(got, oracle_state(oracle, c)) < TOL
+    smp = np.array(ss.Sample(st, 1000, 1), np.uint64)
+    assert np.mean(smp == d["s64"]) >= 0.995
+    assert np.mean(smp == d["s32"]) >= 0.995
+
+
+@pytest.mark.parametrize("f", [2, 3, 4, 5, 6])
+def test_fused_plans_on_device(eng, oracle, f):
+    q, E, ctx, ss, sim = eng
+    for c in (E.Circuit.grid(3, 5, 0, 12, 2), E.Circuit.layered_u3(13, 5, 3, 4),
+              E.Circuit.chain(16, 10, 3)):
+        want = oracle_state(oracle, c)
+        st = ss.Create(c.num_qubits)
+        ss.SetStateZero(st)
+        E.Plan(c, max_fused_size=f).run(ctx, st)
+        assert rel_l2(ss.to_numpy(st), want) < TOL
+
+
+def test_graph_capture_replay(eng, oracle):
+    q, E, ctx, ss, sim = eng
+    c = E.Circuit.grid(3, 6, 0, 10, 7)
+    n = c.num_qubits
+    want = oracle_state(oracle, c)
+    plan = E.Plan(c, max_fused_size=6)  # includes k = 6 ops (device matrices)
+    assert plan.info()["max_k"] == 6
+    st = ss.Create(n)
+    plan.capture(ctx, st)
+    for _ in range(2):  # replays are idempotent from |0>
+        ss.SetStateZero(st)
+        plan.replay(ctx)
+        ctx.sync()
+        assert rel_l2(ss.to_numpy(st), want) < TOL
+
+
+def test_plan_with_measurements(eng, oracle):
+    """Measurements inside a plan draw from std::mt19937(seed) and collapse
+    the state as StateSpace::Measure (lib/statespace.h:84-95)."""
+    q, E, ctx, ss, sim = eng
+    text = ("6\n0 h 0\n0 h 1\n0 h 2\n0 h 3\n0 h 4\n0 h 5\n"
+            "1 cz 0 1\n1 cz 2 3\n2 rx 4 0.7\n2 fs 1 2 0.5 0.25\n"
+            "3 m 0 2 4\n4 h 0\n4 cnot 1 5\n5 m 1 5\n")
+    c = E.Circuit.parse(text)
+    n = c.num_qubits
+    st = ss.Create(n)
+    ss.SetStateZero(st)
+    bits = E.Plan(c, max_fused_size=4).run(ctx, st, seed=5)
+    assert len(bits) == 2
+    # Emulate on the oracle with the same generator stream.
+    rng = q.Rng(5)
+    s = oracle.zero_state(n)
+    for o in c.ops():
+        if o["kind"] == 2:
+            mask = sum(1 << qq for qq in o["qs"])
+            u = rng.uniform(1.0)
+            idx = oracle.find_index(s, n, u * oracle.norm(s, n))
+            b = idx & mask
+            oracle.collapse(s, n, mask, b)
+            assert b == int(bits[0 if o["qs"] == [0, 2, 4] else 1])
+        else:
+            oracle.apply_gate(s, n, o["qs"], o["m"]) if o["kind"] == 0 else \
+                oracle.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
+    assert rel_l2(ss.to_numpy(st), s) < TOL
+
+
+def test_pauli_sum_expectation(eng, oracle):
+    """Config-3 shape at 14 qubits: U3 layers + CZ/CNOT + controlled U3,
+    then 64 Pauli strings of weight 1..6; FP64-reduced EVs within 1e-5."""
+    q, E, ctx, ss, sim = eng
+    from conftest import pauli_matrix
+    c = E.Circuit.layered_u3(14, 8, 8, 12)
+    n = c.num_qubits
+    st = ss.Create(n)
+    ss.SetStateZero(st)
+    E.Plan(c, max_fused_size=4).run(ctx, st)
+    ref = oracle_state(oracle, c)
+    total_gpu, total_ref = 0.0, 0.0
+    for qs, letters, coeff in E.pauli_sum(n, 64, 6, 13):
+        m = pauli_matrix(letters)
+        ev = sim.ExpectationValue(qs, np.ascontiguousarray(m.astype(np.complex64)).view(np.float32), st)
+        evr = oracle.expectation_value(ref, n, qs, m)
+        assert abs(ev - evr) < 1e-5
+        total_gpu += coeff * ev.real
+        total_ref += coeff * evr.real
+    assert abs(total_gpu - total_ref) < 1e-4
+
+
+def test_plan_profile_and_launch_count(eng):
+    q, E, ctx, ss, sim = eng
+    c = E.Circuit.grid(4, 5, 0, 6, 1)
+    plan = E.Plan(c, max_fused_size=4)
+    st = ss.Create(c.num_qubits)
+    ss.SetStateZero(st)
+    before = ctx.launches()
+    ms = plan.profile(ctx, st)
+    assert len(ms) == len(plan) and np.all(ms > 0)
+    assert ctx.launches() - before == len(plan)
