@@ -127,10 +127,15 @@ def max_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
-def traffic_from_profiles(n: int):
-    """dram read+write bytes per launch of the dominant kernel, from the
-    committed ncu summary (scaled from its capture size to n qubits)."""
-    p = os.path.join(ROOT, "profiles", "gate_tile_k4_plain_pass.md")
+def traffic_from_profiles(n: int, kernel: str):
+    """dram read+write bytes per launch of `kernel`, from its committed ncu
+    summary (scaled from the capture's qubit count to n: traffic grows in
+    proportion to the state)."""
+    name = {"gate_tile_kernel": "gate_tile_k4_plain_pass.md",
+            "tc_gate_kernel": "tc_gate_k6_pass.md"}.get(kernel)
+    if name is None:
+        return None
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     nq, tb = None, None
@@ -227,6 +232,10 @@ def run_engine(args, world, rank, local, dist):
     forms["plain_f4"] = E.Plan(c, max_fused_size=4)
     forms["plain_f5"] = E.Plan(c, max_fused_size=5)
     forms["plain_f6"] = E.Plan(c, max_fused_size=6)
+    # Tensor-core forms: blocks of >= tc_min_k qubits on tcgen05.
+    forms["tc_f6"] = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5)
+    forms["tc_f6_all"] = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=1)
+    forms["tc_f5_all"] = E.Plan(c, max_fused_size=5, tensor_path=True, tc_min_k=1)
 
     def time_form(plan, steps, warmup):
         plan.capture(ctx, st)
@@ -265,26 +274,41 @@ def run_engine(args, world, rank, local, dist):
     ms = max_over_ranks(dist, ms)
     value = ms / 1e3
 
-    # Roofline of the dominant kernel: per-op CUDA-event times of the plain
-    # f=4 plan; algorithmic bytes per launch = 16 * 2^n (one read + one
-    # write of the state).
+    # Roofline of the dominant kernel of the headline plan: per-op CUDA-event
+    # times; algorithmic bytes per launch = 16 * 2^n (one read + one write
+    # of the state).
     ss.SetStateZero(st)
-    prof = forms["plain_f4"].profile(ctx, st)
-    ops4 = forms["plain_f4"].ops()
-    ks = [len(o["qs"]) for o in ops4]
-    gate_ms = [t for t, k in zip(prof, ks)]
-    avg_launch_ms = float(np.mean(gate_ms))
-    achieved = 16.0 * (1 << n) / (avg_launch_ms * 1e-3) / 1e9
-    per_k = {}
-    for k in sorted(set(ks)):
-        ts = [t for t, kk in zip(prof, ks) if kk == k]
-        per_k[str(k)] = {"launches": len(ts), "avg_ms": float(np.mean(ts)),
-                         "gbs": 16.0 * (1 << n) / (float(np.mean(ts)) * 1e-3) / 1e9}
+    prof = head.profile(ctx, st)
+    hops = head.ops()
+    kern_of = lambda o: "tc_gate_kernel" if o["path"] == 1 else "gate_tile_kernel"
+    per_kernel = {}
+    for t, o in zip(prof, hops):
+        d = per_kernel.setdefault(kern_of(o), {"launches": 0, "total_ms": 0.0})
+        d["launches"] += 1
+        d["total_ms"] += float(t)
+    dom = max(per_kernel, key=lambda kname: per_kernel[kname]["total_ms"])
+    for kname, d in per_kernel.items():
+        d["avg_ms"] = d["total_ms"] / d["launches"]
+        d["gbs"] = 16.0 * (1 << n) / (d["avg_ms"] * 1e-3) / 1e9
+        d["share"] = d["total_ms"] / float(np.sum(prof))
+    achieved = per_kernel[dom]["gbs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic_from_profiles(n),
-                "kernel": "gate_tile_kernel (plain f=4 plan, all launches)",
-                "peak_source": peak_kind, "per_k": per_k}
+                "traffic": traffic_from_profiles(n, dom),
+                "kernel": dom, "peak_source": peak_kind,
+                "bytes_per_launch": 16 * (1 << n),
+                "per_kernel": per_kernel}
+    # Plain f=4 plan breakdown by gate size (CUDA-core tile kernel).
+    ss.SetStateZero(st)
+    prof4 = forms["plain_f4"].profile(ctx, st)
+    ops4 = forms["plain_f4"].ops()
+    ks = [len(o["qs"]) for o in ops4]
+    per_k = {}
+    for k in sorted(set(ks)):
+        ts = [t for t, kk in zip(prof4, ks) if kk == k]
+        per_k[str(k)] = {"launches": len(ts), "avg_ms": float(np.mean(ts)),
+                         "gbs": 16.0 * (1 << n) / (float(np.mean(ts)) * 1e-3) / 1e9}
+    roofline["plain_f4_per_k"] = per_k
 
     # End to end through the public API with host buffers.
     hbuf = C.c_void_p()

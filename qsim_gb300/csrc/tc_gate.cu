@@ -10,21 +10,29 @@
 //   * Real form: out = A_real * in with A_real the 128 x 128 matrix
 //     [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im), and `in` the
 //     tile's 64 groups x 128 real components.  One CTA tile = 64 groups x 64
-//     members = 4096 amplitudes; D (128 x 64 FP32) lives in tensor memory.
+//     members = 4096 amplitudes (32 KiB).
 //   * Split TF32: A = A_hi + A_lo and B = B_hi + B_lo with every part
 //     pre-rounded to TF32; D = A_hi B_hi + A_hi B_lo + A_lo B_hi (3 x 16
 //     MMAs of M=128, N=64, K=8), FP32 accumulation.  The dropped A_lo B_lo
 //     term and the rounding of the lo parts leave ~2^-21 relative error per
 //     product, the FP32 level of the CUDA-core path.
-//   * Operands sit in shared memory in the canonical no-swizzle K-major
-//     layout (8-row x 16-byte core matrices; LBO = 128 B between core
-//     matrices along K, SBO = 4 KiB between 8-row blocks).  The gate's two
-//     parts (128 KiB) are copied once per CTA; amplitudes arrive with 8-byte
-//     cp.async straight into their (group, member) slots, double buffered.
+//   * Tensor memory holds the gate (A_hi, A_lo: 2 x 128 columns, loaded once
+//     per CTA) and two 64-column accumulators, so the MMAs of tile i run
+//     while the epilogue of tile i-1 drains the other accumulator.
+//   * Shared memory: three raw tile buffers fed by 16-byte cp.async in tile
+//     order (three tiles in flight per SM), and two operand buffers (hi, lo)
+//     in the canonical no-swizzle K-major layout (8-row x 16-byte core
+//     matrices; LBO = 128 B along K, SBO = 4 KiB between 8-row blocks),
+//     written by a split pass with conflict-free 128-bit stores.
 //   * One thread issues the MMAs and commits them to an mbarrier; every wait
-//     is bounded and sets an error flag instead of hanging.  The epilogue
-//     reads D with tcgen05.ld, pairs re/im lanes with a shuffle and stores
-//     amplitudes to HBM.
+//     is bounded by a clock budget and sets an error flag instead of hanging.
+//     The epilogue reads D with tcgen05.ld, pairs re/im lanes with a shuffle,
+//     stages the tile in shared memory and stores it with coalesced 128-bit
+//     writes.
+//
+// All tile addressing is bitwise linear: a tile index e (12 bits) maps each
+// of its bits to one state bit, one group bit or one member bit, so every
+// offset is an OR of a per-thread part and a per-iteration table entry.
 
 #include <algorithm>
 #include <cmath>
@@ -38,32 +46,46 @@ namespace qsg {
 
 namespace tc {
 
-constexpr int kThreads = 128;
+// Warp roles: 8 producer warps (split raw tiles into operands, refill raw
+// buffers), 8 epilogue warps (drain tensor memory, stage, store; two per TMEM
+// lane quadrant) and one MMA warp (its lane 0 issues every tcgen05.mma).
+constexpr int kProdWarps = 8, kEpiWarps = 8;
+constexpr int kProdThreads = 32 * kProdWarps;            // 256
+constexpr int kEpiThreads = 32 * kEpiWarps;              // 256
+constexpr int kThreads = kProdThreads + kEpiThreads + 32;  // 544
+constexpr int kRoleBits = 8;                              // log2(256)
 constexpr int kK = 6;                  // targets per tensor-core gate
 constexpr int kD = 1 << kK;            // members per group (64)
 constexpr int kReal = 2 * kD;          // real dimension (128) = M = K
 constexpr int kGroups = 64;            // N
 constexpr int kTileBits = 12;          // 64 groups x 64 members
 constexpr int kTileAmps = 1 << kTileBits;
-constexpr uint32_t kABytes = kReal * kReal * 4;        // 64 KiB per part
-constexpr uint32_t kBBytes = kGroups * kReal * 4;      // 32 KiB per buffer
-constexpr uint32_t kLBO = 128;                          // K-adjacent cores
-constexpr uint32_t kSBOA = (kReal / 4) * 128;           // 4 KiB
-constexpr uint32_t kSBOB = (kReal / 4) * 128;           // 4 KiB
-constexpr uint32_t kTmemCols = 128;   // D uses 64; headroom
-constexpr long long kWaitCycles = 4000000000LL;         // ~2 s at 2 GHz
+constexpr uint32_t kARowFloats = kReal;                  // A row length
+constexpr uint32_t kOperandFloats = 2 * kReal * kReal;   // A_hi | A_lo
+constexpr uint32_t kTileBytes = kTileAmps * 8;           // 32 KiB
+constexpr uint32_t kLBO = 128;                           // K-adjacent cores
+constexpr uint32_t kSBOB = (kReal / 4) * 128;            // 4 KiB
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmemAhi = 0, kTmemAlo = 128, kTmemD = 256;  // columns
+constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
+constexpr int kRawStages = 3;
+constexpr int kUnitsPerRole = kTileAmps / 2 / kProdThreads;  // 8 (= epilogue)
 
 // Shared-memory map (bytes).
-constexpr uint32_t kOffAhi = 0;
-constexpr uint32_t kOffAlo = kOffAhi + kABytes;
-constexpr uint32_t kOffB0 = kOffAlo + kABytes;
-constexpr uint32_t kOffB1 = kOffB0 + kBBytes;
-constexpr uint32_t kOffBlo = kOffB1 + kBBytes;
-constexpr uint32_t kOffTabLoadS = kOffBlo + kBBytes;     // 32 x u32
-constexpr uint32_t kOffTabLoadG = kOffTabLoadS + 128;    // 32 x u64
-constexpr uint32_t kOffTabGroup = kOffTabLoadG + 256;    // 64 x u64
-constexpr uint32_t kOffBar = kOffTabGroup + 512;         // mbarrier
-constexpr uint32_t kOffTmem = kOffBar + 16;              // tmem address
+constexpr uint32_t kOffRaw = 0;                                  // 3 x 32 KiB
+constexpr uint32_t kOffOp = kOffRaw + kRawStages * kTileBytes;    // 2 x 64 KiB
+constexpr uint32_t kOpBytes = 2 * kTileBytes;                     // hi | lo
+// The epilogue stages its output tile in the operand buffer of that tile
+// (its MMAs have completed when the accumulator is full).
+constexpr uint32_t kOffTabG = kOffOp + 2 * kOpBytes;    // 8 x u64 unit goff
+constexpr uint32_t kOffTabSplitE = kOffTabG + 64;       // 8 x u32 raw index
+constexpr uint32_t kOffTabSplitO = kOffTabSplitE + 32;  // 8 x u32 op offset
+constexpr uint32_t kOffTabGrpE = kOffTabSplitO + 32;    // 64 x u32 group e
+constexpr uint32_t kOffTabRd = kOffTabGrpE + 256;       // 8 x u32 stage read
+constexpr uint32_t kOffTabWr = kOffTabRd + 32;          // 8 x u32 raw write
+constexpr uint32_t kOffBar = kOffTabWr + 32;            // 9 mbarriers
+constexpr uint32_t kOffFlag = kOffBar + 80;             // failure flag
+constexpr uint32_t kOffTmem = kOffFlag + 16;
 constexpr uint32_t kSmemBytes = kOffTmem + 16;
 
 static_assert(kSmemBytes <= 232448, "shared memory budget");
@@ -85,11 +107,18 @@ struct TcGeom {
   uint32_t tile_is_target[kTileBits];
   uint32_t target_slot[kTileBits];   // member bit of a target tile bit
   uint32_t group_slot[kTileBits];    // group bit of a non-target tile bit
+  // XOR swizzles of tile indices, X(e) = OR_i bit(e, src[i]) << dst[i] with
+  // src >= 4 and dst < 4, so that the accesses of a half-warp fall on
+  // distinct banks.  `out`: epilogue staging (8-byte writes by member x
+  // group-bit-3 lanes, 16-byte linear reads).  `raw`: raw tile buffer
+  // (16-byte cp.async writes, 8-byte split reads); it never touches bit 0.
+  uint32_t out_src[4], out_dst[4], out_n;
+  uint32_t raw_src[4], raw_dst[4], raw_n;
 };
 
 struct TcArgs {
   TcGeom g;
-  const uint4* operands;  // A_hi | A_lo smem images (kABytes each)
+  const float* operands;  // A_hi | A_lo, row-major 128 x 128 each
   int* error;             // set on a timed-out wait
 };
 
@@ -109,7 +138,7 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo,
 }
 
 // Instruction descriptor: D = F32, A = B = TF32, both K-major, N = 64,
-// M = 128.
+// M = 128 (A is read from tensor memory).
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) |
                             (uint32_t(kGroups >> 3) << 17) |
                             (uint32_t(kReal >> 4) << 24);
@@ -158,14 +187,35 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b,
-                                         uint32_t accumulate) {
+// D[tmem] (+)= A[tmem] * B[smem descriptor].
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem,
+                                            uint64_t b, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(
           d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate)
       : "memory");
+}
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr,
+                                          const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};\n" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]),
+      "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]),
+      "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]),
+      "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]),
+      "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]),
+      "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -191,6 +241,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+        "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
@@ -213,16 +274,47 @@ __device__ __forceinline__ uint64_t tile_goff(uint32_t e, const TcGeom& g) {
   return o;
 }
 
-// Tile index e -> byte offset of its 8-byte amplitude in a B buffer.
-__device__ __forceinline__ uint32_t tile_soff(uint32_t e, const TcGeom& g) {
-  uint32_t n = 0, m = 0;
+// Group n (6 bits) and member m (6 bits) -> tile index e.
+__device__ __forceinline__ uint32_t tile_e(uint32_t n, uint32_t m,
+                                           const TcGeom& g) {
+  uint32_t e = 0;
 #pragma unroll
   for (int j = 0; j < kTileBits; ++j) {
-    const uint32_t bit = (e >> j) & 1;
-    if (g.tile_is_target[j]) m |= bit << g.target_slot[j];
-    else n |= bit << g.group_slot[j];
+    const uint32_t bit = g.tile_is_target[j] ? (m >> g.target_slot[j]) & 1
+                                             : (n >> g.group_slot[j]) & 1;
+    e |= bit << j;
   }
-  return kmajor_off(n, 2 * m, kSBOB);
+  return e;
+}
+
+// Split-pass work item idx (11 bits) = (n bits 0-2 | pair p << 3 |
+// n bits 3-5 << 8): the 16-byte operand row chunk of group n, members 2p
+// and 2p+1.  Lanes 0..7 of a warp cover the 8 rows of one core matrix, so
+// the 128-bit operand stores are conflict free.
+__device__ __forceinline__ uint32_t split_n(uint32_t idx) {
+  return (idx & 7) | ((idx >> 8) << 3);
+}
+__device__ __forceinline__ uint32_t split_p(uint32_t idx) {
+  return (idx >> 3) & 31;
+}
+__host__ __device__ __forceinline__ uint32_t op_off(uint32_t n, uint32_t p) {
+  return (n / 8) * kSBOB + p * kLBO + (n % 8) * 16;
+}
+
+__device__ __forceinline__ uint32_t swz_x(uint32_t e, const uint32_t* src,
+                                          const uint32_t* dst, uint32_t n) {
+  uint32_t x = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (i < int(n)) x |= ((e >> src[i]) & 1u) << dst[i];
+  return x;
+}
+// s(e) = e ^ X(e); for disjoint a, b: s(a | b) = s(a) ^ s(b).
+__device__ __forceinline__ uint32_t swz_out(uint32_t e, const TcGeom& g) {
+  return e ^ swz_x(e, g.out_src, g.out_dst, g.out_n);
+}
+__device__ __forceinline__ uint32_t swz_raw(uint32_t e, const TcGeom& g) {
+  return e ^ swz_x(e, g.raw_src, g.raw_dst, g.raw_n);
 }
 
 __device__ __forceinline__ uint64_t expand_outer_tc(uint64_t t,
@@ -236,45 +328,85 @@ __device__ __forceinline__ uint64_t expand_outer_tc(uint64_t t,
   return x;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// Named barrier over `count` threads; returns true if any of them passed
+// true (bar.red.or).
+__device__ __forceinline__ bool bar_or(int id, int count, bool v) {
+  uint32_t out;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n"
+      " bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(out)
+      : "r"(uint32_t(v)), "r"(id), "r"(count)
+      : "memory");
+  return out != 0;
+}
+
+__device__ __forceinline__ void bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+
+// Bounded wait on an mbarrier phase; false if the clock budget ran out or
+// another role already failed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* flag) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*flag) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *flag = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gate_kernel(float2* __restrict__ st, const __grid_constant__ TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const TcGeom& g = a.g;
   const uint32_t tid = threadIdx.x;
   const uint32_t warp = tid / 32, lane = tid % 32;
-  uint32_t* tab_ls = reinterpret_cast<uint32_t*>(smem + kOffTabLoadS);
-  uint64_t* tab_lg = reinterpret_cast<uint64_t*>(smem + kOffTabLoadG);
-  uint64_t* tab_grp = reinterpret_cast<uint64_t*>(smem + kOffTabGroup);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kOffBar);
+  uint64_t* tab_g = reinterpret_cast<uint64_t*>(smem + kOffTabG);
+  uint32_t* tab_se = reinterpret_cast<uint32_t*>(smem + kOffTabSplitE);
+  uint32_t* tab_so = reinterpret_cast<uint32_t*>(smem + kOffTabSplitO);
+  uint32_t* tab_ge = reinterpret_cast<uint32_t*>(smem + kOffTabGrpE);
+  uint32_t* tab_rd = reinterpret_cast<uint32_t*>(smem + kOffTabRd);
+  uint32_t* tab_wr = reinterpret_cast<uint32_t*>(smem + kOffTabWr);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kOffBar);
+  uint64_t* op_full = bars + 0;   // [2] producers -> MMA
+  uint64_t* op_free = bars + 2;   // [2] epilogue (staging read out) -> producers
+  uint64_t* acc_full = bars + 4;  // [2] MMA commit -> epilogue
+  uint64_t* acc_free = bars + 6;  // [2] epilogue -> MMA
+  uint64_t* gate_ready = bars + 8;  // epilogue (gate in TMEM) -> MMA
+  volatile int* flag = reinterpret_cast<volatile int*>(smem + kOffFlag);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kOffTmem);
   const uint32_t sbase = smem_u32(smem);
 
-  // Gate operands: one copy per CTA.
-  for (uint32_t i = tid; i < 2 * kABytes / 16; i += kThreads)
-    cp_async16(sbase + kOffAhi + 16 * i, a.operands + i);
-  cp_commit();
-
-  // Address tables.  Tile index e = lo7 | (j << 7): offsets are bitwise
-  // linear in e, so per-thread bases OR per-j table entries.
-  if (tid < 32) {
-    tab_ls[tid] = tile_soff(tid << 7, g);
-    tab_lg[tid] = tile_goff(tid << 7, g);
+  // ---- set-up ------------------------------------------------------------
+  // Unit u = rtid + 256 j (rtid: thread index inside a role, j < 8) of a
+  // tile is tile index e = 2u: bits 1..8 from rtid, bits 9..11 from j.
+  if (tid < kUnitsPerRole) {
+    tab_g[tid] = tile_goff(uint32_t(tid) << (kRoleBits + 1), g);
+    tab_rd[tid] = swz_out(uint32_t(tid) << (kRoleBits + 1), g);
+    tab_wr[tid] = swz_raw(uint32_t(tid) << (kRoleBits + 1), g);
+    // Split item idx = rtid + 256 j: j supplies idx bits 8..10 (n bits 3-5).
+    const uint32_t idx = tid << kRoleBits;
+    tab_se[tid] = swz_raw(tile_e(split_n(idx), 2 * split_p(idx), g), g);
+    tab_so[tid] = op_off(split_n(idx), split_p(idx));
   }
-  if (tid < kGroups) {
-    uint32_t e = 0, gi = tid;
-    for (int j = 0; j < kTileBits; ++j) {
-      if (!g.tile_is_target[j]) {
-        e |= (gi & 1) << j;
-        gi >>= 1;
-      }
-    }
-    tab_grp[tid] = tile_goff(e, g);
-  }
+  if (tid < kGroups) tab_ge[tid] = swz_out(tile_e(tid, 0, g), g);
   if (tid == 0) {
-    mbar_init(bar, 1);
+    for (int i = 0; i < 9; ++i) mbar_init(&bars[i], 1);
+    *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {
+  const uint32_t mma_warp = kProdWarps + kEpiWarps;
+  if (warp == mma_warp) {
     asm volatile(
         "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
             smem_u32(tmem_slot)),
@@ -288,135 +420,177 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const uint64_t step = gridDim.x;
+  const uint64_t t0 = blockIdx.x;
 
-  const uint32_t my_ls = tile_soff(tid, g);
-  const uint64_t my_lg = tile_goff(tid, g);
-
-  // Epilogue role: TMEM lane = 32*warp + lane = output row 2r + part.
-  const uint32_t row = 32 * warp + lane;
-  const uint32_t r_member = row / 2;
-  uint64_t member_goff = 0;
-  {
-    uint32_t e = 0, mi = r_member;
-    for (int j = 0; j < kTileBits; ++j) {
-      if (g.tile_is_target[j]) {
-        e |= ((mi >> g.target_slot[j]) & 1) << j;
-      }
-    }
-    member_goff = tile_goff(e, g);
-  }
-
-  auto issue_loads = [&](uint64_t t, uint32_t boff) {
-    if (t < g.num_tiles) {
-      const uint64_t base = expand_outer_tc(t, g);
-      const float2* gp = st + (base | my_lg);
-#pragma unroll 8
-      for (int j = 0; j < kTileAmps / kThreads; ++j) {
-        cp_async8(sbase + boff + (my_ls | tab_ls[j]), gp + tab_lg[j]);
-      }
-    }
-    cp_commit();
-  };
-
-  uint64_t t = blockIdx.x;
-  issue_loads(t, kOffB0);
-  issue_loads(t + gridDim.x, kOffB1);
-  cp_wait<2>();  // the operand group is complete
-  uint32_t phase = 0;
-  bool failed = false;
-
-  for (int stage = 0; t < g.num_tiles; t += gridDim.x, stage ^= 1) {
-    const uint32_t boff = stage ? kOffB1 : kOffB0;
-    cp_wait<1>();
-    __syncthreads();
-    // Split the tile: hi (in place) and lo parts, both TF32-exact.
-    {
-      float4* hb = reinterpret_cast<float4*>(smem + boff);
-      float4* lb = reinterpret_cast<float4*>(smem + kOffBlo);
-      for (uint32_t i = tid; i < kBBytes / 16; i += kThreads) {
-        float4 x = hb[i], h, l;
-        h.x = tf32_round(x.x); l.x = tf32_round(x.x - h.x);
-        h.y = tf32_round(x.y); l.y = tf32_round(x.y - h.y);
-        h.z = tf32_round(x.z); l.z = tf32_round(x.z - h.z);
-        h.w = tf32_round(x.w); l.w = tf32_round(x.w - h.w);
-        hb[i] = h;
-        lb[i] = l;
-      }
-    }
-    fence_async_smem();
-    __syncthreads();
-
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t ahi = sbase + kOffAhi, alo = sbase + kOffAlo;
-      const uint32_t bhi = sbase + boff, blo = sbase + kOffBlo;
-      uint32_t acc = 0;
-#pragma unroll 1
-      for (int kk = 0; kk < kReal / 8; ++kk) {
-        const uint32_t ko = kk * 2 * kLBO;  // two core matrices per K=8
-        mma_tf32(tmem, make_desc(ahi + ko, kLBO, kSBOA),
-                 make_desc(bhi + ko, kLBO, kSBOB), acc);
-        acc = 1;
-        mma_tf32(tmem, make_desc(ahi + ko, kLBO, kSBOA),
-                 make_desc(blo + ko, kLBO, kSBOB), 1);
-        mma_tf32(tmem, make_desc(alo + ko, kLBO, kSBOA),
-                 make_desc(bhi + ko, kLBO, kSBOB), 1);
-      }
-      mma_commit(bar);
-    }
-    // Bounded wait for the MMAs of this tile.
-    {
-      const long long t0 = clock64();
-      while (!mbar_try_wait(bar, phase)) {
-        if (clock64() - t0 > kWaitCycles) {
-          failed = true;
-          break;
-        }
-      }
-      phase ^= 1;
-    }
-    if (__syncthreads_or(failed)) {
-      if (tid == 0) atomicExch(a.error, 1);
-      failed = true;
-      break;
-    }
-    tc_fence_after();
-
-    // Epilogue: row `row` of D holds output component (r_member, row & 1)
-    // of the 64 groups.  Even lanes store groups 0..31, odd lanes 32..63.
-    const uint64_t base = expand_outer_tc(t, g);
-    uint32_t v0[32], v1[32];
-    const uint32_t taddr = tmem + ((32 * warp) << 16);
-    tmem_ld32(taddr, v0);
-    tmem_ld32(taddr + 32, v1);
-    tmem_wait_ld();
-    const bool odd = lane & 1;
+  if (warp < kProdWarps) {
+    // ======================== producers ==================================
+    const uint32_t rt = tid;
+    const uint64_t my_g = tile_goff(rt << 1, g);
+    const uint32_t my_wr = swz_raw(rt << 1, g);
+    const uint32_t my_se = swz_raw(tile_e(split_n(rt), 2 * split_p(rt), g), g);
+    const uint32_t my_so = op_off(split_n(rt), split_p(rt));
+    uint32_t e_m1 = 0;
+    for (int j = 0; j < kTileBits; ++j)
+      if (g.tile_is_target[j] && g.target_slot[j] == 0) e_m1 = 1u << j;
+    e_m1 = swz_raw(e_m1, g);
+    auto issue_loads = [&](uint64_t t, int stage) {
+      if (t < g.num_tiles) {
+        const float4* gp = reinterpret_cast<const float4*>(
+            st + (expand_outer_tc(t, g) | my_g));
+        const uint32_t sdst = sbase + kOffRaw + stage * kTileBytes;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      // Even lane sends its value of columns 32..63, odd lane of 0..31.
-      const uint32_t send = odd ? v0[j] : v1[j];
-      const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, 1);
-      const uint32_t mine = odd ? v1[j] : v0[j];
-      const float re = __uint_as_float(odd ? recv : mine);
-      const float im = __uint_as_float(odd ? mine : recv);
-      const uint32_t grp = odd ? 32 + j : j;
-      st[base | member_goff | tab_grp[grp]] = make_float2(re, im);
+        for (int j = 0; j < kUnitsPerRole; ++j)
+          cp_async16(sdst + 8 * (my_wr ^ tab_wr[j]), gp + (tab_g[j] >> 1));
+      }
+      cp_commit();
+    };
+    for (int q = 0; q < kRawStages; ++q) issue_loads(t0 + q * step, q);
+    int i = 0;
+    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+      const int rs = i % kRawStages;
+      const int s = i & 1;
+      cp_wait<kRawStages - 1>();
+      // Operand buffer s is free once the epilogue read tile i-2 out of it
+      // (the ((i-2)/2)-th completion of op_free[s]).
+      bool bad = false;
+      if (i >= 2) bad = !mbar_wait(&op_free[s], ((i - 2) >> 1) & 1, flag);
+      if (bar_or(1, kProdThreads, bad)) break;
+      // Split the raw tile into hi / lo operand rows (K-major).
+      const float2* raw = reinterpret_cast<const float2*>(smem + kOffRaw + rs * kTileBytes);
+      const uint32_t obuf = kOffOp + s * kOpBytes;
+#pragma unroll
+      for (int j = 0; j < kUnitsPerRole; ++j) {
+        const uint32_t e0 = my_se ^ tab_se[j];
+        const float2 x0 = raw[e0];
+        const float2 x1 = raw[e0 ^ e_m1];
+        float4 h, l;
+        h.x = tf32_round(x0.x); l.x = tf32_round(x0.x - h.x);
+        h.y = tf32_round(x0.y); l.y = tf32_round(x0.y - h.y);
+        h.z = tf32_round(x1.x); l.z = tf32_round(x1.x - h.z);
+        h.w = tf32_round(x1.y); l.w = tf32_round(x1.y - h.w);
+        const uint32_t o = my_so | tab_so[j];
+        *reinterpret_cast<float4*>(smem + obuf + o) = h;
+        *reinterpret_cast<float4*>(smem + obuf + kTileBytes + o) = l;
+      }
+      fence_async_smem();
+      bar_sync(1, kProdThreads);
+      if (rt == 0) mbar_arrive(&op_full[s]);
+      issue_loads(t + kRawStages * step, rs);  // raw[rs] is consumed
     }
-    tc_fence_before();
-    __syncthreads();
-    issue_loads(t + 2 * uint64_t(gridDim.x), boff);
-  }
-  cp_wait<0>();
-  if (failed) {
-    // Give the MMAs of the abandoned tile one more bounded wait before the
-    // tensor memory they write is released.
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, phase ^ 1) && clock64() - t0 < kWaitCycles) {
+    cp_wait<0>();
+  } else if (warp < kProdWarps + kEpiWarps) {
+    // ======================== epilogue ===================================
+    const uint32_t et = tid - kProdThreads;
+    const uint32_t ew = warp - kProdWarps;
+    const uint32_t quad = warp % 4, chalf = ew / 4;  // TMEM lane quadrant
+    const uint32_t lane_base = (32 * quad) << 16;
+    const uint32_t row = 32 * quad + lane;
+    // Gate into tensor memory: rows of this quadrant, columns of this half
+    // (A_hi and A_lo, 64 columns each).
+    {
+      const float* ahi = a.operands + size_t(row) * kARowFloats + 64 * chalf;
+      const float* alo = a.operands + size_t(kReal) * kReal +
+                         size_t(row) * kARowFloats + 64 * chalf;
+      uint32_t r[32];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(ahi[32 * c + q]);
+        tmem_st32(tmem + lane_base + kTmemAhi + 64 * chalf + 32 * c, r);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(alo[32 * c + q]);
+        tmem_st32(tmem + lane_base + kTmemAlo + 64 * chalf + 32 * c, r);
+      }
+      tmem_wait_st();
+      tc_fence_before();
+      bar_sync(2, kEpiThreads);
+      if (et == 0) mbar_arrive(gate_ready);  // gate loaded: MMAs may start
+    }
+    const uint64_t my_g = tile_goff(et << 1, g);
+    const uint32_t my_rd = swz_out(et << 1, g);
+    const uint32_t my_me = swz_out(tile_e(0, row / 2, g), g);
+    int i = 0;
+    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+      const int s = i & 1;
+      const bool bad = !mbar_wait(&acc_full[s], (i >> 1) & 1, flag);
+      if (bar_or(2, kEpiThreads, bad)) break;
+      tc_fence_after();
+      uint32_t v[32];
+      tmem_ld32(tmem + lane_base + kTmemD + 64 * s + 32 * chalf, v);
+      tmem_wait_ld();
+      tc_fence_before();
+      bar_sync(2, kEpiThreads);
+      if (et == 0) mbar_arrive(&acc_free[s]);  // accumulator s drained
+      float2* stage = reinterpret_cast<float2*>(smem + kOffOp + s * kOpBytes);
+      const bool odd = lane & 1;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        // Of this warp's 32 columns, even lanes (re rows) keep the first 16
+        // groups and odd lanes (im rows) the last 16.
+        const uint32_t send = odd ? v[j] : v[16 + j];
+        const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, 1);
+        const uint32_t mine = odd ? v[16 + j] : v[j];
+        const float re = __uint_as_float(odd ? recv : mine);
+        const float im = __uint_as_float(odd ? mine : recv);
+        const uint32_t grp = 32 * chalf + (odd ? 16 + j : j);
+        stage[my_me ^ tab_ge[grp]] = make_float2(re, im);
+      }
+      bar_sync(2, kEpiThreads);
+      const uint64_t base = expand_outer_tc(t, g);
+      float4* gp = reinterpret_cast<float4*>(st + (base | my_g));
+      const float4* so = reinterpret_cast<const float4*>(stage);
+#pragma unroll
+      for (int j = 0; j < kUnitsPerRole; ++j) {
+        const uint32_t sidx = my_rd ^ tab_rd[j];
+        float4 w = so[sidx >> 1];
+        if (sidx & 1) w = make_float4(w.z, w.w, w.x, w.y);
+        gp[tab_g[j] >> 1] = w;
+      }
+      bar_sync(2, kEpiThreads);
+      if (et == 0) mbar_arrive(&op_free[s]);  // operand buffer s free
+    }
+  } else if (lane == 0) {
+    // ======================== MMA issuer =================================
+    int i = 0;
+    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+      const int s = i & 1;
+      if (!mbar_wait(&op_full[s], (i >> 1) & 1, flag)) break;
+      // The gate must be in tensor memory before the first MMA, and
+      // accumulator s is free once the epilogue drained tile i-2 (the
+      // ((i-2)/2)-th completion of acc_free[s]).
+      if (i == 0) {
+        if (!mbar_wait(gate_ready, 0, flag)) break;
+      } else if (i >= 2) {
+        if (!mbar_wait(&acc_free[s], ((i - 2) >> 1) & 1, flag)) break;
+      }
+      tc_fence_after();
+      const uint32_t obuf = kOffOp + s * kOpBytes;
+      const uint32_t d = tmem + kTmemD + 64 * s;
+      const uint64_t dhi = make_desc(sbase + obuf, kLBO, kSBOB);
+      const uint64_t dlo = make_desc(sbase + obuf + kTileBytes, kLBO, kSBOB);
+#pragma unroll
+      for (int kk = 0; kk < kReal / 8; ++kk) {
+        const uint64_t ko = uint64_t(kk) * (2 * kLBO >> 4);
+        mma_tf32_ts(d, tmem + kTmemAhi + 8 * kk, dhi + ko, kk > 0);
+        mma_tf32_ts(d, tmem + kTmemAhi + 8 * kk, dlo + ko, 1);
+        mma_tf32_ts(d, tmem + kTmemAlo + 8 * kk, dhi + ko, 1);
+      }
+      mma_commit(&acc_full[s]);
     }
   }
-  tc_fence_before();
+
+  // ---- tear-down -----------------------------------------------------------
   __syncthreads();
-  if (warp == 0) {
+  if (warp == mma_warp) {
+    if (*flag) {
+      if (lane == 0) atomicExch(a.error, 1);
+      // The MMAs of an abandoned tile get one more bounded wait before
+      // their tensor memory is released.
+      const long long c0 = clock64();
+      while (clock64() - c0 < kWaitCycles / 4) {
+      }
+    }
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(
                      tmem),
@@ -465,10 +639,10 @@ static float tf32_host(float x) {
   return r;
 }
 
-// A_real images (hi, lo) in the K-major no-swizzle shared-memory layout.
+// A_real (hi, lo), row-major 128 x 128 each: row 2r+pr, column 2c+pc.
 static void build_a_images(const float* m6, unsigned char* out) {
   float* hi = reinterpret_cast<float*>(out);
-  float* lo = reinterpret_cast<float*>(out + kABytes);
+  float* lo = hi + kReal * kReal;
   for (uint32_t r = 0; r < kD; ++r)
     for (uint32_t c = 0; c < kD; ++c) {
       const float mr = m6[2 * (r * kD + c)], mi = m6[2 * (r * kD + c) + 1];
@@ -478,7 +652,7 @@ static void build_a_images(const float* m6, unsigned char* out) {
           const float x = v[pr][pc];
           const float h = tf32_host(x);
           const float l = tf32_host(x - h);
-          const uint32_t off = kmajor_off(2 * r + pr, 2 * c + pc, kSBOA) / 4;
+          const size_t off = size_t(2 * r + pr) * kReal + (2 * c + pc);
           hi[off] = h;
           lo[off] = l;
         }
@@ -515,6 +689,38 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
     }
   }
   if (tslot != kK || gslot != 6) return false;
+  // Swizzles.  Tile positions of group bits and member bits:
+  unsigned gpos[6], tpos[6];
+  for (unsigned j = 0; j < tb; ++j) {
+    if (g.tile_is_target[j]) tpos[g.target_slot[j]] = j;
+    else gpos[g.group_slot[j]] = j;
+  }
+  auto build = [](const std::vector<unsigned>& vary, unsigned allowed,
+                  uint32_t* src, uint32_t* dst, uint32_t* n) {
+    unsigned covered = 0;
+    std::vector<unsigned> srcs;
+    for (unsigned p : vary) {
+      if (p < 4) covered |= 1u << p;
+      else srcs.push_back(p);
+    }
+    std::vector<unsigned> dsts;
+    for (unsigned b2 = 0; b2 < 4; ++b2)
+      if (((allowed >> b2) & 1) && !((covered >> b2) & 1)) dsts.push_back(b2);
+    *n = unsigned(std::min(srcs.size(), dsts.size()));
+    for (unsigned i = 0; i < *n; ++i) {
+      src[i] = srcs[i];
+      dst[i] = dsts[i];
+    }
+  };
+  // Epilogue writes: half-warp lanes vary member bits 0..2 and group bit 4
+  // (even lanes keep groups 0..15 of a warp's 32 columns, odd lanes 16..31).
+  build({tpos[0], tpos[1], tpos[2], gpos[4]}, 0xF, g.out_src, g.out_dst,
+        &g.out_n);
+  // Split reads: half-warp lanes vary group bits 0..2 and member bit 1
+  // (pair bit 0); 16-byte units keep bit 0 in place.
+  build({gpos[0], gpos[1], gpos[2], tpos[1]}, 0xE, g.raw_src, g.raw_dst,
+        &g.raw_n);
+
   std::vector<unsigned> ins(qs6 + kK - h, qs6 + kK);
   std::sort(ins.begin(), ins.end());
   g.n_ins = ins.size();
@@ -525,7 +731,7 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
 
 }  // namespace tc
 
-size_t tc_operand_bytes(unsigned) { return 2 * size_t(tc::kABytes); }
+size_t tc_operand_bytes(unsigned) { return size_t(tc::kOperandFloats) * 4; }
 
 void tc_build_operands(unsigned k, const float* m32, void* host_out) {
   // The plan stores matrices already padded to 6 targets (k == 6).
@@ -543,6 +749,19 @@ void tc_pad_gate(unsigned n, const unsigned* qs, unsigned k, const float* m32,
 
 static int* g_tc_err = nullptr;
 
+// One-time set-up (error flag, shared-memory opt-in); must precede any
+// graph capture that contains tensor-core launches.
+int tc_setup() {
+  if (!g_tc_err) {
+    QSG_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
+    QSG_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
+    QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(tc::kSmemBytes)));
+  }
+  return QSG_OK;
+}
+
 int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
                   unsigned k, const float* m32, const void* operands) {
   using namespace tc;
@@ -559,19 +778,10 @@ int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
     set_error("tensor-core gate without device operands");
     return QSG_ERR_INVALID;
   }
-  a.operands = static_cast<const uint4*>(operands);
-  if (!g_tc_err) {
-    QSG_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
-    QSG_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
-  }
+  a.operands = static_cast<const float*>(operands);
+  int rc0 = tc_setup();
+  if (rc0) return rc0;
   a.error = g_tc_err;
-  static bool attr = false;
-  if (!attr) {
-    QSG_CUDA(cudaFuncSetAttribute(tc_gate_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(kSmemBytes)));
-    attr = true;
-  }
   const uint64_t grid = std::min<uint64_t>(a.g.num_tiles, ctx->num_sms);
   tc_gate_kernel<<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
       reinterpret_cast<float2*>(state), a);

@@ -64,6 +64,13 @@ int PlanRuntime::upload(qsg_ctx* c) {
 
 int PlanRuntime::prepare_tc() {
   if (tc_ready) return QSG_OK;
+  for (const auto& op : plan.ops) {
+    if (op.kind == OpKind::kGate && op.path == Path::kTensor) {
+      int rc = tc_setup();
+      if (rc) return rc;
+      break;
+    }
+  }
   size_t total = 0;
   tc_off.assign(plan.ops.size(), size_t(-1));
   for (size_t i = 0; i < plan.ops.size(); ++i) {

@@ -24,6 +24,7 @@ void set_error_msg(const char* msg);
 void tc_pad_gate(unsigned n, const unsigned* qs, unsigned k, const float* m32,
                  unsigned* qs6, float* m6_out);
 int tc_check_error(qsg_ctx* ctx, int* out);
+int tc_setup();
 
 namespace host {
 
