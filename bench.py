@@ -364,8 +364,41 @@ def run_engine(args, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def kernel_case(spec: str, n: int, reps: int):
+    """Small profiling case: `spec` = "gate:q0,q1,.." (CUDA-core tile
+    kernel) or "tc:q0,.." (tensor-core kernel); one random unitary applied
+    `reps` times to a uniform n-qubit state."""
+    import numpy as np
+    import qsim_gb300 as q
+    from qsim_gb300 import _native as N
+    kind, qs = spec.split(":")
+    qs = [int(x) for x in qs.split(",")]
+    ctx = q.Context(0)
+    ss, sim = q.StateSpace(ctx=ctx), q.Simulator(ctx=ctx)
+    st = ss.Create(n)
+    ss.SetStateUniform(st)
+    k = len(qs)
+    rng = np.random.default_rng(0)
+    u, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) +
+                        1j * rng.normal(size=(1 << k, 1 << k)))
+    m = np.ascontiguousarray(u.astype(np.complex64)).view(np.float32)
+    for _ in range(reps):
+        if kind == "tc":
+            N.check(N.lib.qsg_apply_gate_tc(ctx.h, st.get(), n, N.u32_array(qs),
+                                            k, m.ctypes.data_as(N.P_f32)))
+        else:
+            sim.ApplyGate(qs, m, st)
+    ctx.sync()
+    print(json.dumps({"kernel_case": spec, "n": n, "reps": reps,
+                      "norm": ss.Norm(st)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel-case", default=None,
+                    help='profiling case "gate:q,..." or "tc:q,..."')
+    ap.add_argument("--qubits", type=int, default=26)
+    ap.add_argument("--reps", type=int, default=4)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -375,6 +408,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--distinct-replicas", action="store_true")
     args = ap.parse_args()
+    if args.kernel_case:
+        kernel_case(args.kernel_case, args.qubits, args.reps)
+        return
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local, dist = dist_setup()

@@ -1,0 +1,72 @@
+"""The C++ drop-in: header-only StateSpace / Simulator / Factory adapters in
+include/qsim_gb300/ that the reference's QSimRunner, MultiQubitGateFuser,
+ExpectationValue and QuantumTrajectorySimulator templates accept unchanged.
+
+CPU: both test programs compile and link against libqsim_gb300.so (the
+reference-runner program only where a qsim checkout is present: it includes
+the reference's own headers).  GPU: the adapter program runs a golden gate
+list through the adapters and matches the reference's outputs."""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden, rel_l2, unpack_ops
+
+LIBDIR = os.path.join(ROOT, "qsim_gb300", "_build")
+REF = os.environ.get("QSG_REFERENCE", "/root/reference")
+
+
+def compile_prog(src, out, extra=()):
+    cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+           *extra, os.path.join(ROOT, "tests", "cpp", src), "-o", out,
+           "-L" + LIBDIR, "-lqsim_gb300", "-Wl,-rpath," + LIBDIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_adapter_program_compiles(tmp_path):
+    compile_prog("adapter_run.cc", str(tmp_path / "adapter_run"))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lib")),
+                    reason="qsim checkout (reference headers) not present")
+def test_reference_runner_compiles_with_gb300_factory(tmp_path):
+    """QSimRunner<IO, MultiQubitGateFuser<IO>, FactoryGB300>,
+    ExpectationValue<IO, MultiQubitGateFuser<IO>> (both variants) and
+    QuantumTrajectorySimulator<IO, Runner> instantiate with the adapters."""
+    compile_prog("dropin_qsim_runner.cc", str(tmp_path / "dropin"),
+                 extra=("-I" + os.path.join(REF, "lib"),))
+
+
+@pytest.mark.gpu
+def test_adapter_program_matches_reference(tmp_path, oracle):
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from make_golden import write_gate_list
+    d = load_golden("rand14_k2")
+    n = int(d["n"])
+    ops = unpack_ops(d)
+    gl_ops = [dict(kind={0: "g", 1: "c"}[o["kind"]], time=i, qs=o["qs"],
+                   cqs=o["cqs"], cvals=o["cvals"], m=o["m"])
+              for i, o in enumerate(ops)]
+    gl = tmp_path / "gates.txt"
+    write_gate_list(str(gl), n, gl_ops)
+    exe = str(tmp_path / "adapter_run")
+    compile_prog("adapter_run.cc", exe)
+    out = str(tmp_path / "out")
+    qs = [int(q) for q in d["meas_qs"]]
+    r = subprocess.run([exe, str(gl), out, str(int(d["meas_seed"]))] +
+                       [str(q) for q in qs], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    state = np.fromfile(out + ".state", np.float32).view(np.complex64)
+    assert rel_l2(state.astype(np.complex128), d["f64"]) < 1e-5
+    # First Measure(qubits, mt19937(seed)) on the final state is the first
+    # of the reference's measurement sequence.
+    bits = np.fromfile(out + ".bits", np.uint64)[0]
+    assert int(bits) == int(d["meas_bits"][0])
+    samples = np.fromfile(out + ".samples", np.uint64)
+    want = oracle.sample(state.astype(np.complex128), n, 1000, 7)
+    assert np.mean(samples == want) >= 0.999
