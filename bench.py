@@ -331,6 +331,11 @@ def run_engine(args, world, rank, local, dist):
     N.lib.qsg_host_free(hbuf)
     e2e = max_over_ranks(dist, statistics.median(e2e_times))
 
+    # Batched trajectories (replicas for N > 1: every rank runs the batch).
+    traj = bench_trajectories(args.traj_streams, args.traj_f)
+    traj["wall_s"] = max_over_ranks(dist, traj["wall_s"])
+    traj["value"] = world * traj["trajectories"] / traj["wall_s"]
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         t, done, threads = cpu_sample(n, ops4, args.cpu_ops)
@@ -360,8 +365,59 @@ def run_engine(args, world, rank, local, dist):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "trajectories": traj,
         }
         print(json.dumps(line), flush=True)
+
+
+TRAJ = dict(circuits=128, reps=32, n_min=12, n_max=24, cycles=12,
+            p_depol=1e-3, gamma=5e-3, seed=4)
+TRAJ_WORKLOAD = ("4096 noisy trajectories: 128 chain random circuits, n ~ "
+                 "U{12..24}, depth 12, depolarizing 1e-3 after each gate "
+                 "qubit, amplitude damping 5e-3 per qubit per cycle, 32 "
+                 "repetitions each")
+
+
+def bench_trajectories(num_streams: int, max_fused_size: int = 4,
+                       warm: bool = True):
+    """Batched-trajectory workload: every trajectory from |0..0>, its final
+    state left normalised in HBM and its Kraus statistics copied to the
+    host.  traj/s = trajectories / batch wall time (host enqueue, device work
+    and the final synchronisation); latency = per-trajectory device time."""
+    import numpy as np
+    from qsim_gb300 import engine as E
+    rng = np.random.default_rng(TRAJ["seed"])
+    ns = rng.integers(TRAJ["n_min"], TRAJ["n_max"] + 1, size=TRAJ["circuits"])
+    t0 = time.perf_counter()
+    runners = []
+    for i, n in enumerate(ns):
+        c = E.Circuit.chain(int(n), TRAJ["cycles"], 1000 + i)
+        nc = E.NoisyCircuit.make(c, TRAJ["p_depol"], TRAJ["gamma"], 2)
+        runners.append(E.Trajectories(nc, max_fused_size=max_fused_size))
+    setup_s = time.perf_counter() - t0
+    items = [(i, r) for i in range(len(runners)) for r in range(TRAJ["reps"])]
+    if warm:
+        E.run_trajectory_batch(runners, [(i, 10**6) for i in range(len(runners))],
+                               num_streams=num_streams)
+    per, lat, wall = E.run_trajectory_batch(runners, items,
+                                            num_streams=num_streams)
+    amp_ops = sum(float(2 ** int(ns[i])) * runners[i].info()["num_fused_ops"]
+                  for i, _ in items)
+    escapes = 0
+    for (i, _), st in zip(items, per):
+        s = E.Trajectories.samples(st)
+        escapes += int(np.sum(s == 1))
+    return {
+        "value": len(items) / wall, "unit": "traj/s",
+        "wall_s": wall, "trajectories": len(items),
+        "latency_ms_p50": float(np.percentile(lat, 50)),
+        "latency_ms_p99": float(np.percentile(lat, 99)),
+        "streams": num_streams, "max_fused_size": max_fused_size,
+        "setup_s": setup_s,
+        "fused_pass_bytes_per_s": 16.0 * amp_ops / wall,
+        "non_default_kraus_choices": escapes,
+        "workload": TRAJ_WORKLOAD,
+    }
 
 
 def kernel_case(spec: str, n: int, reps: int):
@@ -407,9 +463,17 @@ def main():
                     help="fused ops timed on the CPU for the baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--distinct-replicas", action="store_true")
+    ap.add_argument("--traj-only", action="store_true",
+                    help="run only the batched-trajectory workload")
+    ap.add_argument("--traj-streams", type=int, default=8)
+    ap.add_argument("--traj-f", type=int, default=4)
     args = ap.parse_args()
     if args.kernel_case:
         kernel_case(args.kernel_case, args.qubits, args.reps)
+        return
+    if args.traj_only:
+        print(json.dumps({"trajectories": bench_trajectories(
+            args.traj_streams, args.traj_f)}), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -269,6 +269,82 @@ int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p);
 int qsg_plan_profile(qsg_ctx* ctx, qsg_plan* p, float* state, float* op_ms,
                      uint64_t cap);
 
+/* ---- noisy circuits and quantum trajectories ---------------------------
+ * Channels (lib/channel.h:31-125, lib/channels_cirq.h), MakeNoisy
+ * (lib/circuit_noisy.h:33-64) and QuantumTrajectorySimulator::RunOnce /
+ * RunBatch (lib/qtrajectory.h:80-236).  Trajectory `rep` draws from
+ * std::mt19937(rep) exactly as the reference does, so every Kraus choice that
+ * the lower probability bounds decide is the reference's; choices that need
+ * the state are made on the device.  Per-op statistics: entry i is the Kraus
+ * index chosen for op i (0 for a gate), the measured bits of a measurement,
+ * or QSG_NO_STAT where the reference records nothing; the reference's
+ * stat.samples are the entries that are not QSG_NO_STAT. */
+#define QSG_NO_STAT (~(uint64_t)0)
+enum {
+  QSG_CHANNEL_DEPOLARIZING = 0,      /* lib/channels_cirq.h:127-199, p      */
+  QSG_CHANNEL_AMPLITUDE_DAMPING = 1, /* :274-300, gamma                     */
+  QSG_CHANNEL_PHASE_DAMPING = 2,     /* :313-345, gamma                     */
+  QSG_CHANNEL_BIT_FLIP = 3,          /* :425-447, p                         */
+  QSG_CHANNEL_PHASE_FLIP = 4,        /* :393-415, p                         */
+  QSG_CHANNEL_RESET = 5              /* :359-380                            */
+};
+typedef struct qsg_noisy qsg_noisy;
+int qsg_noisy_create(unsigned num_qubits, qsg_noisy** out);
+int qsg_noisy_destroy(qsg_noisy* h);
+int qsg_noisy_info(const qsg_noisy* h, unsigned* num_qubits,
+                   uint64_t* num_ops, uint64_t* num_channels);
+/* Appends the circuit's ops unchanged (times kept). */
+int qsg_noisy_append_circuit(qsg_noisy* h, const qsg_circuit* c);
+int qsg_noisy_add_channel(qsg_noisy* h, int kind, unsigned time,
+                          const unsigned* qs, unsigned nq, double p);
+/* A general channel: Kraus operator k is the matrix
+ * matrices[k * 2 * 4^nq ...] on qs (interleaved complex double, bit j <->
+ * qs[j]) with lower-bound probability probs[k]; K^dagger K is computed. */
+int qsg_noisy_add_kraus_channel(qsg_noisy* h, unsigned time,
+                                const unsigned* qs, unsigned nq,
+                                unsigned num_kops, const int* unitary,
+                                const double* probs, const double* matrices);
+/* MakeNoisy with a depolarizing(p_depol) channel after each op on each of
+ * its qubits; with gamma > 0 an amplitude damping(gamma) channel on every
+ * qubit after each cycle of `cycle_len` time steps of the clean circuit. */
+int qsg_noisy_make(const qsg_circuit* c, double p_depol, double gamma,
+                   unsigned cycle_len, qsg_noisy** out);
+int qsg_noisy_get_op(const qsg_noisy* h, uint64_t i, int* is_channel,
+                     unsigned* time, unsigned* nq, unsigned* qs,
+                     unsigned* num_kops);
+
+typedef struct qsg_traj qsg_traj;
+typedef struct qsg_traj_options {
+  unsigned max_fused_size;         /* 0: 4 */
+  unsigned seeds;                  /* 0: default */
+  int collect_kop_stat;            /* lib/qtrajectory.h:48-58 */
+  int collect_mea_stat;
+  int normalize_before_mea_gates;
+} qsg_traj_options;
+/* Fuses the noisy circuit once (each channel as its first Kraus operator).
+ * QSG_ERR_UNSUPPORTED for a non-unitary channel on more than 2 qubits or
+ * whose K^dagger K is not diagonal. */
+int qsg_traj_create(const qsg_noisy* h, const qsg_traj_options* opts,
+                    qsg_traj** out);
+int qsg_traj_destroy(qsg_traj* t);
+int qsg_traj_info(const qsg_traj* t, unsigned* num_qubits, uint64_t* num_ops,
+                  uint64_t* num_fused_ops);
+/* RunOnce: trajectory `rep` from |0..0> on `state` (synchronous); stats
+ * receives num_ops entries (may be NULL). */
+int qsg_traj_run(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
+                 uint64_t* stats);
+/* RunBatch over items (runners[item_runner[i]], item_rep[i]) on
+ * `num_streams` concurrent streams of `device`.  stats (may be NULL): the
+ * items' entries concatenated in item order; out_states (may be NULL, or
+ * hold NULLs): per item a device buffer of qsg_min_size(n) floats for the
+ * final state; latency_ms: per-item device time; wall_s: batch wall time. */
+int qsg_traj_run_batch(int device, qsg_traj* const* runners,
+                       uint64_t num_runners, const uint32_t* item_runner,
+                       const uint64_t* item_rep, uint64_t num_items,
+                       unsigned num_streams, uint64_t* stats,
+                       float* const* out_states, float* latency_ms,
+                       double* wall_s);
+
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,
  * qsg_timer_stop records a second one, synchronises and returns the elapsed

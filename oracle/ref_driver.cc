@@ -31,6 +31,17 @@
 //       reference text format through CircuitQsimParser, FP64 state (.f64)
 //   fuse <gates> <max_fused_size>
 //       number of fused ops of MultiQubitGateFuser and their size histogram
+//   traj <noisy> <out-prefix> <max_fused_size> <r0> <r1>
+//       The gate list may also hold channels (one qubit each):
+//         D|A|P|B|F <time> <q> <param>   depolarizing, amplitude damping,
+//                                        phase damping, bit flip, phase flip
+//         R <time> <q>                   reset
+//       Runs QuantumTrajectorySimulator::RunBatch over repetitions [r0, r1)
+//       with QSimRunner + MultiQubitGateFuser, collect_kop_stat and
+//       collect_mea_stat on, in float (host SIMD simulator) and in double
+//       (SimulatorBasic).  Writes per repetition the count and the
+//       stat.samples (.stat32 / .stat64, uint64) and the final state in
+//       normal order (.f32 / .f64).
 //   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
 //       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
 //       with one std::mt19937(seed); writes bits per round (.bits) and the
@@ -45,6 +56,8 @@
 #include <string>
 #include <vector>
 
+#include "channel.h"
+#include "channels_cirq.h"
 #include "circuit.h"
 #include "circuit_qsim_parser.h"
 #include "io_file.h"
@@ -55,6 +68,7 @@
 #include "gates_qsim.h"
 #include "io.h"
 #include "operation.h"
+#include "qtrajectory.h"
 #include "run_qsim.h"
 #include "simmux.h"
 #include "simulator_basic.h"
@@ -68,7 +82,12 @@ struct GateSpec {
   std::vector<unsigned> qs, cqs;
   uint64_t cvals = 0;
   std::vector<float> m;
+  double param = 0;  // channels
 };
+
+static bool IsChannel(char k) {
+  return k == 'D' || k == 'A' || k == 'P' || k == 'B' || k == 'F' || k == 'R';
+}
 
 static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
   std::ifstream f(path);
@@ -84,6 +103,17 @@ static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
     }
     GateSpec g;
     g.kind = tag[0];
+    if (IsChannel(g.kind)) {
+      g.qs.resize(1);
+      ss >> g.time >> g.qs[0];
+      if (g.kind != 'R') {
+        std::string t;
+        ss >> t;
+        g.param = std::strtod(t.c_str(), nullptr);
+      }
+      out.push_back(std::move(g));
+      continue;
+    }
     unsigned k;
     ss >> g.time >> k;
     g.qs.resize(k);
@@ -112,6 +142,23 @@ static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
 template <typename FP>
 static Operation<FP> ToOp(const GateSpec& g) {
   if (g.kind == 'm') return CreateMeasurement(g.time, g.qs);
+  const unsigned q = g.qs.empty() ? 0 : g.qs[0];
+  switch (g.kind) {
+    case 'D':
+      return Cirq::DepolarizingChannel<FP>::Create(g.time, q, g.param);
+    case 'A':
+      return Cirq::AmplitudeDampingChannel<FP>::Create(g.time, q, g.param);
+    case 'P':
+      return Cirq::PhaseDampingChannel<FP>::Create(g.time, q, g.param);
+    case 'B':
+      return Cirq::BitFlipChannel<FP>::Create(g.time, q, g.param);
+    case 'F':
+      return Cirq::PhaseFlipChannel<FP>::Create(g.time, q, g.param);
+    case 'R':
+      return Cirq::ResetChannel<FP>::Create(g.time, q);
+    default:
+      break;
+  }
   Gate<FP> gate;
   gate.kind = kGateMatrix1;
   gate.time = g.time;
@@ -269,6 +316,59 @@ static int CmdMeasure(int argc, char** argv) {
   return 0;
 }
 
+struct Factory64 {
+  using Simulator = SimulatorBasic<For, double>;
+  using StateSpace = Simulator::StateSpace;
+  StateSpace CreateStateSpace() const { return StateSpace(1); }
+  Simulator CreateSimulator() const { return Simulator(1); }
+};
+
+template <typename FP, typename Factory>
+static bool RunTraj(const std::vector<GateSpec>& specs, unsigned n,
+                    unsigned fsize, uint64_t r0, uint64_t r1,
+                    const std::string& out, const char* suffix) {
+  Circuit<Operation<FP>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<FP>(g));
+  using Runner = QSimRunner<IO, MultiQubitGateFuser<IO>, Factory>;
+  using QTSim = QuantumTrajectorySimulator<IO, Runner>;
+  typename QTSim::Parameter param;
+  param.max_fused_size = fsize;
+  param.verbosity = 0;
+  param.collect_kop_stat = true;
+  param.collect_mea_stat = true;
+  Factory factory;
+  auto ss = factory.CreateStateSpace();
+  auto sim = factory.CreateSimulator();
+  std::vector<uint64_t> stats;
+  std::vector<FP> states;
+  auto tmp = ss.Create(n);
+  auto measure = [&](uint64_t, const typename Factory::StateSpace::State& st,
+                     const typename QTSim::Stat& stat) {
+    stats.push_back(stat.samples.size());
+    stats.insert(stats.end(), stat.samples.begin(), stat.samples.end());
+    ss.Copy(st, tmp);
+    ss.InternalToNormalOrder(tmp);
+    states.insert(states.end(), tmp.get(), tmp.get() + 2 * (uint64_t{1} << n));
+  };
+  if (!QTSim::RunBatch(param, circuit, r0, r1, ss, sim, measure)) return false;
+  WriteRaw(out + ".stat" + suffix, stats.data(), stats.size() * 8);
+  WriteRaw(out + ".f" + suffix, states.data(), states.size() * sizeof(FP));
+  return true;
+}
+
+static int CmdTraj(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  std::string out = argv[3];
+  unsigned fsize = std::atoi(argv[4]);
+  uint64_t r0 = std::strtoull(argv[5], nullptr, 10);
+  uint64_t r1 = std::strtoull(argv[6], nullptr, 10);
+  if (!RunTraj<float, Factory32>(specs, n, fsize, r0, r1, out, "32")) return 1;
+  if (!RunTraj<double, Factory64>(specs, n, fsize, r0, r1, out, "64")) return 1;
+  return 0;
+}
+
 // fuse <gates> <max_fused_size>: prints the number of fused operations
 // MultiQubitGateFuser produces and the size histogram.
 static int CmdFuse(int argc, char** argv) {
@@ -319,5 +419,6 @@ int main(int argc, char** argv) {
   if (cmd == "mt") return CmdMt(argc, argv);
   if (cmd == "run") return CmdRun(argc, argv);
   if (cmd == "measure") return CmdMeasure(argc, argv);
+  if (cmd == "traj") return CmdTraj(argc, argv);
   return 2;
 }

@@ -103,6 +103,22 @@ SIGNATURES = {
     "qsg_plan_capture": (i32, [vp, vp, vp]),
     "qsg_plan_replay": (i32, [vp, vp]),
     "qsg_plan_profile": (i32, [vp, vp, vp, P_f32, u64]),
+    "qsg_noisy_create": (i32, [u32, C.POINTER(vp)]),
+    "qsg_noisy_destroy": (i32, [vp]),
+    "qsg_noisy_info": (i32, [vp, P_u32, P_u64, P_u64]),
+    "qsg_noisy_append_circuit": (i32, [vp, vp]),
+    "qsg_noisy_add_channel": (i32, [vp, i32, u32, P_u32, u32, f64]),
+    "qsg_noisy_add_kraus_channel": (i32, [vp, u32, P_u32, u32, u32,
+                                          C.POINTER(C.c_int), P_f64, P_f64]),
+    "qsg_noisy_make": (i32, [vp, f64, f64, u32, C.POINTER(vp)]),
+    "qsg_noisy_get_op": (i32, [vp, u64, C.POINTER(C.c_int), P_u32, P_u32,
+                               P_u32, P_u32]),
+    "qsg_traj_create": (i32, [vp, vp, C.POINTER(vp)]),
+    "qsg_traj_destroy": (i32, [vp]),
+    "qsg_traj_info": (i32, [vp, P_u32, P_u64, P_u64]),
+    "qsg_traj_run": (i32, [vp, vp, vp, u64, P_u64]),
+    "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
+                                 u32, P_u64, C.POINTER(vp), P_f32, P_f64]),
     "qsg_timer_start": (i32, [vp]),
     "qsg_timer_stop": (i32, [vp, P_f32]),
 }
@@ -118,6 +134,13 @@ class FuseOptions(C.Structure):
     _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
                 ("tensor_path", C.c_int), ("tc_min_k", C.c_uint),
                 ("cost_model", C.c_void_p)]
+
+
+class TrajOptions(C.Structure):
+    """qsg_traj_options."""
+    _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
+                ("collect_kop_stat", C.c_int), ("collect_mea_stat", C.c_int),
+                ("normalize_before_mea_gates", C.c_int)]
 
 
 class QsgError(RuntimeError):

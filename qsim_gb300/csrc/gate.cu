@@ -2,6 +2,7 @@
 // ApplyControlledGate and ExpectationValue (lib/simulator_cuda.h:70-260).
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -107,8 +108,11 @@ static bool plan_tile(unsigned n, const unsigned* qs, unsigned k,
 // before any graph capture by apply_gate_prepare.
 template <int K, bool PAIR, int MODE>
 static int tile_setup(int* occupancy) {
-  static int o = 0;
-  if (o == 0) {
+  // Host threads driving separate streams may race here; the set-up is
+  // idempotent and the result is published once it is complete.
+  static std::atomic<int> o{0};
+  int cur = o.load(std::memory_order_acquire);
+  if (cur == 0) {
     auto kern = gate_tile_kernel<K, PAIR, MODE>;
     const size_t smem = TileShape<K, PAIR>::SMEM;
     QSG_CUDA(cudaFuncSetAttribute(
@@ -116,9 +120,10 @@ static int tile_setup(int* occupancy) {
     int v = 0;
     QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &v, kern, kTileThreads, smem));
-    o = v < 1 ? 1 : v;
+    cur = v < 1 ? 1 : v;
+    o.store(cur, std::memory_order_release);
   }
-  *occupancy = o;
+  *occupancy = cur;
   return QSG_OK;
 }
 

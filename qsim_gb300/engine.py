@@ -233,3 +233,144 @@ class Plan:
             N.lib.qsg_plan_destroy(self.h)
         except Exception:
             pass
+
+
+# ---- noisy circuits and trajectories ---------------------------------------
+
+CHANNEL_DEPOLARIZING, CHANNEL_AMPLITUDE_DAMPING, CHANNEL_PHASE_DAMPING = 0, 1, 2
+CHANNEL_BIT_FLIP, CHANNEL_PHASE_FLIP, CHANNEL_RESET = 3, 4, 5
+NO_STAT = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+class NoisyCircuit:
+    """Circuit with channels (lib/circuit_noisy.h, lib/channels_cirq.h)."""
+
+    def __init__(self, num_qubits: int = 0, _handle=None):
+        if _handle is not None:
+            self.h = _handle
+        else:
+            h = C.c_void_p()
+            check(N.lib.qsg_noisy_create(num_qubits, C.byref(h)))
+            self.h = h
+
+    @classmethod
+    def make(cls, circuit: Circuit, p_depol: float, gamma: float = 0.0,
+             cycle_len: int = 2) -> "NoisyCircuit":
+        """MakeNoisy with depolarizing(p_depol) after each op's qubits and,
+        with gamma > 0, amplitude damping(gamma) on every qubit after each
+        cycle of `cycle_len` clean time steps."""
+        h = C.c_void_p()
+        check(N.lib.qsg_noisy_make(circuit.h, p_depol, gamma, cycle_len,
+                                   C.byref(h)))
+        return cls(_handle=h)
+
+    def append(self, circuit: Circuit):
+        check(N.lib.qsg_noisy_append_circuit(self.h, circuit.h))
+
+    def _append_one(self, build):
+        c = Circuit(self.info()["num_qubits"])
+        build(c)
+        self.append(c)
+
+    def add_gate(self, time, qs, matrix):
+        self._append_one(lambda c: c.add_gate(time, qs, matrix))
+
+    def add_controlled_gate(self, time, qs, cqs, cvals, matrix):
+        self._append_one(lambda c: c.add_controlled_gate(time, qs, cqs, cvals,
+                                                         matrix))
+
+    def add_measurement(self, time, qs):
+        self._append_one(lambda c: c.add_measurement(time, qs))
+
+    def add_channel(self, kind: int, time: int, qs, p: float = 0.0):
+        check(N.lib.qsg_noisy_add_channel(self.h, kind, time, _u32(qs),
+                                          len(qs), p))
+
+    def add_kraus_channel(self, time: int, qs, kops):
+        """kops: list of (unitary: bool, prob: float, matrix 2^k x 2^k)."""
+        mats = np.ascontiguousarray(
+            np.stack([np.asarray(m, np.complex128).reshape(-1) for _, _, m in kops]))
+        uni = (C.c_int * len(kops))(*[int(u) for u, _, _ in kops])
+        pr = (C.c_double * len(kops))(*[float(p) for _, p, _ in kops])
+        check(N.lib.qsg_noisy_add_kraus_channel(
+            self.h, time, _u32(qs), len(qs), len(kops), uni, pr,
+            mats.view(np.float64).ctypes.data_as(N.P_f64)))
+
+    def info(self):
+        n, m, c = C.c_uint(), C.c_uint64(), C.c_uint64()
+        check(N.lib.qsg_noisy_info(self.h, C.byref(n), C.byref(m), C.byref(c)))
+        return dict(num_qubits=n.value, num_ops=m.value, num_channels=c.value)
+
+    def __len__(self):
+        return self.info()["num_ops"]
+
+    def op(self, i: int) -> dict:
+        ch, t, nq, nk = C.c_int(), C.c_uint(), C.c_uint(), C.c_uint()
+        qs = (C.c_uint * 64)()
+        check(N.lib.qsg_noisy_get_op(self.h, i, C.byref(ch), C.byref(t),
+                                     C.byref(nq), qs, C.byref(nk)))
+        return dict(is_channel=bool(ch.value), time=t.value,
+                    qs=list(qs[:nq.value]), num_kops=nk.value)
+
+    def __del__(self):
+        try:
+            N.lib.qsg_noisy_destroy(self.h)
+        except Exception:
+            pass
+
+
+class Trajectories:
+    """QuantumTrajectorySimulator for one noisy circuit (lib/qtrajectory.h)."""
+
+    def __init__(self, noisy: NoisyCircuit, max_fused_size: int = 4,
+                 seeds: int = 0, collect_kop_stat: bool = True,
+                 collect_mea_stat: bool = True,
+                 normalize_before_mea_gates: bool = True):
+        self.noisy = noisy
+        o = N.TrajOptions(max_fused_size, seeds, int(collect_kop_stat),
+                          int(collect_mea_stat), int(normalize_before_mea_gates))
+        h = C.c_void_p()
+        check(N.lib.qsg_traj_create(noisy.h, C.byref(o), C.byref(h)))
+        self.h = h
+
+    def info(self):
+        n, m, f = C.c_uint(), C.c_uint64(), C.c_uint64()
+        check(N.lib.qsg_traj_info(self.h, C.byref(n), C.byref(m), C.byref(f)))
+        return dict(num_qubits=n.value, num_ops=m.value, num_fused_ops=f.value)
+
+    def run(self, ctx, state, rep: int) -> np.ndarray:
+        """RunOnce: trajectory `rep` into `state`; per-op statistics."""
+        stats = np.zeros(max(1, self.info()["num_ops"]), dtype=np.uint64)
+        check(N.lib.qsg_traj_run(ctx.h, self.h, state.get(), rep,
+                                 stats.ctypes.data_as(N.P_u64)))
+        return stats
+
+    @staticmethod
+    def samples(stats: np.ndarray) -> np.ndarray:
+        """The reference's stat.samples: entries other than NO_STAT."""
+        return stats[stats != NO_STAT]
+
+
+def run_trajectory_batch(runners, items, num_streams: int = 8, device: int = 0,
+                         out_states=None):
+    """RunBatch over items [(runner index, rep)] on concurrent streams.
+    Returns (per-item stats list, latency_ms array, wall seconds)."""
+    nr = len(runners)
+    rh = (C.c_void_p * max(1, nr))(*[r.h.value for r in runners])
+    ir = np.ascontiguousarray([i for i, _ in items], dtype=np.uint32)
+    rp = np.ascontiguousarray([r for _, r in items], dtype=np.uint64)
+    sizes = [runners[i].info()["num_ops"] for i, _ in items]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    stats = np.zeros(max(1, int(offs[-1])), dtype=np.uint64)
+    lat = np.zeros(max(1, len(items)), dtype=np.float32)
+    wall = C.c_double()
+    outs = None
+    if out_states is not None:
+        outs = (C.c_void_p * len(items))(*[s.get() if s is not None else None
+                                           for s in out_states])
+    check(N.lib.qsg_traj_run_batch(
+        device, rh, nr, ir.ctypes.data_as(N.P_u32), rp.ctypes.data_as(N.P_u64),
+        len(items), num_streams, stats.ctypes.data_as(N.P_u64), outs,
+        lat.ctypes.data_as(N.P_f32), C.byref(wall)))
+    per = [stats[offs[i]:offs[i + 1]] for i in range(len(items))]
+    return per, lat[:len(items)], wall.value

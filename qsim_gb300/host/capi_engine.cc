@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 
+#include "capi_types.h"
 #include "engine.h"
 #include "internal.h"
 #include "runner.h"
@@ -12,9 +13,6 @@
 using namespace qsg;
 using namespace qsg::host;
 
-struct qsg_circuit {
-  Circuit c;
-};
 
 struct qsg_plan {
   PlanRuntime rt;

@@ -121,6 +121,9 @@ Plan unfused(const Circuit& c);
 // qubit set `qs`.
 std::vector<cplx> block_matrix(const Circuit& c, const std::vector<int>& members,
                                const std::vector<unsigned>& qs);
+// Same product for gates given by pointer (qubits of each within `qs`).
+std::vector<cplx> block_matrix_ops(const std::vector<const Op*>& ops,
+                                   const std::vector<unsigned>& qs);
 
 }  // namespace host
 }  // namespace qsg

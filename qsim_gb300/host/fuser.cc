@@ -31,14 +31,22 @@ unsigned Plan::max_k() const {
 
 std::vector<cplx> block_matrix(const Circuit& c, const std::vector<int>& members,
                                const std::vector<unsigned>& qs) {
+  std::vector<const Op*> ops;
+  ops.reserve(members.size());
+  for (int idx : members) ops.push_back(&c.ops[idx]);
+  return block_matrix_ops(ops, qs);
+}
+
+std::vector<cplx> block_matrix_ops(const std::vector<const Op*>& ops,
+                                   const std::vector<unsigned>& qs) {
   const unsigned k = qs.size();
   const unsigned d = 1u << k;
   // Columns of the block matrix evolve as k-qubit states.
   std::vector<cplx> m(size_t(d) * d, 0.0);
   for (unsigned i = 0; i < d; ++i) m[i * d + i] = 1.0;
   std::vector<cplx> tmp(d);
-  for (int idx : members) {
-    const Op& op = c.ops[idx];
+  for (const Op* opp : ops) {
+    const Op& op = *opp;
     const unsigned gk = op.qs.size();
     const unsigned gd = 1u << gk;
     // Positions of the gate's qubits inside the block.

@@ -95,8 +95,12 @@ def write_gate_list(path, n, ops):
                 cq = " ".join(map(str, o["cqs"]))
                 f.write(f"c {o['time']} {k} {q} {len(o['cqs'])} {cq} "
                         f"{o['cvals']} {hexf(interleave(o['m']))}\n")
-            else:
+            elif o["kind"] == "m":
                 f.write(f"m {o['time']} {k} {q}\n")
+            elif o["kind"] == "R":
+                f.write(f"R {o['time']} {q}\n")
+            else:  # one-qubit channel with one parameter
+                f.write(f"{o['kind']} {o['time']} {q} {float(o['p']).hex()}\n")
 
 
 def pack_ops(ops):
@@ -294,8 +298,123 @@ def mt_case():
         print("mt19937 written")
 
 
+CHANNEL_CODES = {"D": 0, "A": 1, "P": 2, "B": 3, "F": 4, "R": 5}
+
+
+def noisy_chain_ops(n, cycles, seed, p_depol, gamma, cycle_len=2):
+    """The chain workload with noise inserted by the rule of the engine's
+    make_noisy (lib/circuit_noisy.h:33-64 plus amplitude damping on every
+    qubit after each cycle), written out op by op."""
+    sys.path.insert(0, ROOT)
+    from qsim_gb300 import engine as E
+    c = E.Circuit.chain(n, cycles, seed)
+    clean = c.ops()
+    ops = []
+    for i, o in enumerate(clean):
+        t = o["time"]
+        t2 = 2 * (t + t // cycle_len) if gamma > 0 else 2 * t
+        kind = {0: "g", 1: "c", 2: "m"}[o["kind"]]
+        d = dict(kind=kind, time=t2, qs=o["qs"])
+        if kind != "m":
+            d["m"] = o["m"]
+        if kind == "c":
+            d["cqs"], d["cvals"] = o["cqs"], o["cvals"]
+        ops.append(d)
+        if p_depol > 0:
+            for q in o["qs"] + o["cqs"]:
+                ops.append(dict(kind="D", time=t2 + 1, qs=[q], p=p_depol))
+        last = i + 1 == len(clean) or clean[i + 1]["time"] // cycle_len != t // cycle_len
+        if gamma > 0 and last:
+            for q in range(n):
+                ops.append(dict(kind="A", time=t2 + 2, qs=[q], p=gamma))
+    return ops
+
+
+def mixed_noisy_ops(rng, n, layers):
+    """Random one- and two-qubit gates with every one-qubit channel kind of
+    lib/channels_cirq.h and measurements."""
+    ops = []
+    t = 0
+    for layer in range(layers):
+        for q in range(n):
+            ops.append(dict(kind="g", time=t, qs=[q], m=random_unitary(rng, 1)))
+        for q in range(layer % 2, n - 1, 2):
+            ops.append(dict(kind="g", time=t + 1, qs=[q, q + 1],
+                            m=random_unitary(rng, 2)))
+        for q in range(n):
+            kind = "DAPBFR"[int(rng.integers(6))] if rng.random() < 0.5 else None
+            if kind is None:
+                continue
+            p = {"D": 0.2, "A": 0.3, "P": 0.25, "B": 0.15, "F": 0.15, "R": 0}[kind]
+            ops.append(dict(kind=kind, time=t + 2, qs=[q], p=p))
+        if layer in (1, layers - 1):
+            qs = sorted(rng.choice(n, size=2, replace=False).tolist())
+            ops.append(dict(kind="m", time=t + 3, qs=qs))
+        t += 4
+    return ops
+
+
+def pack_noisy(ops):
+    """Fixture arrays: gates packed as pack_ops does, plus per op a channel
+    code (-1 for gates and measurements) and parameter."""
+    gate_ops = [o for o in ops if o["kind"] in "gcm"]
+    data = pack_ops(gate_ops)
+    data["op_channel"] = np.array([CHANNEL_CODES.get(o["kind"], -1) for o in ops],
+                                  np.int32)
+    data["op_time"] = np.array([o["time"] for o in ops], np.int64)
+    data["op_q"] = np.array([o["qs"][0] if o["kind"] in CHANNEL_CODES else -1
+                             for o in ops], np.int32)
+    data["op_p"] = np.array([o.get("p", 0.0) for o in ops], np.float64)
+    return data
+
+
+def traj_case(name, n, ops, fsize, r0, r1, states_c64=False):
+    """QuantumTrajectorySimulator::RunBatch of the reference over [r0, r1):
+    stat.samples per repetition and the final states, in float (SIMD
+    simulator) and double (SimulatorBasic)."""
+    with tempfile.TemporaryDirectory() as td:
+        gl = os.path.join(td, "noisy.txt")
+        write_gate_list(gl, n, ops)
+        out = os.path.join(td, "out")
+        subprocess.run([DRIVER, "traj", gl, out, str(fsize), str(r0), str(r1)],
+                       check=True)
+        data = dict(n=np.int32(n), fsize=np.int32(fsize), r0=np.int64(r0),
+                    r1=np.int64(r1))
+        for suf in ("32", "64"):
+            st = np.fromfile(out + ".stat" + suf, np.uint64)
+            counts, flat, i = [], [], 0
+            while i < len(st):
+                c = int(st[i])
+                counts.append(c)
+                flat.extend(st[i + 1:i + 1 + c].tolist())
+                i += 1 + c
+            data["stat_count" + suf] = np.array(counts, np.int64)
+            data["stat" + suf] = np.array(flat, np.uint64)
+        f32 = np.fromfile(out + ".f32", np.float32).view(np.complex64)
+        f64 = np.fromfile(out + ".f64", np.float64).view(np.complex128)
+        data["f32"] = f32.reshape(r1 - r0, -1)
+        data["f64"] = (f64.astype(np.complex64) if states_c64 else f64).reshape(r1 - r0, -1)
+        data.update(pack_noisy(ops))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+        print(name, "written")
+
+
+def traj_cases():
+    traj_case("traj_depol8", 8, noisy_chain_ops(8, 4, 3, 0.05, 0.0), 2, 0, 48)
+    traj_case("traj_ad8", 8, noisy_chain_ops(8, 4, 4, 0.02, 0.1), 3, 0, 48)
+    rng = np.random.default_rng(99)
+    traj_case("traj_mixed6", 6, mixed_noisy_ops(rng, 6, 5), 2, 0, 40)
+    # The batched-trajectory workload's noise model at n = 12, depth 12.
+    traj_case("traj_chain12", 12, noisy_chain_ops(12, 12, 5, 1e-3, 5e-3), 4,
+              0, 8, states_c64=True)
+
+
 def main():
     if not os.path.exists(DRIVER):
+        sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
+    if sys.argv[1:] == ["traj"]:
+        traj_cases()
+        return
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
     mt_case()
     text_case("text_gates9", 9, 30, 5)
@@ -319,6 +438,7 @@ def main():
     ops = random_gate_list(rng, 14, 60, 2)
     run_case("rand14_k2", 14, ops, 2, 4000, 1,
              measure=(17, 6, [0, 5, 13]))
+    traj_cases()
 
 
 if __name__ == "__main__":
