@@ -332,7 +332,8 @@ def run_engine(args, world, rank, local, dist):
     e2e = max_over_ranks(dist, statistics.median(e2e_times))
 
     # Batched trajectories (replicas for N > 1: every rank runs the batch).
-    traj = bench_trajectories(args.traj_streams, args.traj_f)
+    traj = bench_trajectories(args.traj_streams, args.traj_f,
+                              args.traj_big_qubits, args.traj_big_streams)
     traj["wall_s"] = max_over_ranks(dist, traj["wall_s"])
     traj["value"] = world * traj["trajectories"] / traj["wall_s"]
 
@@ -379,6 +380,7 @@ TRAJ_WORKLOAD = ("4096 noisy trajectories: 128 chain random circuits, n ~ "
 
 
 def bench_trajectories(num_streams: int, max_fused_size: int = 4,
+                       big_qubits: int = 0, big_streams: int = 1,
                        warm: bool = True):
     """Batched-trajectory workload: every trajectory from |0..0>, its final
     state left normalised in HBM and its Kraus statistics copied to the
@@ -396,26 +398,34 @@ def bench_trajectories(num_streams: int, max_fused_size: int = 4,
         runners.append(E.Trajectories(nc, max_fused_size=max_fused_size))
     setup_s = time.perf_counter() - t0
     items = [(i, r) for i in range(len(runners)) for r in range(TRAJ["reps"])]
+    kw = dict(num_streams=num_streams, big_qubits=big_qubits,
+              big_streams=big_streams)
     if warm:
         E.run_trajectory_batch(runners, [(i, 10**6) for i in range(len(runners))],
-                               num_streams=num_streams)
-    per, lat, wall = E.run_trajectory_batch(runners, items,
-                                            num_streams=num_streams)
+                               **kw)
+    per, lat, wall, launches = E.run_trajectory_batch(
+        runners, items, return_launches=True, **kw)
     amp_ops = sum(float(2 ** int(ns[i])) * runners[i].info()["num_fused_ops"]
                   for i, _ in items)
     escapes = 0
     for (i, _), st in zip(items, per):
         s = E.Trajectories.samples(st)
         escapes += int(np.sum(s == 1))
+    per_n = {}
+    for (i, _), t in zip(items, lat):
+        per_n.setdefault(int(ns[i]), []).append(float(t))
     return {
         "value": len(items) / wall, "unit": "traj/s",
         "wall_s": wall, "trajectories": len(items),
         "latency_ms_p50": float(np.percentile(lat, 50)),
         "latency_ms_p99": float(np.percentile(lat, 99)),
-        "streams": num_streams, "max_fused_size": max_fused_size,
-        "setup_s": setup_s,
+        "streams": num_streams, "big_qubits": big_qubits,
+        "big_streams": big_streams, "max_fused_size": max_fused_size,
+        "setup_s": setup_s, "gpu_launches": launches,
         "fused_pass_bytes_per_s": 16.0 * amp_ops / wall,
         "non_default_kraus_choices": escapes,
+        "latency_ms_mean_by_n": {str(k): float(np.mean(v))
+                                 for k, v in sorted(per_n.items())},
         "workload": TRAJ_WORKLOAD,
     }
 
@@ -467,13 +477,16 @@ def main():
                     help="run only the batched-trajectory workload")
     ap.add_argument("--traj-streams", type=int, default=8)
     ap.add_argument("--traj-f", type=int, default=4)
+    ap.add_argument("--traj-big-qubits", type=int, default=0)
+    ap.add_argument("--traj-big-streams", type=int, default=1)
     args = ap.parse_args()
     if args.kernel_case:
         kernel_case(args.kernel_case, args.qubits, args.reps)
         return
     if args.traj_only:
         print(json.dumps({"trajectories": bench_trajectories(
-            args.traj_streams, args.traj_f)}), flush=True)
+            args.traj_streams, args.traj_f, args.traj_big_qubits,
+            args.traj_big_streams)}), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3

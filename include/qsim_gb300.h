@@ -333,17 +333,23 @@ int qsg_traj_info(const qsg_traj* t, unsigned* num_qubits, uint64_t* num_ops,
  * receives num_ops entries (may be NULL). */
 int qsg_traj_run(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
                  uint64_t* stats);
-/* RunBatch over items (runners[item_runner[i]], item_rep[i]) on
- * `num_streams` concurrent streams of `device`.  stats (may be NULL): the
- * items' entries concatenated in item order; out_states (may be NULL, or
- * hold NULLs): per item a device buffer of qsg_min_size(n) floats for the
- * final state; latency_ms: per-item device time; wall_s: batch wall time. */
+/* RunBatch over items (runners[item_runner[i]], item_rep[i]) on concurrent
+ * streams of `device` (one host thread, stream, state buffer and workspace
+ * each).  stats (may be NULL): the items' entries concatenated in item
+ * order; out_states (may be NULL, or hold NULLs): per item a device buffer
+ * of qsg_min_size(n) floats for the final state; latency_ms: per-item device
+ * time; wall_s: batch wall time; launches: kernels launched. */
+typedef struct qsg_batch_options {
+  unsigned num_streams;  /* 0: 8 */
+  unsigned big_qubits;   /* circuits of >= big_qubits qubits run only on   */
+  unsigned big_streams;  /* the first big_streams streams (0 / 0: no split) */
+} qsg_batch_options;
 int qsg_traj_run_batch(int device, qsg_traj* const* runners,
                        uint64_t num_runners, const uint32_t* item_runner,
                        const uint64_t* item_rep, uint64_t num_items,
-                       unsigned num_streams, uint64_t* stats,
+                       const qsg_batch_options* opts, uint64_t* stats,
                        float* const* out_states, float* latency_ms,
-                       double* wall_s);
+                       double* wall_s, uint64_t* launches);
 
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,

@@ -118,7 +118,8 @@ SIGNATURES = {
     "qsg_traj_info": (i32, [vp, P_u32, P_u64, P_u64]),
     "qsg_traj_run": (i32, [vp, vp, vp, u64, P_u64]),
     "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
-                                 u32, P_u64, C.POINTER(vp), P_f32, P_f64]),
+                                 vp, P_u64, C.POINTER(vp), P_f32, P_f64,
+                                 P_u64]),
     "qsg_timer_start": (i32, [vp]),
     "qsg_timer_stop": (i32, [vp, P_f32]),
 }
@@ -141,6 +142,12 @@ class TrajOptions(C.Structure):
     _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
                 ("collect_kop_stat", C.c_int), ("collect_mea_stat", C.c_int),
                 ("normalize_before_mea_gates", C.c_int)]
+
+
+class BatchOptions(C.Structure):
+    """qsg_batch_options."""
+    _fields_ = [("num_streams", C.c_uint), ("big_qubits", C.c_uint),
+                ("big_streams", C.c_uint)]
 
 
 class QsgError(RuntimeError):

@@ -352,9 +352,11 @@ class Trajectories:
 
 
 def run_trajectory_batch(runners, items, num_streams: int = 8, device: int = 0,
-                         out_states=None):
+                         out_states=None, big_qubits: int = 0,
+                         big_streams: int = 1, return_launches: bool = False):
     """RunBatch over items [(runner index, rep)] on concurrent streams.
-    Returns (per-item stats list, latency_ms array, wall seconds)."""
+    Returns (per-item stats list, latency_ms array, wall seconds) and, with
+    return_launches, the number of kernels launched."""
     nr = len(runners)
     rh = (C.c_void_p * max(1, nr))(*[r.h.value for r in runners])
     ir = np.ascontiguousarray([i for i, _ in items], dtype=np.uint32)
@@ -364,13 +366,17 @@ def run_trajectory_batch(runners, items, num_streams: int = 8, device: int = 0,
     stats = np.zeros(max(1, int(offs[-1])), dtype=np.uint64)
     lat = np.zeros(max(1, len(items)), dtype=np.float32)
     wall = C.c_double()
+    launches = C.c_uint64()
     outs = None
     if out_states is not None:
         outs = (C.c_void_p * len(items))(*[s.get() if s is not None else None
                                            for s in out_states])
+    o = N.BatchOptions(num_streams, big_qubits, big_streams)
     check(N.lib.qsg_traj_run_batch(
         device, rh, nr, ir.ctypes.data_as(N.P_u32), rp.ctypes.data_as(N.P_u64),
-        len(items), num_streams, stats.ctypes.data_as(N.P_u64), outs,
-        lat.ctypes.data_as(N.P_f32), C.byref(wall)))
+        len(items), C.byref(o), stats.ctypes.data_as(N.P_u64), outs,
+        lat.ctypes.data_as(N.P_f32), C.byref(wall), C.byref(launches)))
     per = [stats[offs[i]:offs[i + 1]] for i in range(len(items))]
+    if return_launches:
+        return per, lat[:len(items)], wall.value, launches.value
     return per, lat[:len(items)], wall.value

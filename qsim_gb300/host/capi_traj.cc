@@ -228,9 +228,9 @@ int qsg_traj_run(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
 int qsg_traj_run_batch(int device, qsg_traj* const* runners,
                        uint64_t num_runners, const uint32_t* item_runner,
                        const uint64_t* item_rep, uint64_t num_items,
-                       unsigned num_streams, uint64_t* stats,
+                       const qsg_batch_options* opts, uint64_t* stats,
                        float* const* out_states, float* latency_ms,
-                       double* wall_s) {
+                       double* wall_s, uint64_t* launches) {
   if (!runners || (num_items && (!item_runner || !item_rep)))
     return invalid("null argument");
   std::vector<BatchItem> items(num_items);
@@ -245,7 +245,13 @@ int qsg_traj_run_batch(int device, qsg_traj* const* runners,
     items[i].out_state = out_states ? out_states[i] : nullptr;
     off += r->num_ops();
   }
-  int rc = run_trajectory_batch(device, items, num_streams, wall_s);
+  BatchOptions o;
+  if (opts) {
+    o.num_streams = opts->num_streams;
+    o.big_qubits = opts->big_qubits;
+    o.big_streams = opts->big_streams;
+  }
+  int rc = run_trajectory_batch(device, items, o, wall_s, launches);
   if (latency_ms)
     for (uint64_t i = 0; i < num_items; ++i) latency_ms[i] = items[i].latency_ms;
   return rc;

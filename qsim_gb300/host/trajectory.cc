@@ -648,18 +648,40 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
 // ---------------------------------------------------------------------------
 
 int run_trajectory_batch(int device, std::vector<BatchItem>& items,
-                         unsigned num_streams, double* wall_s) {
-  if (items.empty()) {
-    if (wall_s) *wall_s = 0;
-    return QSG_OK;
-  }
+                         const BatchOptions& opt, double* wall_s,
+                         uint64_t* launches) {
+  if (wall_s) *wall_s = 0;
+  if (launches) *launches = 0;
+  if (items.empty()) return QSG_OK;
   unsigned max_n = 1;
   for (const auto& it : items) {
     if (!it.runner) return invalid("batch item without a runner");
     max_n = std::max(max_n, it.runner->num_qubits());
   }
-  if (num_streams == 0) num_streams = 8;
+  unsigned num_streams = opt.num_streams ? opt.num_streams : 8;
   num_streams = unsigned(std::min<size_t>(num_streams, items.size()));
+
+  // Two queues, largest circuits first.  With big_qubits set, circuits of
+  // at least that many qubits run only on the first big_streams streams,
+  // one at a time per stream, so that a state that fits in L2 stays there
+  // for its whole trajectory; the other streams take the small circuits.
+  std::vector<size_t> big, small;
+  for (size_t i = 0; i < items.size(); ++i) {
+    if (opt.big_qubits && items[i].runner->num_qubits() >= opt.big_qubits)
+      big.push_back(i);
+    else
+      small.push_back(i);
+  }
+  auto by_size = [&](size_t a, size_t b) {
+    return items[a].runner->num_qubits() > items[b].runner->num_qubits();
+  };
+  std::stable_sort(big.begin(), big.end(), by_size);
+  std::stable_sort(small.begin(), small.end(), by_size);
+  unsigned num_big = 0;
+  if (!big.empty()) {
+    num_big = opt.big_streams ? opt.big_streams : 1;
+    num_big = std::min(num_big, num_streams);
+  }
 
   struct Worker {
     qsg_ctx* ctx = nullptr;
@@ -667,10 +689,13 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
     TrajWorkspace ws;
     std::vector<std::pair<size_t, std::pair<cudaEvent_t, cudaEvent_t>>> done;
     int rc = QSG_OK;
+    bool serves_big = false;
   };
   std::vector<Worker> workers(num_streams);
   int rc = QSG_OK;
-  for (auto& w : workers) {
+  for (unsigned wi = 0; wi < num_streams; ++wi) {
+    Worker& w = workers[wi];
+    w.serves_big = wi < num_big;
     rc = qsg_ctx_create(device, nullptr, &w.ctx);
     if (rc) break;
     void* p = nullptr;
@@ -686,16 +711,9 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
       if (rc) break;
     }
   }
-  if (rc == QSG_OK) {
-    rc = qsg_ctx_sync(workers[0].ctx);
-  }
+  if (rc == QSG_OK) rc = qsg_ctx_sync(workers[0].ctx);
 
-  std::vector<size_t> order(items.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
-    return items[a].runner->num_qubits() > items[b].runner->num_qubits();
-  });
-  std::atomic<size_t> next{0};
+  std::atomic<size_t> next_big{0}, next_small{0};
   std::atomic<int> first_err{QSG_OK};
   const auto t0 = std::chrono::steady_clock::now();
   if (rc == QSG_OK) {
@@ -707,9 +725,17 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
         cudaStream_t s = static_cast<cudaStream_t>(ctx_stream(w.ctx));
         for (;;) {
           if (first_err.load() != QSG_OK) break;
-          const size_t idx = next.fetch_add(1);
-          if (idx >= order.size()) break;
-          BatchItem& it = items[order[idx]];
+          size_t item = size_t(-1);
+          if (w.serves_big) {
+            const size_t b = next_big.fetch_add(1);
+            if (b < big.size()) item = big[b];
+          }
+          if (item == size_t(-1)) {
+            const size_t m = next_small.fetch_add(1);
+            if (m < small.size()) item = small[m];
+          }
+          if (item == size_t(-1)) break;
+          BatchItem& it = items[item];
           cudaEvent_t e0 = nullptr, e1 = nullptr;
           if (cudaEventCreate(&e0) != cudaSuccess ||
               cudaEventCreate(&e1) != cudaSuccess) {
@@ -726,7 +752,7 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
               r = QSG_ERR_CUDA;
           }
           cudaEventRecord(e1, s);
-          w.done.push_back({order[idx], {e0, e1}});
+          w.done.push_back({item, {e0, e1}});
           if (r != QSG_OK) {
             w.rc = r;
             break;
@@ -754,6 +780,7 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
   const auto t1 = std::chrono::steady_clock::now();
   if (wall_s) *wall_s = std::chrono::duration<double>(t1 - t0).count();
   for (auto& w : workers) {
+    if (launches && w.ctx) *launches += qsg_ctx_launch_count(w.ctx);
     w.ws.release();
     if (w.state) dev_free(w.ctx, w.state);
     if (w.ctx) qsg_ctx_destroy(w.ctx);

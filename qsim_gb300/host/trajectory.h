@@ -166,11 +166,19 @@ struct BatchItem {
   float latency_ms = 0;   // device time from the item's first to last launch
 };
 
-// Runs the items on `num_streams` host threads, each with its own stream,
+struct BatchOptions {
+  unsigned num_streams = 8;  // host threads, each with its own stream
+  unsigned big_qubits = 0;   // circuits of >= big_qubits qubits run only on
+  unsigned big_streams = 1;  // the first big_streams streams (0: no split)
+};
+
+// Runs the items on concurrent host threads, each with its own stream,
 // state buffer and workspace on `device`; larger circuits are started
-// first.  `wall_s` receives the elapsed wall time of the whole batch.
+// first.  `wall_s` receives the elapsed wall time of the whole batch and
+// `launches` the number of kernels launched.
 int run_trajectory_batch(int device, std::vector<BatchItem>& items,
-                         unsigned num_streams, double* wall_s);
+                         const BatchOptions& opt, double* wall_s,
+                         uint64_t* launches);
 
 }  // namespace host
 }  // namespace qsg

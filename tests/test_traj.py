@@ -153,16 +153,21 @@ def ctx():
     return api.Context()
 
 
+@pytest.fixture(scope="module")
+def ss(ctx):
+    from qsim_gb300 import api
+    return api.StateSpace(ctx=ctx)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", CASES)
-def test_gpu_trajectories_match_reference(case, ctx):
-    from qsim_gb300 import api
+def test_gpu_trajectories_match_reference(case, ctx, ss):
     d = load_golden(case)
     n = int(d["n"])
     t = E.Trajectories(build_noisy(d), max_fused_size=int(d["fsize"]))
     ref32 = ref_samples(d, "32")
     ref64 = ref_samples(d, "64")
-    st = api.State(ctx, n)
+    st = ss.Create(n)
     agree = 0
     for i, rep in enumerate(range(int(d["r0"]), int(d["r1"]))):
         stats = t.run(ctx, st, rep)
@@ -170,38 +175,36 @@ def test_gpu_trajectories_match_reference(case, ctx):
         if got == [int(x) for x in ref32[i]]:
             agree += 1
         if got == [int(x) for x in ref64[i]]:
-            s = st.to_numpy().astype(np.complex128)
+            s = ss.to_numpy(st)
             want = d["f64"][i].astype(np.complex128)
             assert rel_l2(s, want) < STATE_TOL, (case, rep, rel_l2(s, want))
     assert agree >= MIN_AGREE[case] * len(ref32), (case, agree, len(ref32))
 
 
 @pytest.mark.gpu
-def test_gpu_batch_matches_single_runs(ctx):
-    from qsim_gb300 import api
+def test_gpu_batch_matches_single_runs(ctx, ss):
     runners, circuits = [], []
     for n, seed in ((9, 1), (12, 2), (7, 3)):
         nc = E.NoisyCircuit.make(E.Circuit.chain(n, 6, seed), 0.02, 0.05, 2)
         circuits.append(n)
         runners.append(E.Trajectories(nc, max_fused_size=3))
     items = [(i % 3, 100 + i) for i in range(12)]
-    outs = [api.State(ctx, circuits[r]) for r, _ in items]
+    outs = [ss.Create(circuits[r]) for r, _ in items]
     per, lat, wall = E.run_trajectory_batch(runners, items, num_streams=4,
                                             out_states=outs)
     assert wall > 0 and np.all(lat > 0)
     for (r, rep), stats, out in zip(items, per, outs):
-        st = api.State(ctx, circuits[r])
+        st = ss.Create(circuits[r])
         single = runners[r].run(ctx, st, rep)
         assert np.array_equal(single, stats)
-        np.testing.assert_array_equal(st.to_numpy(), out.to_numpy())
+        np.testing.assert_array_equal(ss.to_numpy(st), ss.to_numpy(out))
 
 
 @pytest.mark.gpu
-def test_gpu_batched_workload_noise_vs_oracle(ctx, oracle):
+def test_gpu_batched_workload_noise_vs_oracle(ctx, ss, oracle):
     """The batched-trajectory workload's noise model (depolarizing 1e-3 after
     each gate qubit, amplitude damping 5e-3 per qubit per cycle) at n = 14,
     depth 12, against the FP64 oracle."""
-    from qsim_gb300 import api
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     from make_golden import noisy_chain_ops
     n = 14
@@ -213,12 +216,12 @@ def test_gpu_batched_workload_noise_vs_oracle(ctx, oracle):
             ops.append(dict(channel="DA".index(o["kind"]), q=o["qs"][0], p=o["p"]))
         else:
             ops.append(dict(kind=0, qs=o["qs"], m=o["m"]))
-    st = api.State(ctx, n)
+    st = ss.Create(n)
     agree = 0
     for rep in range(6):
         stats = t.run(ctx, st, rep)
         s_ref, stats_ref = traj_oracle.run_trajectory(oracle, n, ops, rep)
         if [int(x) for x in E.Trajectories.samples(stats)] == list(stats_ref):
             agree += 1
-            assert rel_l2(st.to_numpy().astype(np.complex128), s_ref) < STATE_TOL
+            assert rel_l2(ss.to_numpy(st), s_ref) < STATE_TOL
     assert agree >= 5
