@@ -56,6 +56,7 @@ SIGNATURES = {
     "qsg_inner_product": (i32, [vp, vp, vp, u32, P_f64]),
     "qsg_real_inner_product": (i32, [vp, vp, vp, u32, P_f64]),
     "qsg_norm": (i32, [vp, vp, u32, P_f64]),
+    "qsg_norm_noalloc": (i32, [vp, vp, u32, P_f64]),
     "qsg_num_chunks": (u64, [u32]),
     "qsg_partial_norms": (i32, [vp, vp, u32, P_f64]),
     "qsg_find_measured_bits": (i32, [vp, vp, u32, u64, f64, u64, P_u64]),

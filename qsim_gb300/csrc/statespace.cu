@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <vector>
 
@@ -680,6 +681,72 @@ int qsg_norm(qsg_ctx* ctx, const float* state, unsigned n, double* out) {
   int rc = reduce<0>(ctx, state, nullptr, n, 0, 0, r);
   *out = r[0];
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Norm.  Same kernels and partition as qsg_norm, but the
+// per-block partial sums and the result live in a fixed file-scope device
+// array instead of the context's scratch (which the context grows with
+// cudaMalloc, and whose pinned result slot comes from cudaMallocHost, on
+// first use).  Every slot is written before it is read, so nothing in the
+// array has to start at zero.
+
+constexpr unsigned kNormNoAllocPartials = 4096;  // 64 KiB of double2
+static __device__ __align__(256) double2
+    g_norm_noalloc_scratch[kNormNoAllocPartials + 1];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_norm_noalloc_mu;
+static double2* g_norm_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the array for `device`, looked up once per device with
+// that device current.
+static int norm_noalloc_scratch(int device, double2** out) {
+  std::lock_guard<std::mutex> lock(g_norm_noalloc_mu);
+  if (device < 0 || device >= kNoAllocMaxDevices) {
+    set_error("qsg_norm_noalloc: device %d out of range", device);
+    return QSG_ERR_INVALID;
+  }
+  if (g_norm_noalloc_ptr[device] == nullptr) {
+    int cur = -1;
+    QSG_CUDA(cudaGetDevice(&cur));
+    if (cur != device) QSG_CUDA(cudaSetDevice(device));
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_norm_noalloc_scratch);
+    if (cur != device) cudaSetDevice(cur);
+    if (e != cudaSuccess)
+      return cuda_status(e, "cudaGetSymbolAddress(norm scratch)");
+    g_norm_noalloc_ptr[device] = static_cast<double2*>(p);
+  }
+  *out = g_norm_noalloc_ptr[device];
+  return QSG_OK;
+}
+
+int qsg_norm_noalloc(qsg_ctx* ctx, const float* state, unsigned n,
+                     double* out) {
+  QSG_CHECK_ARG(ctx && state && out, "qsg_norm_noalloc: null argument");
+  QSG_CHECK_ARG(n <= kMaxQubits, "qsg_norm_noalloc: %u qubits (maximum %u)",
+                n, kMaxQubits);
+  const uint64_t units = units_of(n);
+  const unsigned grid = grid_for(ctx, units, kRedThreads * kRedUnroll);
+  QSG_CHECK_ARG(grid <= kNormNoAllocPartials,
+                "qsg_norm_noalloc: %u partial sums needed, the fixed scratch "
+                "holds %u", grid, kNormNoAllocPartials);
+  double2* scratch = nullptr;
+  int rc = norm_noalloc_scratch(ctx->device, &scratch);
+  if (rc) return rc;
+  reduce_kernel<0><<<grid, kRedThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float4*>(state), nullptr, units, 0, 0, scratch);
+  QSG_LAUNCHED(ctx);
+  double2* result = scratch + kNormNoAllocPartials;
+  final_reduce_kernel<<<1, 1024, 0, ctx->stream>>>(scratch, grid, result);
+  QSG_LAUNCHED(ctx);
+  double2 r = make_double2(0.0, 0.0);
+  QSG_CUDA(cudaMemcpyAsync(&r, result, sizeof(double2),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
+  *out = r.x;
+  return QSG_OK;
 }
 
 uint64_t qsg_num_chunks(unsigned n) { return num_chunks(n); }
