@@ -216,6 +216,7 @@ def run_engine(args, world, rank, local, dist):
     import qsim_gb300 as q
     from qsim_gb300 import engine as E
     from qsim_gb300 import _native as N
+    from qsim_gb300 import learned as L
 
     hbm_peak, _, peak_kind = peaks()
     ctx = q.Context(0)
@@ -234,6 +235,11 @@ def run_engine(args, world, rank, local, dist):
     forms["plain_f6"] = E.Plan(c, max_fused_size=6)
     # Tensor-core forms: blocks of >= tc_min_k qubits on tcgen05.
     forms["tc_f6"] = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5)
+    # Learned planner: block boundaries, sizes and paths from the cost model
+    # trained on this engine's GB300 launch times.
+    model = L.CostMLP.load()
+    forms["learned_tc_f6"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                                    tc_min_k=2, cost_model=model)
     forms["tc_f6_all"] = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=1)
     forms["tc_f5_all"] = E.Plan(c, max_fused_size=5, tensor_path=True, tc_min_k=1)
 
@@ -337,6 +343,10 @@ def run_engine(args, world, rank, local, dist):
     N.lib.qsg_host_free(hbuf)
     e2e = max_over_ranks(dist, statistics.median(e2e_times))
 
+    # Learned planner on the 32-qubit 5x6+2 grid depth-24 circuit (32 GiB).
+    del st
+    learned = bench_learned_planner(ctx, ss, model, dist)
+
     # Batched trajectories (replicas for N > 1: every rank runs the batch).
     traj = bench_trajectories(args.traj_streams, args.traj_f,
                               args.traj_big_qubits, args.traj_big_streams)
@@ -375,8 +385,67 @@ def run_engine(args, world, rank, local, dist):
             "cpu_baseline": cpu,
             "clocks": clocks,
             "trajectories": traj,
+            "learned_planner": learned,
         }
         print(json.dumps(line), flush=True)
+
+
+LEARN_GRID = dict(rows=5, cols=6, extra=2, cycles=24, seed=1)
+
+
+def bench_learned_planner(ctx, ss, model, dist):
+    """Seconds per run of the 32-qubit 5x6+2 grid depth-24 circuit for the
+    learned plan and the fixed-size plans (CUDA-core f = 4, 5, 6 and
+    tensor-core f = 6), each replayed from a CUDA graph, and the fidelity of
+    the learned plan's state against the plain f = 4 plan's."""
+    import numpy as np
+    from qsim_gb300 import engine as E
+    from qsim_gb300 import _native as N
+    c = E.Circuit.grid(*LEARN_GRID.values())
+    n = c.num_qubits
+    forms = {
+        "plain_f4": E.Plan(c, max_fused_size=4),
+        "plain_f5": E.Plan(c, max_fused_size=5),
+        "plain_f6": E.Plan(c, max_fused_size=6),
+        "tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5),
+        "learned_tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True,
+                                tc_min_k=2, cost_model=model),
+    }
+    st = ss.Create(n)
+    ref = ss.Create(n)
+    if ss.IsNull(st) or ss.IsNull(ref):
+        return {"skipped": "not enough device memory for two 32-qubit states"}
+    times, predicted = {}, {}
+    for name, p in forms.items():
+        p.capture(ctx, st)
+        ss.SetStateZero(st)
+        p.replay(ctx)
+        ctx.sync()
+        barrier(dist)
+        ctx.timer_start()
+        ss.SetStateZero(st)
+        p.replay(ctx)
+        times[name] = max_over_ranks(dist, ctx.timer_stop() / 1e3)
+        predicted[name] = sum(model.cost_us(n, o["qs"], len(o["cqs"]), o["path"])
+                              for o in p.ops() if o["kind"] != 2) / 1e6
+        if name == "plain_f4":
+            ss.Copy(st, ref)
+    ip = C.c_double * 2
+    r = ip()
+    N.check(N.lib.qsg_inner_product(ctx.h, ref.get(), st.get(), n, r))
+    fid = (r[0] ** 2 + r[1] ** 2) / (ss.Norm(ref) * ss.Norm(st))
+    fixed = {k: v for k, v in times.items() if k != "learned_tc_f6"}
+    best_fixed = min(fixed, key=fixed.get)
+    return {
+        "workload": "grid5x6+2 (32 qubits) random circuit depth 24, seed 1, "
+                    "complex64 (32 GiB)",
+        "unit": "s/run", "forms_s": times, "predicted_s": predicted,
+        "passes": {k: len(v) for k, v in forms.items()},
+        "learned_vs_best_fixed": times[best_fixed] / times["learned_tc_f6"],
+        "best_fixed": best_fixed,
+        "learned_vs_plain_f4": times["plain_f4"] / times["learned_tc_f6"],
+        "fidelity_learned_vs_plain_f4": fid,
+    }
 
 
 TRAJ = dict(circuits=128, reps=32, n_min=12, n_max=24, cycles=12,

@@ -261,7 +261,7 @@ typedef struct qsg_fuse_options {
   unsigned seeds;           /* front gates tried per block (0: default) */
   int tensor_path;          /* route blocks of >= tc_min_k qubits to tcgen05 */
   unsigned tc_min_k;        /* 0: default 5 */
-  const void* cost_model;   /* engine cost model (NULL: gate-count rule) */
+  const void* cost_model;   /* a qsg_mlp* (NULL: gate-count rule) */
 } qsg_fuse_options;
 int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* opts,
                     qsg_plan** out);
@@ -286,6 +286,48 @@ int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p);
  * op_ms[i] = milliseconds of op i (measurement ops are skipped, 0). */
 int qsg_plan_profile(qsg_ctx* ctx, qsg_plan* p, float* state, float* op_ms,
                      uint64_t cap);
+
+/* ---- learned fusion planner --------------------------------------------
+ * No counterpart in the reference (its fuser, lib/fuser_mqubit.h:282-526,
+ * fuses up to a fixed max_fused_size).  A perceptron with 16 inputs, two
+ * hidden layers of 64 ReLU units and one output predicts the time of one
+ * fused-gate launch from features of the block (qsg_block_features):
+ * output = log(microseconds) - (n - 24) log 2.  It is trained on the device
+ * (forward, backward and Adam kernels of this library) on launch times the
+ * engine records with qsg_plan_profile.  Passed as
+ * qsg_fuse_options.cost_model, it makes qsg_plan_create choose block
+ * boundaries, block sizes up to max_fused_size and the path of each block
+ * (tensor cores for blocks of >= tc_min_k qubits when tensor_path is set) by
+ * the lowest predicted time per fused gate.  The plan changes only speed:
+ * every plan applies the same circuit. */
+#define QSG_MLP_INPUTS 16
+typedef struct qsg_mlp qsg_mlp;
+uint64_t qsg_mlp_num_params(void);
+/* He-uniform weights from std::mt19937_64(seed), zero biases. */
+int qsg_mlp_create(uint64_t seed, qsg_mlp** out);
+int qsg_mlp_destroy(qsg_mlp* m);
+/* Host copies of the qsg_mlp_num_params() parameters: W1[16][64], b1[64],
+ * W2[64][64], b2[64], W3[64], b3. */
+int qsg_mlp_get_params(const qsg_mlp* m, float* out);
+int qsg_mlp_set_params(qsg_mlp* m, const float* in);
+/* Host arrays x[n][16], y[n].  Gradient of the mean squared error over all
+ * samples (grad: qsg_mlp_num_params() floats) and that error, on the device. */
+int qsg_mlp_gradient(qsg_ctx* ctx, const qsg_mlp* m, const float* x,
+                     const float* y, uint64_t n, float* grad, double* loss);
+/* `steps` Adam steps (rate lr) on minibatches of `batch` samples from
+ * per-epoch permutations drawn from std::mt19937_64(seed). */
+int qsg_mlp_train(qsg_ctx* ctx, qsg_mlp* m, const float* x, const float* y,
+                  uint64_t n, unsigned steps, unsigned batch, float lr,
+                  uint64_t seed, double* final_loss);
+int qsg_mlp_predict(qsg_ctx* ctx, const qsg_mlp* m, const float* x,
+                    uint64_t n, float* out);
+/* Features of one launch: sorted target qubits as launched (the padded six
+ * for the tensor-core path, path = 1), control count. */
+int qsg_block_features(unsigned n, const unsigned* qs, unsigned k,
+                       unsigned ncontrols, int path, float* out);
+/* Predicted microseconds of a launch (qubits before tensor-core padding). */
+int qsg_mlp_cost_us(const qsg_mlp* m, unsigned n, const unsigned* qs,
+                    unsigned k, unsigned ncontrols, int path, double* out);
 
 /* ---- noisy circuits and quantum trajectories ---------------------------
  * Channels (lib/channel.h:31-125, lib/channels_cirq.h), MakeNoisy

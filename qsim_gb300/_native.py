@@ -121,6 +121,17 @@ SIGNATURES = {
     "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                  vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                  P_u64]),
+    "qsg_mlp_num_params": (u64, []),
+    "qsg_mlp_create": (i32, [u64, C.POINTER(vp)]),
+    "qsg_mlp_destroy": (i32, [vp]),
+    "qsg_mlp_get_params": (i32, [vp, P_f32]),
+    "qsg_mlp_set_params": (i32, [vp, P_f32]),
+    "qsg_mlp_gradient": (i32, [vp, vp, P_f32, P_f32, u64, P_f32, P_f64]),
+    "qsg_mlp_train": (i32, [vp, vp, P_f32, P_f32, u64, u32, u32, f32, u64,
+                            P_f64]),
+    "qsg_mlp_predict": (i32, [vp, vp, P_f32, u64, P_f32]),
+    "qsg_block_features": (i32, [u32, P_u32, u32, u32, i32, P_f32]),
+    "qsg_mlp_cost_us": (i32, [vp, u32, P_u32, u32, u32, i32, P_f64]),
     "qsg_timer_start": (i32, [vp]),
     "qsg_timer_stop": (i32, [vp, P_f32]),
 }

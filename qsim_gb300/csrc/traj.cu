@@ -203,6 +203,42 @@ __global__ void __launch_bounds__(kTrajThreads)
   }
 }
 
+// Rescales the state by sqrt(norm_before / norm_after), both given as the
+// partial sums of traj_stats_kernel (4 doubles per block); every block sums
+// the partials itself.
+__global__ void __launch_bounds__(kTrajThreads)
+    norm_restore_kernel(float4* __restrict__ s, uint64_t units,
+                        const double* __restrict__ before, unsigned nb,
+                        const double* __restrict__ after, unsigned na) {
+  __shared__ double red[2][kTrajThreads / 32];
+  double b = 0, a = 0;
+  for (unsigned i = threadIdx.x; i < 4 * nb; i += kTrajThreads) b += before[i];
+  for (unsigned i = threadIdx.x; i < 4 * na; i += kTrajThreads) a += after[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = b;
+    red[1][warp] = a;
+  }
+  __syncthreads();
+  b = 0;
+  a = 0;
+  for (int w = 0; w < kTrajThreads / 32; ++w) {
+    b += red[0][w];
+    a += red[1][w];
+  }
+  const float f = a > 0 ? float(sqrt(b / a)) : 1.f;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < units;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float4 x = s[i];
+    s[i] = make_float4(x.x * f, x.y * f, x.z * f, x.w * f);
+  }
+}
+
 // ---------------------------------------------------------------------------
 
 static unsigned traj_grid(qsg_ctx* ctx, uint64_t work, uint64_t per_block) {
@@ -249,6 +285,17 @@ int traj_apply(qsg_ctx* ctx, float* state, unsigned n, unsigned nq,
   traj_apply_kernel<<<grid, kTrajThreads, 0, ctx->stream>>>(
       reinterpret_cast<float2*>(state), groups, nq, nq > 0 ? q[0] : 0,
       nq > 1 ? q[1] : 0, mat_dev);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+int norm_restore(qsg_ctx* ctx, float* state, unsigned n, const double* before,
+                 unsigned nb, const double* after, unsigned na) {
+  QSG_CHECK_ARG(n >= 1, "norm restore: n >= 1");
+  const uint64_t units = uint64_t{1} << (n - 1);
+  const unsigned grid = traj_grid(ctx, units, uint64_t(kTrajThreads) * 8);
+  norm_restore_kernel<<<grid, kTrajThreads, 0, ctx->stream>>>(
+      reinterpret_cast<float4*>(state), units, before, nb, after, na);
   QSG_LAUNCHED(ctx);
   return QSG_OK;
 }

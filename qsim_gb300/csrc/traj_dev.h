@@ -50,4 +50,10 @@ int traj_choose(qsg_ctx* ctx, const double* partial, unsigned nparts,
 int traj_apply(qsg_ctx* ctx, float* state, unsigned n, unsigned nq,
                const unsigned* q, const float* mat_dev);
 
+// Rescales `state` by sqrt(norm_before / norm_after), the norms given as
+// traj_channel_stats partials (nq = 0) of the state before and after a
+// unitary sequence of launches.
+int norm_restore(qsg_ctx* ctx, float* state, unsigned n, const double* before,
+                 unsigned nb, const double* after, unsigned na);
+
 }  // namespace qsg

@@ -171,6 +171,8 @@ class Plan:
         if unfused:
             check(N.lib.qsg_plan_create_unfused(circuit.h, C.byref(h)))
         else:
+            if cost_model is not None and hasattr(cost_model, "h"):
+                cost_model = cost_model.h.value   # a learned.CostMLP
             o = N.FuseOptions(max_fused_size, seeds, int(tensor_path), tc_min_k,
                               cost_model)
             check(N.lib.qsg_plan_create(circuit.h, C.byref(o), C.byref(h)))
@@ -207,6 +209,7 @@ class Plan:
         return [self.op(i) for i in range(len(self))]
 
     def run(self, ctx, state, seed: int = 1, max_meas: int = 1024):
+        self._ctx = ctx   # the plan's device buffers belong to this context
         bits = np.zeros(max_meas, dtype=np.uint64)
         nm = C.c_uint64()
         check(N.lib.qsg_plan_run(ctx.h, self.h, state.get(), seed,
@@ -215,10 +218,12 @@ class Plan:
         return bits[:nm.value]
 
     def capture(self, ctx, state):
+        self._ctx = ctx   # the plan's device buffers belong to this context
         check(N.lib.qsg_plan_capture(ctx.h, self.h, state.get()))
 
     def profile(self, ctx, state):
         """Per-op milliseconds (CUDA events around each launch)."""
+        self._ctx = ctx   # the plan's device buffers belong to this context
         n = len(self)
         ms = np.zeros(max(1, n), dtype=np.float32)
         check(N.lib.qsg_plan_profile(ctx.h, self.h, state.get(),
@@ -226,6 +231,7 @@ class Plan:
         return ms[:n]
 
     def replay(self, ctx):
+        self._ctx = ctx   # the plan's device buffers belong to this context
         check(N.lib.qsg_plan_replay(ctx.h, self.h))
 
     def __del__(self):

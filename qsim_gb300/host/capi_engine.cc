@@ -7,6 +7,7 @@
 
 #include "capi_types.h"
 #include "engine.h"
+#include "learned.h"
 #include "internal.h"
 #include "runner.h"
 
@@ -227,7 +228,7 @@ int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* o,
     fo.seeds = o->seeds ? o->seeds : fo.seeds;
     fo.tensor_path = o->tensor_path != 0;
     fo.tc_min_k = o->tc_min_k ? o->tc_min_k : fo.tc_min_k;
-    fo.cost = static_cast<const CostModel*>(o->cost_model);
+    fo.cost = qsg::cost_model_from_handle(o->cost_model);
   }
   if (fo.max_fused_size < 1 || fo.max_fused_size > 6)
     return invalid("max_fused_size must be 1..6");

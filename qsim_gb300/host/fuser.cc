@@ -106,6 +106,7 @@ struct Block {
   std::vector<int> members;
   uint64_t mask = 0;
   double score = -1e300;
+  Path path = Path::kCudaCore;
 };
 
 // One absorb scan over the unscheduled ops of [first, end): ops whose qubits
@@ -245,8 +246,16 @@ Plan unfused(const Circuit& c) {
   return p;
 }
 
-Plan fuse(const Circuit& c, const FuseOptions& opt) {
-  const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
+namespace {
+
+// One greedy pass with block-size limit f.  Without a cost model (and with
+// per_gate false) every block grows to f qubits, the candidate absorbing the
+// most gates wins and blocks of >= tc_min_k qubits take the tensor-core
+// path.  With a cost model each block's path is the one with the lower
+// predicted time; with per_gate, blocks of every size limit from the seed's
+// size to f compete and the lowest predicted time per absorbed gate wins.
+Plan fuse_greedy(const Circuit& c, const FuseOptions& opt, unsigned f,
+                 bool per_gate) {
   Plan plan;
   plan.num_qubits = c.num_qubits;
   const size_t nops = c.ops.size();
@@ -255,11 +264,19 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
   auto fusible = [&](const Op& op) {
     return op.kind == OpKind::kGate && op.qs.size() <= f;
   };
-  auto cost_of = [&](const std::vector<unsigned>& qs) {
-    return opt.cost->cost_us(c.num_qubits, qs, 0,
-                             (opt.tensor_path && qs.size() >= opt.tc_min_k)
-                                 ? Path::kTensor
-                                 : Path::kCudaCore);
+  // With a cost model: the cheaper path for a block (tensor cores only for
+  // blocks of >= tc_min_k qubits on >= 12-qubit states) and its cost.
+  auto cost_of = [&](const std::vector<unsigned>& qs, Path* path) {
+    double best = opt.cost->cost_us(c.num_qubits, qs, 0, Path::kCudaCore);
+    *path = Path::kCudaCore;
+    if (opt.tensor_path && qs.size() >= opt.tc_min_k && c.num_qubits >= 12) {
+      const double t = opt.cost->cost_us(c.num_qubits, qs, 0, Path::kTensor);
+      if (t < best) {
+        best = t;
+        *path = Path::kTensor;
+      }
+    }
+    return best;
   };
 
   size_t seg_begin = 0;
@@ -305,18 +322,34 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
       }
       Block best;
       for (size_t seed : seeds) {
-        Block b = grow_block(c, done, first, seg_end, seed, f, fusible);
-        std::vector<unsigned> qs;
-        for (unsigned q = 0; q < c.num_qubits; ++q)
-          if ((b.mask >> q) & 1) qs.push_back(q);
-        if (opt.cost) {
-          double alone = 0;
-          for (int mi : b.members) alone += cost_of(c.ops[mi].qs);
-          b.score = alone - cost_of(qs);
-        } else {
-          b.score = double(b.members.size()) - 1e-3 * double(qs.size());
+        // Without a cost model every block grows to f qubits and the one
+        // absorbing the most gates wins.  With one, blocks of every size
+        // limit from the seed's size to f compete, and the one with the
+        // lowest predicted time per absorbed gate wins: the model chooses
+        // the block boundaries, the block size and the path.
+        const unsigned lo = (opt.cost && per_gate)
+                                ? std::max<unsigned>(
+                                      1, unsigned(c.ops[seed].qs.size()))
+                                : f;
+        for (unsigned lim = lo; lim <= f; ++lim) {
+          Block b = grow_block(c, done, first, seg_end, seed, lim, fusible);
+          std::vector<unsigned> qs;
+          for (unsigned q = 0; q < c.num_qubits; ++q)
+            if ((b.mask >> q) & 1) qs.push_back(q);
+          if (opt.cost && per_gate) {
+            b.score = -cost_of(qs, &b.path) / double(b.members.size());
+          } else if (opt.cost) {
+            b.score = double(b.members.size()) - 1e-3 * double(qs.size());
+            cost_of(qs, &b.path);
+          } else {
+            b.score = double(b.members.size()) - 1e-3 * double(qs.size());
+            b.path = (opt.tensor_path && qs.size() >= opt.tc_min_k &&
+                      c.num_qubits >= 12)
+                         ? Path::kTensor
+                         : Path::kCudaCore;
+          }
+          if (b.score > best.score) best = std::move(b);
         }
-        if (b.score > best.score) best = std::move(b);
       }
       PlanOp po;
       po.kind = OpKind::kGate;
@@ -326,8 +359,7 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
       po.members = best.members;
       for (int mi : best.members) done[mi] = 1;
       finish(c, po);
-      if (opt.tensor_path && po.qs.size() >= opt.tc_min_k &&
-          c.num_qubits >= 12) {
+      if (best.path == Path::kTensor) {
         pad_block_to_6(c.num_qubits, po);
         po.path = Path::kTensor;
       }
@@ -346,6 +378,42 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
     seg_begin = seg_end + 1;
   }
   return plan;
+}
+
+double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
+  double t = 0;
+  for (const auto& op : p.ops) {
+    if (op.kind == OpKind::kMeasure) continue;
+    t += m.cost_us(c.num_qubits, op.qs, unsigned(op.cqs.size()), op.path);
+  }
+  return t;
+}
+
+}  // namespace
+
+Plan fuse(const Circuit& c, const FuseOptions& opt) {
+  const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
+  if (!opt.cost) return fuse_greedy(c, opt, f, false);
+  // Learned planner: candidate plans for every block-size limit up to f,
+  // grown by gate count and by predicted time per gate, each block on its
+  // predicted-faster path; the plan of lowest predicted total time wins.
+  // The fixed-size plans of the gate-count rule are among the candidates.
+  Plan best;
+  double best_t = 0;
+  bool have = false;
+  for (unsigned ff = 1; ff <= f; ++ff) {
+    for (int pg = 0; pg < 2; ++pg) {
+      if (ff == 1 && pg) continue;
+      Plan p = fuse_greedy(c, opt, ff, pg != 0);
+      const double t = plan_cost(c, p, *opt.cost);
+      if (!have || t < best_t) {
+        best = std::move(p);
+        best_t = t;
+        have = true;
+      }
+    }
+  }
+  return best;
 }
 
 }  // namespace host

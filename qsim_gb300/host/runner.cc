@@ -8,6 +8,7 @@
 // given state buffer and replayed; k = 6 matrices and tensor-core operands
 // then live in a device buffer owned by the plan.
 
+#include <cmath>
 #include <cstring>
 #include <random>
 
@@ -16,6 +17,7 @@
 #include "engine.h"
 #include "internal.h"
 #include "runner.h"
+#include "traj_dev.h"
 
 namespace qsg {
 namespace host {
@@ -26,8 +28,20 @@ void PlanRuntime::release() {
   if (graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph_exec));
   if (graph) cudaGraphDestroy(static_cast<cudaGraph_t>(graph));
   graph_exec = graph = nullptr;
-  if (dmat && ctx) dev_free(ctx, dmat);
-  if (tc_buf && ctx) dev_free(ctx, tc_buf);
+  // Freed on the device that holds them, without the context: the context
+  // may already be gone (cudaFree waits for the device).
+  if ((dmat || tc_buf || norm_buf) && device >= 0) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(device);
+    if (dmat) cudaFree(dmat);
+    if (tc_buf) cudaFree(tc_buf);
+    if (norm_buf) cudaFree(norm_buf);
+    cudaSetDevice(cur);
+  }
+  norm_buf = nullptr;
+  restore_norm = false;
+  uploaded = false;
   dmat = nullptr;
   tc_buf = nullptr;
   dmat_off.clear();
@@ -35,9 +49,45 @@ void PlanRuntime::release() {
   tc_ready = false;
 }
 
+namespace {
+
+bool is_unitary(const std::vector<cplx>& m) {
+  const size_t d = size_t(std::sqrt(double(m.size())) + 0.5);
+  for (size_t r = 0; r < d; ++r)
+    for (size_t c = 0; c < d; ++c) {
+      cplx a = 0;
+      for (size_t j = 0; j < d; ++j) a += std::conj(m[j * d + r]) * m[j * d + c];
+      if (std::abs(a - (r == c ? 1.0 : 0.0)) > 1e-5) return false;
+    }
+  return true;
+}
+
+}  // namespace
+
 int PlanRuntime::upload(qsg_ctx* c) {
-  if (dmat) return QSG_OK;
+  if (uploaded) return QSG_OK;
   ctx = c;
+  device = ctx_device(c);
+  bool tc = false, unitary = true;
+  for (const auto& op : plan.ops) {
+    if (op.kind == OpKind::kMeasure) unitary = false;
+    if (op.kind == OpKind::kGate && op.path == Path::kTensor) tc = true;
+  }
+  if (tc && unitary) {
+    for (const auto& op : plan.ops)
+      if (!is_unitary(op.m)) {
+        unitary = false;
+        break;
+      }
+  }
+  if (tc && unitary) {
+    void* p = nullptr;
+    int rc = dev_alloc(ctx, 2 * size_t(traj_max_parts(ctx)) * 4 * sizeof(double),
+                       &p);
+    if (rc) return rc;
+    norm_buf = static_cast<double*>(p);
+    restore_norm = true;
+  }
   size_t total = 0;
   dmat_off.assign(plan.ops.size(), size_t(-1));
   for (size_t i = 0; i < plan.ops.size(); ++i) {
@@ -48,7 +98,10 @@ int PlanRuntime::upload(qsg_ctx* c) {
       total += op.m32.size();
     }
   }
-  if (total == 0) return QSG_OK;
+  if (total == 0) {
+    uploaded = true;
+    return QSG_OK;
+  }
   void* p = nullptr;
   int rc = dev_alloc(ctx, total * sizeof(float), &p);
   if (rc) return rc;
@@ -59,7 +112,9 @@ int PlanRuntime::upload(qsg_ctx* c) {
     std::memcpy(&host[dmat_off[i]], plan.ops[i].m32.data(),
                 plan.ops[i].m32.size() * sizeof(float));
   }
-  return dev_upload(ctx, dmat, host.data(), total * sizeof(float));
+  rc = dev_upload(ctx, dmat, host.data(), total * sizeof(float));
+  if (rc == QSG_OK) uploaded = true;
+  return rc;
 }
 
 int PlanRuntime::prepare_tc() {
@@ -85,6 +140,7 @@ int PlanRuntime::prepare_tc() {
     int rc = dev_alloc(ctx, total, &p);
     if (rc) return rc;
     tc_buf = p;
+    device = ctx_device(ctx);
     std::vector<unsigned char> host(total);
     for (size_t i = 0; i < plan.ops.size(); ++i) {
       if (tc_off[i] == size_t(-1)) continue;
@@ -117,6 +173,29 @@ int PlanRuntime::launch_op(size_t i, float* state) {
                        dm);
 }
 
+int PlanRuntime::launch_all(float* state) {
+  const unsigned n = plan.num_qubits;
+  double* before = norm_buf;
+  double* after = norm_buf ? norm_buf + size_t(traj_max_parts(ctx)) * 4 : nullptr;
+  unsigned nb = 0, na = 0;
+  int rc;
+  if (restore_norm) {
+    rc = traj_channel_stats(ctx, state, n, 0, nullptr, before, &nb);
+    if (rc) return rc;
+  }
+  for (size_t i = 0; i < plan.ops.size(); ++i) {
+    rc = launch_op(i, state);
+    if (rc) return rc;
+  }
+  if (restore_norm) {
+    rc = traj_channel_stats(ctx, state, n, 0, nullptr, after, &na);
+    if (rc) return rc;
+    rc = norm_restore(ctx, state, n, before, nb, after, na);
+    if (rc) return rc;
+  }
+  return QSG_OK;
+}
+
 int PlanRuntime::run(qsg_ctx* c, float* state, unsigned seed,
                      std::vector<uint64_t>* mbits) {
   ctx = c;
@@ -124,6 +203,7 @@ int PlanRuntime::run(qsg_ctx* c, float* state, unsigned seed,
   if (rc) return rc;
   rc = prepare_tc();
   if (rc) return rc;
+  if (restore_norm) return launch_all(state);
   std::mt19937 rgen(seed);
   const unsigned n = plan.num_qubits;
   for (size_t i = 0; i < plan.ops.size(); ++i) {
@@ -176,14 +256,12 @@ int PlanRuntime::capture(qsg_ctx* c, float* state) {
     set_error_msg("cudaStreamBeginCapture failed");
     return QSG_ERR_CUDA;
   }
-  for (size_t i = 0; i < plan.ops.size(); ++i) {
-    rc = launch_op(i, state);
-    if (rc) {
-      cudaGraph_t g;
-      cudaStreamEndCapture(s, &g);
-      if (g) cudaGraphDestroy(g);
-      return rc;
-    }
+  rc = launch_all(state);
+  if (rc) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(s, &g);
+    if (g) cudaGraphDestroy(g);
+    return rc;
   }
   cudaGraph_t g = nullptr;
   if (cudaStreamEndCapture(s, &g) != cudaSuccess) {

@@ -39,6 +39,13 @@ struct PlanRuntime {
   void* graph = nullptr;             // cudaGraph_t
   void* graph_exec = nullptr;        // cudaGraphExec_t
   float* captured_state = nullptr;
+  int device = -1;                   // device of dmat / tc_buf / norm_buf
+  // Tensor-core plans of unitary gates rescale the state to its input norm
+  // after the last launch: the tensor cores' FP32 accumulation rounds
+  // toward zero and shrinks the norm by ~6e-7 per pass.
+  bool restore_norm = false;
+  bool uploaded = false;
+  double* norm_buf = nullptr;        // two sets of norm partials
 
   PlanRuntime() = default;
   PlanRuntime(const PlanRuntime&) = delete;
@@ -50,6 +57,8 @@ struct PlanRuntime {
   int prepare_tc();
   const void* tc_operands(size_t i) const;
   int launch_op(size_t i, float* state);
+  // Every gate op in order (with the norm restoration); no measurements.
+  int launch_all(float* state);
   // Runs every op; measurement bits are appended to `mbits`.
   int run(qsg_ctx* ctx, float* state, unsigned seed,
           std::vector<uint64_t>* mbits);

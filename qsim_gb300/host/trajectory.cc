@@ -258,7 +258,7 @@ TrajectoryRunner::~TrajectoryRunner() {
   if (dev_table_) {
     int cur = 0;
     cudaGetDevice(&cur);
-    cudaSetDevice(ctx_device(dev_ctx_));
+    cudaSetDevice(dev_device_);
     cudaFree(dev_table_);
     cudaSetDevice(cur);
   }
@@ -399,7 +399,7 @@ int TrajectoryRunner::upload(qsg_ctx* ctx) const {
     return rc;
   }
   dev_table_ = static_cast<TrajChannelDev*>(p);
-  dev_ctx_ = ctx;
+  dev_device_ = ctx_device(ctx);
   return QSG_OK;
 }
 

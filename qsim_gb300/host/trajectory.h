@@ -151,7 +151,7 @@ class TrajectoryRunner {
   std::vector<Channel> chans_;
   std::vector<std::vector<Op>> kop_ops_;  // per channel, per kop: one op
   mutable TrajChannelDev* dev_table_ = nullptr;
-  mutable qsg_ctx* dev_ctx_ = nullptr;
+  mutable int dev_device_ = -1;
   size_t num_dev_channels_ = 0;
 };
 

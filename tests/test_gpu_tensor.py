@@ -122,3 +122,29 @@ def test_tc_plan_matches_oracle(eng, oracle, f):
         ctx.sync()
         assert rel_l2(ss.to_numpy(st), want) < 1e-5
     assert tc_error(N, ctx) == 0
+
+
+def test_tc_deep_plan_keeps_norm_and_accuracy(eng, oracle):
+    """A plan with ~70 tensor-core passes stays within relative L2 1e-5 of
+    FP64: the tensor cores' FP32 accumulation rounds toward zero (about
+    6e-7 of norm lost per pass), which the plan corrects by restoring the
+    input norm after its last launch (unitary plans)."""
+    q, E, N, ctx, ss, sim = eng
+    c = E.Circuit.grid(4, 5, 0, 40, 21)
+    n = c.num_qubits
+    plan = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=2)
+    assert plan.info()["num_tensor_ops"] >= 40
+    want = oracle.zero_state(n)
+    for o in c.ops():
+        oracle.apply_gate(want, n, o["qs"], o["m"])
+    st = ss.Create(n)
+    ss.SetStateZero(st)
+    plan.run(ctx, st)
+    got = ss.to_numpy(st)
+    assert abs(np.linalg.norm(got) - 1) < 1e-6
+    assert rel_l2(got, want) < 1e-5
+    plan.capture(ctx, st)
+    ss.SetStateZero(st)
+    plan.replay(ctx)
+    ctx.sync()
+    assert rel_l2(ss.to_numpy(st), want) < 1e-5

@@ -1,0 +1,179 @@
+"""Learned fusion planner: the cost-model network and the planner that uses
+it (no counterpart in the reference; its fixed-size fuser is the judge).
+
+CPU: the FP64 oracle of the network (oracle/mlp_oracle.py) is checked
+against finite differences; the engine's host inference matches it; the
+committed GB300-trained weights fit the committed timing data; the planner
+with the model yields valid plans whose predicted time is no worse than the
+fixed-size plans'.  GPU: the device forward pass and gradients match the
+oracle; device training is deterministic and fits; a learned plan applies
+the same circuit as the fixed plans, and its measured time is compared with
+the fixed-size plans on the GB300."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_l2
+
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import mlp_oracle as MO  # noqa: E402
+
+from qsim_gb300 import engine as E  # noqa: E402
+from qsim_gb300 import learned as L  # noqa: E402
+
+WEIGHTS = os.path.join(ROOT, "qsim_gb300", "data", "cost_mlp_gb300.npz")
+TIMINGS = os.path.join(ROOT, "qsim_gb300", "data", "cost_timings_gb300.npz")
+
+GRAD_TOL = 1e-4     # device FP32 gradient vs FP64 oracle, relative L2
+FWD_TOL = 1e-4      # device / host FP32 forward vs FP64 oracle, absolute
+
+
+def random_batch(n=3000, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n, 16)).astype(np.float32)
+    y = (np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2] - 0.3 * x[:, 3]).astype(np.float32)
+    return x, y
+
+
+# ------------------------------------------------------------------ CPU --
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(1)
+    p = L.CostMLP(5).get_params().astype(np.float64)
+    x = rng.normal(size=(40, 16))
+    y = rng.normal(size=40)
+    _, g = MO.loss_and_grad(p, x, y)
+    idx = rng.choice(MO.N_PARAMS, 60, replace=False)
+    fd = MO.finite_difference_grad(p, x, y, idx)
+    assert np.max(np.abs(fd - g[idx])) <= 1e-7 * max(1.0, np.max(np.abs(g[idx])))
+
+
+def test_host_inference_matches_oracle():
+    m = L.CostMLP(11)
+    p = m.get_params()
+    for n, qs, nc, path in [(26, [3, 7, 9, 12], 0, 0), (30, [0, 1, 2, 25, 26, 29], 0, 1),
+                            (24, [5], 2, 0), (32, [30, 31], 0, 0)]:
+        f = L.features(n, qs, nc, path)
+        want = np.exp(MO.forward(p, f[None])[0] + (n - 24) * np.log(2))
+        assert abs(m.cost_us(n, qs, nc, path) - want) <= 1e-5 * want
+
+
+def test_features_encode_the_launch():
+    f = L.features(30, [0, 4, 29], 1, 0)
+    assert f[0] == pytest.approx(0.5) and f[1] == pytest.approx(0.25)
+    assert f[2] == pytest.approx(0.75) and f[3] == 0
+    assert f[10] == 1 and f[13] == pytest.approx(1 / 3)
+    assert list(f[7:10]) == [-0.25, -0.25, -0.25]
+    with pytest.raises(E.N.QsgError):
+        L.features(10, [3, 2], 0, 0)       # unsorted
+
+
+def test_committed_model_fits_committed_timings():
+    with np.load(TIMINGS) as z:
+        X, y, n = z["X"], z["y"], z["n"]
+    m = L.CostMLP.load(WEIGHTS)
+    p = m.get_params()
+    test = np.arange(len(y)) % 10 == 0        # the held-out tenth
+    pred = MO.forward(p, X[test])
+    mse = float(np.mean((pred - y[test]) ** 2))
+    assert mse < 0.01, mse                    # < 10 % rms error in time
+    assert set(np.unique(n)) >= set(range(24, 33))
+
+
+def test_learned_plans_valid_and_predicted_no_worse():
+    m = L.CostMLP.load(WEIGHTS)
+    c = E.Circuit.grid(5, 6, 2, 24, 1)
+    n = c.num_qubits
+    learned = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=2, cost_model=m)
+    for o in learned.ops():
+        assert len(o["qs"]) <= 6
+        if o["path"] == 1:
+            assert len(o["qs"]) == 6
+    pred = lambda p: sum(m.cost_us(n, o["qs"], len(o["cqs"]), o["path"])
+                         for o in p.ops() if o["kind"] != 2)
+    t_learned = pred(learned)
+    for f in (2, 3, 4, 5, 6):
+        for tc in (False, True):
+            fixed = E.Plan(c, max_fused_size=f, tensor_path=tc, tc_min_k=5)
+            assert t_learned <= pred(fixed) * (1 + 1e-9)
+
+
+# ------------------------------------------------------------------ GPU --
+
+@pytest.fixture(scope="module")
+def ctx():
+    from qsim_gb300 import api
+    return api.Context()
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_matches_oracle(ctx):
+    x, y = random_batch()
+    m = L.CostMLP(3)
+    loss, g = m.gradient(ctx, x, y)
+    want_loss, want = MO.loss_and_grad(m.get_params(), x, y)
+    assert abs(loss - want_loss) <= 1e-5 * want_loss
+    assert np.linalg.norm(g - want) <= GRAD_TOL * np.linalg.norm(want)
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle(ctx):
+    x, _ = random_batch(2000, 4)
+    m = L.CostMLP(8)
+    got = m.predict(ctx, x)
+    want = MO.forward(m.get_params(), x)
+    assert np.max(np.abs(got - want)) <= FWD_TOL * max(1.0, np.max(np.abs(want)))
+
+
+@pytest.mark.gpu
+def test_gpu_training_fits_and_is_deterministic(ctx):
+    x, y = random_batch(4096, 2)
+    m1, m2 = L.CostMLP(1), L.CostMLP(1)
+    l0, _ = m1.gradient(ctx, x, y)
+    l1 = m1.train(ctx, x, y, steps=1500, batch=512, lr=2e-3, seed=9)
+    l2 = m2.train(ctx, x, y, steps=1500, batch=512, lr=2e-3, seed=9)
+    assert l1 < 0.05 * l0, (l0, l1)
+    assert l1 == l2
+    np.testing.assert_array_equal(m1.get_params(), m2.get_params())
+
+
+@pytest.mark.gpu
+def test_gpu_learned_plan_same_state_and_timed(ctx):
+    """The plan changes only speed: the learned plan's state matches the
+    fixed-size plan's (fidelity >= 1 - 1e-6), and its measured time is
+    compared with every fixed-size plan (gain reported)."""
+    import qsim_gb300 as q
+    ss = q.StateSpace(ctx=ctx)
+    m = L.CostMLP.load(WEIGHTS)
+    c = E.Circuit.grid(4, 6, 2, 20, 3)        # 26 qubits
+    n = c.num_qubits
+    st = ss.Create(n)
+    plans = {f"f{f}" + ("_tc" if tc else ""): E.Plan(c, max_fused_size=f,
+                                                     tensor_path=tc, tc_min_k=5)
+             for f in (4, 5, 6) for tc in (False, True) if tc or f < 6}
+    plans["learned"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                              tc_min_k=2, cost_model=m)
+    states, times = {}, {}
+    for name, p in plans.items():
+        ss.SetStateZero(st)
+        p.run(ctx, st)
+        states[name] = ss.to_numpy(st)
+        p.capture(ctx, st)
+        ss.SetStateZero(st)
+        p.replay(ctx)
+        ctx.sync()
+        ctx.timer_start()
+        for _ in range(5):
+            ss.SetStateZero(st)
+            p.replay(ctx)
+        times[name] = ctx.timer_stop() / 5
+    for name, s in states.items():
+        fid = abs(np.vdot(states["f4"], s)) ** 2
+        assert fid >= 1 - 1e-6, (name, fid)
+        assert rel_l2(s, states["f4"]) < 1e-5
+    best_fixed = min(v for k, v in times.items() if k != "learned")
+    print("plan times (ms):", {k: round(v, 3) for k, v in times.items()})
+    assert times["learned"] <= 1.05 * best_fixed
+    assert times["learned"] < times["f4"]
