@@ -508,29 +508,69 @@ def bench_trajectories(num_streams: int, max_fused_size: int = 4,
 
 
 def kernel_case(spec: str, n: int, reps: int):
-    """Small profiling case: `spec` = "gate:q0,q1,.." (CUDA-core tile
-    kernel) or "tc:q0,.." (tensor-core kernel); one random unitary applied
-    `reps` times to a uniform n-qubit state."""
+    """Small profiling case on a uniform n-qubit state, `reps` launches of
+    one kind:
+
+      gate:q0,q1,..           CUDA-core tile kernel (random unitary)
+      tc:q0,..                tensor-core kernel (random unitary)
+      ctrl:q0,..:c0,..        controlled gate, controls all 1
+      ev:q0,..                ExpectationValue (tile kernel, mode 1)
+      norm | ip | multiply    reductions / elementwise pass
+      sample                  1000 samples (chunk sums, prefix, search)
+      collapse:mask           Collapse on bits = 0 of `mask` (hex)
+    """
+    import ctypes as Cx
     import numpy as np
     import qsim_gb300 as q
     from qsim_gb300 import _native as N
-    kind, qs = spec.split(":")
-    qs = [int(x) for x in qs.split(",")]
+    parts = spec.split(":")
+    kind = parts[0]
+    qs = [int(x) for x in parts[1].split(",")] if len(parts) > 1 and kind in (
+        "gate", "tc", "ctrl", "ev") else []
+    cqs = [int(x) for x in parts[2].split(",")] if kind == "ctrl" else []
     ctx = q.Context(0)
     ss, sim = q.StateSpace(ctx=ctx), q.Simulator(ctx=ctx)
     st = ss.Create(n)
     ss.SetStateUniform(st)
+    other = None
+    if kind == "ip":
+        other = ss.Create(n)
+        ss.SetStateUniform(other)
     k = len(qs)
     rng = np.random.default_rng(0)
     u, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) +
                         1j * rng.normal(size=(1 << k, 1 << k)))
     m = np.ascontiguousarray(u.astype(np.complex64)).view(np.float32)
+    out2 = (Cx.c_double * 2)()
+    smp = np.zeros(1000, dtype=np.uint64)
     for _ in range(reps):
         if kind == "tc":
             N.check(N.lib.qsg_apply_gate_tc(ctx.h, st.get(), n, N.u32_array(qs),
                                             k, m.ctypes.data_as(N.P_f32)))
-        else:
+        elif kind == "gate":
             sim.ApplyGate(qs, m, st)
+        elif kind == "ctrl":
+            N.check(N.lib.qsg_apply_controlled_gate(
+                ctx.h, st.get(), n, N.u32_array(qs), k, N.u32_array(cqs),
+                len(cqs), (1 << len(cqs)) - 1, m.ctypes.data_as(N.P_f32)))
+        elif kind == "ev":
+            N.check(N.lib.qsg_expectation_value(
+                ctx.h, st.get(), n, N.u32_array(qs), k,
+                m.ctypes.data_as(N.P_f32), out2))
+        elif kind == "norm":
+            N.check(N.lib.qsg_norm(ctx.h, st.get(), n, out2))
+        elif kind == "ip":
+            N.check(N.lib.qsg_inner_product(ctx.h, st.get(), other.get(), n, out2))
+        elif kind == "multiply":
+            N.check(N.lib.qsg_multiply(ctx.h, 1.0, st.get(), n))
+        elif kind == "sample":
+            N.check(N.lib.qsg_sample(ctx.h, st.get(), n, 1000, 1,
+                                     smp.ctypes.data_as(N.P_u64)))
+        elif kind == "collapse":
+            ss.SetStateUniform(st)
+            N.check(N.lib.qsg_collapse(ctx.h, st.get(), n, int(parts[1], 16), 0))
+        else:
+            raise SystemExit(f"unknown kernel case {spec!r}")
     ctx.sync()
     print(json.dumps({"kernel_case": spec, "n": n, "reps": reps,
                       "norm": ss.Norm(st)}))

@@ -39,6 +39,7 @@ def _sources():
 
 def _headers():
     hs = glob.glob(os.path.join(HERE, "csrc", "*.cuh"))
+    hs += glob.glob(os.path.join(HERE, "csrc", "*.h"))
     hs += glob.glob(os.path.join(HERE, "host", "*.h"))
     hs += glob.glob(os.path.join(ROOT, "include", "*.h"))
     hs += glob.glob(os.path.join(ROOT, "include", "qsim_gb300", "*.h"))
