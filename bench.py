@@ -348,10 +348,21 @@ def run_engine(args, world, rank, local, dist):
     learned = bench_learned_planner(ctx, ss, model, dist)
 
     # Batched trajectories (replicas for N > 1: every rank runs the batch).
+    # Headline: one persistent kernel over the packed batch; the stream path
+    # (one launch per fused op, concurrent host threads) is timed beside it.
     traj = bench_trajectories(args.traj_streams, args.traj_f,
-                              args.traj_big_qubits, args.traj_big_streams)
+                              mode=args.traj_mode,
+                              ctas_per_sm=args.traj_ctas_per_sm,
+                              tile_kib=args.traj_tile_kib,
+                              split=args.traj_split)
     traj["wall_s"] = max_over_ranks(dist, traj["wall_s"])
     traj["value"] = world * traj["trajectories"] / traj["wall_s"]
+    # The stream path alone at f = 4 (one launch per fused block) beside it.
+    alt = bench_trajectories(args.traj_streams, 4, mode="streams")
+    traj["streams_only"] = {"value": alt["value"], "wall_s": alt["wall_s"],
+                            "latency_ms_p50": alt["latency_ms_p50"],
+                            "latency_ms_p99": alt["latency_ms_p99"],
+                            "gpu_launches": alt["gpu_launches"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -456,32 +467,58 @@ TRAJ_WORKLOAD = ("4096 noisy trajectories: 128 chain random circuits, n ~ "
                  "repetitions each")
 
 
-def bench_trajectories(num_streams: int, max_fused_size: int = 4,
-                       big_qubits: int = 0, big_streams: int = 1,
-                       warm: bool = True):
+def bench_trajectories(num_streams: int, max_fused_size: int = 0,
+                       mode: str = "auto", ctas_per_sm: int = 0,
+                       tile_kib: int = 0, split: int = -1):
     """Batched-trajectory workload: every trajectory from |0..0>, its final
     state left normalised in HBM and its Kraus statistics copied to the
-    host.  traj/s = trajectories / batch wall time (host enqueue, device work
-    and the final synchronisation); latency = per-trajectory device time."""
+    host.  traj/s = trajectories / batch wall time (program compilation,
+    upload, device work and the final synchronisation); latency =
+    per-trajectory device time.
+
+    mode "auto": the autotuner picks fusion size, the split between the
+    persistent packed kernel and the concurrent stream path, CTAs per SM and
+    tile budget on an eighth of the repetitions (outside the timed run);
+    "packed": every circuit in the persistent kernel; "streams": the stream
+    path only."""
     import numpy as np
     from qsim_gb300 import engine as E
+    from qsim_gb300 import autotune as AT
     rng = np.random.default_rng(TRAJ["seed"])
     ns = rng.integers(TRAJ["n_min"], TRAJ["n_max"] + 1, size=TRAJ["circuits"])
+    made = {}
+
+    def make_runners(f):
+        if f not in made:
+            rs = []
+            for i, n in enumerate(ns):
+                c = E.Circuit.chain(int(n), TRAJ["cycles"], 1000 + i)
+                nc = E.NoisyCircuit.make(c, TRAJ["p_depol"], TRAJ["gamma"], 2)
+                rs.append(E.Trajectories(nc, max_fused_size=f))
+            made[f] = rs
+        return made[f]
+
     t0 = time.perf_counter()
-    runners = []
-    for i, n in enumerate(ns):
-        c = E.Circuit.chain(int(n), TRAJ["cycles"], 1000 + i)
-        nc = E.NoisyCircuit.make(c, TRAJ["p_depol"], TRAJ["gamma"], 2)
-        runners.append(E.Trajectories(nc, max_fused_size=max_fused_size))
+    tune = None
+    if mode == "auto":
+        tune = AT.tune_trajectories(
+            make_runners, ns, TRAJ["reps"], tag="chain d12 depol1e-3 ad5e-3",
+            fs=(max_fused_size,) if max_fused_size else (3, 4),
+            num_streams=num_streams, use_cache=False)
+        cfg = dict(tune["best"])
+    elif mode == "packed":
+        cfg = dict(max_fused_size=max_fused_size or 4, split=int(ns.max()),
+                   ctas_per_sm=ctas_per_sm, tile_kib=tile_kib)
+    else:
+        cfg = dict(max_fused_size=max_fused_size or 4, split=0,
+                   ctas_per_sm=0, tile_kib=0)
+    if split >= 0:
+        cfg["split"] = split
+    runners = make_runners(cfg["max_fused_size"])
     setup_s = time.perf_counter() - t0
     items = [(i, r) for i in range(len(runners)) for r in range(TRAJ["reps"])]
-    kw = dict(num_streams=num_streams, big_qubits=big_qubits,
-              big_streams=big_streams)
-    if warm:
-        E.run_trajectory_batch(runners, [(i, 10**6) for i in range(len(runners))],
-                               **kw)
-    per, lat, wall, launches = E.run_trajectory_batch(
-        runners, items, return_launches=True, **kw)
+    AT.run(runners, [(i, 10**6) for i in range(len(runners))], cfg, num_streams)
+    per, lat, wall, launches, info = AT.run(runners, items, cfg, num_streams)
     amp_ops = sum(float(2 ** int(ns[i])) * runners[i].info()["num_fused_ops"]
                   for i, _ in items)
     escapes = 0
@@ -491,20 +528,26 @@ def bench_trajectories(num_streams: int, max_fused_size: int = 4,
     per_n = {}
     for (i, _), t in zip(items, lat):
         per_n.setdefault(int(ns[i]), []).append(float(t))
-    return {
+    out = {
         "value": len(items) / wall, "unit": "traj/s",
         "wall_s": wall, "trajectories": len(items),
         "latency_ms_p50": float(np.percentile(lat, 50)),
         "latency_ms_p99": float(np.percentile(lat, 99)),
-        "streams": num_streams, "big_qubits": big_qubits,
-        "big_streams": big_streams, "max_fused_size": max_fused_size,
+        "config": cfg, "streams": num_streams,
         "setup_s": setup_s, "gpu_launches": launches,
         "fused_pass_bytes_per_s": 16.0 * amp_ops / wall,
         "non_default_kraus_choices": escapes,
         "latency_ms_mean_by_n": {str(k): float(np.mean(v))
                                  for k, v in sorted(per_n.items())},
         "workload": TRAJ_WORKLOAD,
+        "mode": mode,
+        "packed": info,
     }
+    if tune is not None:
+        out["autotune"] = {"tune_s": tune["tune_s"],
+                           "table": [dict(c, traj_s=round(v, 1))
+                                     for c, v in tune["table"]]}
+    return out
 
 
 def kernel_case(spec: str, n: int, reps: int):
@@ -593,17 +636,23 @@ def main():
     ap.add_argument("--traj-only", action="store_true",
                     help="run only the batched-trajectory workload")
     ap.add_argument("--traj-streams", type=int, default=8)
-    ap.add_argument("--traj-f", type=int, default=4)
-    ap.add_argument("--traj-big-qubits", type=int, default=0)
-    ap.add_argument("--traj-big-streams", type=int, default=1)
+    ap.add_argument("--traj-f", type=int, default=0,
+                    help="fusion size (0: autotuned among 3, 4)")
+    ap.add_argument("--traj-mode", default="auto",
+                    choices=["auto", "packed", "streams"])
+    ap.add_argument("--traj-split", type=int, default=-1,
+                    help="largest qubit count run in the packed kernel")
+    ap.add_argument("--traj-ctas-per-sm", type=int, default=0)
+    ap.add_argument("--traj-tile-kib", type=int, default=0)
     args = ap.parse_args()
     if args.kernel_case:
         kernel_case(args.kernel_case, args.qubits, args.reps)
         return
     if args.traj_only:
         print(json.dumps({"trajectories": bench_trajectories(
-            args.traj_streams, args.traj_f, args.traj_big_qubits,
-            args.traj_big_streams)}), flush=True)
+            args.traj_streams, args.traj_f, mode=args.traj_mode,
+            ctas_per_sm=args.traj_ctas_per_sm, tile_kib=args.traj_tile_kib,
+            split=args.traj_split)}), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -411,6 +411,38 @@ int qsg_traj_run_batch(int device, qsg_traj* const* runners,
                        float* const* out_states, float* latency_ms,
                        double* wall_s, uint64_t* launches);
 
+/* RunBatch as one persistent kernel over a packed batch: every trajectory is
+ * compiled on the host cores into a short device program (Kraus choices the
+ * lower bounds decide are made there; the others are made on the device),
+ * the batch is uploaded once and a single launch runs it, each CTA taking
+ * whole trajectories, largest circuits first.  Replaces the reference's
+ * serial loop over repetitions (lib/qtrajectory.h:141-236).  Items whose
+ * circuit has measurements, fused blocks of more than 4 targets, or more
+ * than max_qubits qubits run on the stream path of qsg_traj_run_batch
+ * afterwards.  Arguments as qsg_traj_run_batch; latency_ms is the item's
+ * device time inside the kernel; `info` (may be NULL) receives counts and
+ * timings. */
+typedef struct qsg_packed_options {
+  unsigned ctas_per_sm;   /* 0: 4 (fewer if the state slots do not fit)   */
+  unsigned max_qubits;    /* 0: 30                                         */
+  unsigned host_threads;  /* threads compiling programs, 0: all cores     */
+  unsigned tile_kib;      /* tile buffers per CTA: 32, 64 or 96 (0: 32)    */
+  int overlap;            /* nonzero: stream path runs while the kernel runs */
+  qsg_batch_options streams;  /* stream path for the other items          */
+} qsg_packed_options;
+typedef struct qsg_packed_info {
+  uint64_t packed_items, stream_items, ops;
+  unsigned ctas, tile_kib;
+  double build_s, upload_s, kernel_s, stream_s;
+} qsg_packed_info;
+int qsg_traj_run_packed(int device, qsg_traj* const* runners,
+                        uint64_t num_runners, const uint32_t* item_runner,
+                        const uint64_t* item_rep, uint64_t num_items,
+                        const qsg_packed_options* opts, uint64_t* stats,
+                        float* const* out_states, float* latency_ms,
+                        double* wall_s, uint64_t* launches,
+                        qsg_packed_info* info);
+
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,
  * qsg_timer_stop records a second one, synchronises and returns the elapsed

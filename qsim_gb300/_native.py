@@ -121,6 +121,9 @@ SIGNATURES = {
     "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                  vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                  P_u64]),
+    "qsg_traj_run_packed": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
+                                  vp, P_u64, C.POINTER(vp), P_f32, P_f64,
+                                  P_u64, vp]),
     "qsg_mlp_num_params": (u64, []),
     "qsg_mlp_create": (i32, [u64, C.POINTER(vp)]),
     "qsg_mlp_destroy": (i32, [vp]),
@@ -160,6 +163,21 @@ class BatchOptions(C.Structure):
     """qsg_batch_options."""
     _fields_ = [("num_streams", C.c_uint), ("big_qubits", C.c_uint),
                 ("big_streams", C.c_uint)]
+
+
+class PackedOptions(C.Structure):
+    """qsg_packed_options."""
+    _fields_ = [("ctas_per_sm", C.c_uint), ("max_qubits", C.c_uint),
+                ("host_threads", C.c_uint), ("tile_kib", C.c_uint),
+                ("overlap", C.c_int), ("streams", BatchOptions)]
+
+
+class PackedInfo(C.Structure):
+    """qsg_packed_info."""
+    _fields_ = [("packed_items", C.c_uint64), ("stream_items", C.c_uint64),
+                ("ops", C.c_uint64), ("ctas", C.c_uint), ("tile_kib", C.c_uint),
+                ("build_s", C.c_double), ("upload_s", C.c_double),
+                ("kernel_s", C.c_double), ("stream_s", C.c_double)]
 
 
 class QsgError(RuntimeError):

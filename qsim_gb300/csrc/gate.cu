@@ -14,9 +14,9 @@ namespace qsg {
 
 // Builds the tile geometry of a (controlled) gate.  `pair` selects pair mode
 // (qubit 0 is not a target).  Returns false on inconsistent input.
-static bool plan_tile(unsigned n, const unsigned* qs, unsigned k,
-                      const unsigned* cqs, unsigned c, uint64_t cvals,
-                      bool pair, int log_items, TileGeom& g) {
+bool plan_tile(unsigned n, const unsigned* qs, unsigned k,
+               const unsigned* cqs, unsigned c, uint64_t cvals, bool pair,
+               int log_items, TileGeom& g) {
   std::memset(&g, 0, sizeof(g));
   unsigned tb = std::min<unsigned>(n, log_items + k + (pair ? 1 : 0));
   unsigned h = 0, b = tb;

@@ -55,6 +55,13 @@ struct TileGeom {
   uint32_t n_sw;
 };
 
+// Host: builds the tile geometry of a (controlled) gate with 2^log_items
+// work items per tile; `pair` when qubit 0 is not a target.  False on
+// inconsistent input.  Defined in gate.cu.
+bool plan_tile(unsigned n, const unsigned* qs, unsigned k,
+               const unsigned* cqs, unsigned c, uint64_t cvals, bool pair,
+               int log_items, TileGeom& g);
+
 template <int K>
 struct GateArgs {
   TileGeom g;
@@ -167,6 +174,27 @@ struct MatAccess {
   }
 };
 
+// Matrix held in registers (k <= 2), loaded from memory once per gate.
+template <int K>
+struct RegMat {
+  static constexpr int D = 1 << K;
+  float2 m[D * D];
+  __device__ __forceinline__ explicit RegMat(const float* src) {
+#pragma unroll
+    for (int i = 0; i < D * D; ++i) m[i] = make_float2(src[2 * i], src[2 * i + 1]);
+  }
+  __device__ __forceinline__ float2 operator()(int row, int col) const {
+    return m[row * D + col];
+  }
+};
+
+// Placeholder accessor for gates whose matrix is read from shared memory.
+struct NoMat {
+  __device__ __forceinline__ float2 operator()(int, int) const {
+    return make_float2(0.f, 0.f);
+  }
+};
+
 __device__ __forceinline__ void cmac(float& ar, float& ai, float2 m, float vr,
                                      float vi) {
   ar = fmaf(m.x, vr, ar);
@@ -175,36 +203,24 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float2 m, float vr,
   ai = fmaf(m.y, vr, ai);
 }
 
-// MODE 0: apply, MODE 1: expectation value.
-template <int K, bool PAIR, int MODE>
-__global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
-    gate_tile_kernel(float4* __restrict__ st,
-                     const __grid_constant__ GateArgs<K> a,
-                     double2* __restrict__ partial) {
+// One CTA's share of a gate pass: tiles t0, t0 + step, ... of geometry g,
+// pipelined through STAGES shared-memory tile buffers (cp.async).  MODE 0
+// applies the matrix, MODE 1 accumulates <s|M|s> into (er, ei).  SMAT: the
+// matrix is read column-major from `smat` (2^k x 2^k float2, staged by the
+// caller); otherwise from the accessor M.  Used by the tile kernel below
+// (grid-stride over tiles) and by the packed-batch kernel (one CTA walks all
+// tiles of a trajectory's gate).
+template <int K, bool PAIR, int MODE, bool SMAT, int STAGES, class MA>
+__device__ __forceinline__ void tile_pass(float4* __restrict__ st,
+                                          const TileGeom& g, const MA& M,
+                                          const float2* smat, float4* tile,
+                                          uint64_t t0, uint64_t step,
+                                          double& er, double& ei) {
   using SH = TileShape<K, PAIR>;
   constexpr int D = SH::D;
   constexpr int R = SH::R;
   constexpr int ITEMS = SH::ITEMS;
   constexpr int NACC = PAIR ? 4 : 2;
-
-  extern __shared__ float4 smem[];
-  const TileGeom& g = a.g;
-  float4* tile = smem;
-  float2* smat = reinterpret_cast<float2*>(smem + SH::STAGES * SH::UNITS);
-
-  if constexpr (SH::SMEM_MAT) {
-    // Column-major copy: smat[c * D + r] = M[r][c].
-    for (int i = threadIdx.x; i < D * D; i += kTileThreads) {
-      const int r = i / D, c = i % D;
-      if constexpr (K <= 5) {
-        smat[c * D + r] = make_float2(a.m[2 * i], a.m[2 * i + 1]);
-      } else {
-        smat[c * D + r] = a.mat[i];
-      }
-    }
-    __syncthreads();
-  }
-  MatAccess<K> M{a};
 
   const uint32_t tid = threadIdx.x;
   const int rb = SH::S == 1 ? 0 : int(tid / ITEMS);
@@ -215,17 +231,15 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
   const bool ok0 = (e & g.cmask_low) == g.cvals_low;
   const bool ok1 = ((e | 1u) & g.cmask_low) == g.cvals_low;
 
-  double er = 0, ei = 0;
+  // Pipeline: tiles t0 .. t0 + (STAGES-1) step are in flight on entry.
+  uint64_t t = t0;
+#pragma unroll
+  for (int q = 0; q < STAGES; ++q)
+    tile_load_async<SH::LPT>(st, tile + q * SH::UNITS, t + q * step, g);
 
-  // Two-stage pipeline: tiles t0 and t0 + grid are in flight on entry.
-  float4* buf[2] = {tile, tile + SH::UNITS};
-  uint64_t t = blockIdx.x;
-  tile_load_async<SH::LPT>(st, buf[0], t, g);
-  tile_load_async<SH::LPT>(st, buf[1], t + gridDim.x, g);
-
-  for (int stage = 0; t < g.num_tiles; t += gridDim.x, stage ^= 1) {
-    float4* cur = buf[stage];
-    cp_async_wait<1>();
+  for (int stage = 0; t < g.num_tiles; t += step) {
+    float4* cur = tile + stage * SH::UNITS;
+    cp_async_wait<STAGES - 1>();
     __syncthreads();
     const uint64_t base = expand_outer(t, g);
 
@@ -236,7 +250,7 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
       for (int j = 0; j < NACC; ++j) acc[r][j] = 0.f;
 
     if (active) {
-      if constexpr (SH::SMEM_MAT) {
+      if constexpr (SMAT) {
         // Rows rb*R .. rb*R+R-1 of column c are contiguous in smat.
         const float4* mbase = reinterpret_cast<const float4*>(smat + rb * R);
         if constexpr (PAIR) {
@@ -352,12 +366,40 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
         }
       }
     }
-    // Every thread is done reading `cur`: refill it with the tile two steps
-    // ahead.
+    // Every thread is done reading `cur`: refill it with the tile STAGES
+    // steps ahead.
     __syncthreads();
-    tile_load_async<SH::LPT>(st, cur, t + 2 * uint64_t(gridDim.x), g);
+    tile_load_async<SH::LPT>(st, cur, t + uint64_t(STAGES) * step, g);
+    stage = stage + 1 == STAGES ? 0 : stage + 1;
   }
   cp_async_wait<0>();
+}
+
+// MODE 0: apply, MODE 1: expectation value.
+template <int K, bool PAIR, int MODE>
+__global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
+    gate_tile_kernel(float4* __restrict__ st,
+                     const __grid_constant__ GateArgs<K> a,
+                     double2* __restrict__ partial) {
+  using SH = TileShape<K, PAIR>;
+  constexpr int D = SH::D;
+  extern __shared__ float4 smem[];
+  float2* smat = reinterpret_cast<float2*>(smem + SH::STAGES * SH::UNITS);
+  if constexpr (SH::SMEM_MAT) {
+    // Column-major copy: smat[c * D + r] = M[r][c].
+    for (int i = threadIdx.x; i < D * D; i += kTileThreads) {
+      const int r = i / D, c = i % D;
+      if constexpr (K <= 5) {
+        smat[c * D + r] = make_float2(a.m[2 * i], a.m[2 * i + 1]);
+      } else {
+        smat[c * D + r] = a.mat[i];
+      }
+    }
+    __syncthreads();
+  }
+  double er = 0, ei = 0;
+  tile_pass<K, PAIR, MODE, SH::SMEM_MAT, SH::STAGES>(
+      st, a.g, MatAccess<K>{a}, smat, smem, blockIdx.x, gridDim.x, er, ei);
 
   if constexpr (MODE == 1) {
     // Block reduction of (er, ei) in FP64, fixed order.

@@ -386,3 +386,38 @@ def run_trajectory_batch(runners, items, num_streams: int = 8, device: int = 0,
     if return_launches:
         return per, lat[:len(items)], wall.value, launches.value
     return per, lat[:len(items)], wall.value
+
+
+def run_trajectory_batch_packed(runners, items, ctas_per_sm: int = 0,
+                                max_qubits: int = 0, host_threads: int = 0,
+                                num_streams: int = 8, device: int = 0,
+                                out_states=None, tile_kib: int = 0,
+                                overlap: bool = False):
+    """RunBatch as one persistent kernel over a packed batch
+    (qsg_traj_run_packed).  Returns (per-item stats list, latency_ms array,
+    wall seconds, launches, info dict)."""
+    nr = len(runners)
+    rh = (C.c_void_p * max(1, nr))(*[r.h.value for r in runners])
+    ir = np.ascontiguousarray([i for i, _ in items], dtype=np.uint32)
+    rp = np.ascontiguousarray([r for _, r in items], dtype=np.uint64)
+    sizes = [runners[i].info()["num_ops"] for i, _ in items]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    stats = np.zeros(max(1, int(offs[-1])), dtype=np.uint64)
+    lat = np.zeros(max(1, len(items)), dtype=np.float32)
+    wall = C.c_double()
+    launches = C.c_uint64()
+    outs = None
+    if out_states is not None:
+        outs = (C.c_void_p * len(items))(*[s.get() if s is not None else None
+                                           for s in out_states])
+    o = N.PackedOptions(ctas_per_sm, max_qubits, host_threads, tile_kib,
+                        int(overlap), N.BatchOptions(num_streams, 0, 0))
+    info = N.PackedInfo()
+    check(N.lib.qsg_traj_run_packed(
+        device, rh, nr, ir.ctypes.data_as(N.P_u32), rp.ctypes.data_as(N.P_u64),
+        len(items), C.byref(o), stats.ctypes.data_as(N.P_u64), outs,
+        lat.ctypes.data_as(N.P_f32), C.byref(wall), C.byref(launches),
+        C.byref(info)))
+    per = [stats[offs[i]:offs[i + 1]] for i in range(len(items))]
+    inf = {f: getattr(info, f) for f, _ in N.PackedInfo._fields_}
+    return per, lat[:len(items)], wall.value, launches.value, inf

@@ -257,4 +257,54 @@ int qsg_traj_run_batch(int device, qsg_traj* const* runners,
   return rc;
 }
 
+int qsg_traj_run_packed(int device, qsg_traj* const* runners,
+                        uint64_t num_runners, const uint32_t* item_runner,
+                        const uint64_t* item_rep, uint64_t num_items,
+                        const qsg_packed_options* opts, uint64_t* stats,
+                        float* const* out_states, float* latency_ms,
+                        double* wall_s, uint64_t* launches,
+                        qsg_packed_info* info) {
+  if (!runners || (num_items && (!item_runner || !item_rep)))
+    return invalid("null argument");
+  std::vector<BatchItem> items(num_items);
+  uint64_t off = 0;
+  for (uint64_t i = 0; i < num_items; ++i) {
+    if (item_runner[i] >= num_runners || !runners[item_runner[i]])
+      return invalid("batch item refers to no runner");
+    const TrajectoryRunner* r = runners[item_runner[i]]->r.get();
+    items[i].runner = r;
+    items[i].rep = item_rep[i];
+    items[i].stats = stats ? stats + off : nullptr;
+    items[i].out_state = out_states ? out_states[i] : nullptr;
+    off += r->num_ops();
+  }
+  PackedOptions o;
+  if (opts) {
+    o.ctas_per_sm = opts->ctas_per_sm;
+    if (opts->max_qubits) o.max_qubits = opts->max_qubits;
+    o.host_threads = opts->host_threads;
+    o.tile_kib = opts->tile_kib;
+    o.overlap = opts->overlap != 0;
+    o.streams.num_streams = opts->streams.num_streams;
+    o.streams.big_qubits = opts->streams.big_qubits;
+    o.streams.big_streams = opts->streams.big_streams;
+  }
+  PackedStats ps;
+  int rc = run_trajectory_batch_packed(device, items, o, wall_s, launches, &ps);
+  if (latency_ms)
+    for (uint64_t i = 0; i < num_items; ++i) latency_ms[i] = items[i].latency_ms;
+  if (info) {
+    info->packed_items = ps.packed_items;
+    info->stream_items = ps.stream_items;
+    info->ops = ps.ops;
+    info->ctas = ps.ctas;
+    info->tile_kib = ps.tile_kib;
+    info->build_s = ps.build_s;
+    info->upload_s = ps.upload_s;
+    info->kernel_s = ps.kernel_s;
+    info->stream_s = ps.stream_s;
+  }
+  return rc;
+}
+
 }  // extern "C"

@@ -255,13 +255,33 @@ std::vector<float> to_f32(const Mat& m) {
 }  // namespace
 
 TrajectoryRunner::~TrajectoryRunner() {
-  if (dev_table_) {
+  if (dev_table_ || dev_mats_) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(dev_device_);
-    cudaFree(dev_table_);
+    if (dev_table_) cudaFree(dev_table_);
+    if (dev_mats_) cudaFree(dev_mats_);
     cudaSetDevice(cur);
   }
+}
+
+int TrajectoryRunner::upload_packed(qsg_ctx* ctx) const {
+  int rc = upload(ctx);
+  if (rc || dev_mats_) return rc;
+  std::vector<float> all;
+  for (const PlanOp& p : base_.ops) all.insert(all.end(), p.m32.begin(), p.m32.end());
+  if (all.empty()) all.push_back(0.f);
+  void* p = nullptr;
+  rc = dev_alloc(ctx, all.size() * sizeof(float), &p);
+  if (rc) return rc;
+  rc = dev_upload(ctx, p, all.data(), all.size() * sizeof(float));
+  if (rc) {
+    dev_free(ctx, p);
+    return rc;
+  }
+  dev_mats_ = static_cast<float*>(p);
+  dev_device_ = ctx_device(ctx);
+  return QSG_OK;
 }
 
 int TrajectoryRunner::create(const NoisyCircuit& nc,
@@ -350,6 +370,12 @@ int TrajectoryRunner::create(const NoisyCircuit& nc,
   fo.tensor_path = false;
   r->base_ = fuse(slots, fo);
   for (auto& p : r->base_.ops) std::sort(p.members.begin(), p.members.end());
+  size_t off = 0;
+  r->mat_off_.assign(r->base_.ops.size(), 0);
+  for (size_t i = 0; i < r->base_.ops.size(); ++i) {
+    r->mat_off_[i] = off;
+    off += r->base_.ops[i].m32.size();
+  }
   *out = std::move(r);
   return QSG_OK;
 }
@@ -467,13 +493,10 @@ int TrajWorkspace::resolve() {
   return QSG_OK;
 }
 
-int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
-                              uint64_t* stats) const {
-  qsg_ctx* ctx = ws.ctx;
-  const unsigned n = nc_.num_qubits;
+template <class Sink>
+int TrajectoryRunner::walk(uint64_t rep, uint64_t* stats, Sink& sink) const {
   const size_t nops = nc_.ops.size();
-  int rc = upload(ctx);
-  if (rc) return rc;
+  int rc = QSG_OK;
 
   // Draws and host-side choices (lib/qtrajectory.h:265-331).
   thread_local std::vector<double> rr;
@@ -535,27 +558,8 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
     }
   }
 
-  rc = qsg_set_state_zero(ctx, state, n);
+  rc = sink.set_zero();
   if (rc) return rc;
-
-  auto normalize = [&]() -> int {
-    unsigned np = 0;
-    int e = traj_channel_stats(ctx, state, n, 0, nullptr, ws.partial, &np);
-    if (e) return e;
-    e = traj_choose(ctx, ws.partial, np, nullptr, 0, 0, ws.dlog, ws.dmat);
-    if (e) return e;
-    return traj_apply(ctx, state, n, 0, nullptr, ws.dmat);
-  };
-  auto launch = [&](const std::vector<unsigned>& qs, const Op* ctl,
-                    const float* m32) -> int {
-    if (ctl) {
-      return apply_gate_ex(ctx, state, n, qs.data(), qs.size(),
-                           ctl->cqs.data(), ctl->cqs.size(), ctl->cvals, m32,
-                           nullptr);
-    }
-    return apply_gate_ex(ctx, state, n, qs.data(), qs.size(), nullptr, 0, 0,
-                         m32, nullptr);
-  };
 
   // Channel kops are fused slots of `base_`; a kop choice other than the
   // first, or a cut, makes the block's matrix be recomputed.
@@ -563,18 +567,19 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
   thread_local std::vector<unsigned> qs;
   const unsigned nseg = unsigned(escapes.size()) + 1;
   for (unsigned s = 0; s < nseg; ++s) {
-    for (const PlanOp& p : base_.ops) {
+    for (size_t pi = 0; pi < base_.ops.size(); ++pi) {
+      const PlanOp& p = base_.ops[pi];
       if (p.kind == OpKind::kMeasure) {
         const int m = p.members[0];
         if (seg[m] != s) continue;
         if (norm_before[m]) {
-          rc = normalize();
+          rc = sink.normalize();
           if (rc) return rc;
         }
         uint64_t mask = 0;
         for (unsigned q : nc_.ops[m].op.qs) mask |= uint64_t{1} << q;
         uint64_t bits = 0;
-        rc = qsg_measure(ctx, state, n, mask, rr[m], 1, &bits);
+        rc = sink.measure(mask, rr[m], &bits);
         if (rc) return rc;
         if (stats) stats[m] = opt_.collect_mea_stat ? bits : kNoStat;
         continue;
@@ -601,12 +606,13 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
       }
       if (present == 0) continue;
       if (p.kind == OpKind::kControlled) {
-        rc = launch(p.qs, &nc_.ops[p.members[0]].op, p.m32.data());
+        rc = sink.gate(p.qs, &nc_.ops[p.members[0]].op, p.m32.data(),
+                       ptrdiff_t(pi));
         if (rc) return rc;
         continue;
       }
       if (present == p.members.size() && all_default) {
-        rc = launch(p.qs, nullptr, p.m32.data());
+        rc = sink.gate(p.qs, nullptr, p.m32.data(), ptrdiff_t(pi));
         if (rc) return rc;
         continue;
       }
@@ -616,7 +622,7 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
       std::sort(qs.begin(), qs.end());
       qs.erase(std::unique(qs.begin(), qs.end()), qs.end());
       std::vector<float> m32 = to_f32(block_matrix_ops(ptrs, qs));
-      rc = launch(qs, nullptr, m32.data());
+      rc = sink.gate(qs, nullptr, m32.data(), -1);
       if (rc) return rc;
     }
     if (s + 1 < nseg) {
@@ -624,25 +630,165 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
       // (lib/qtrajectory.h:331-380).
       const size_t e = escapes[s];
       const Channel& ch = chans_[chan_of_op_[e]];
-      if (ws.log_off >= ws.log_cap) {
-        rc = ws.resolve();
-        if (rc) return rc;
-      }
-      const size_t slot = ws.log_off++;
-      unsigned np = 0;
-      rc = traj_channel_stats(ctx, state, n, ch.qs.size(), ch.qs.data(),
-                              ws.partial, &np);
+      rc = sink.channel(ch.qs, dev_table_ + ch.dev, ch.cp_total, rr[e],
+                        opt_.collect_kop_stat ? stats : nullptr, e);
       if (rc) return rc;
-      rc = traj_choose(ctx, ws.partial, np, dev_table_ + ch.dev, ch.cp_total,
-                       rr[e], ws.dlog + slot, ws.dmat);
-      if (rc) return rc;
-      rc = traj_apply(ctx, state, n, ch.qs.size(), ch.qs.data(), ws.dmat);
-      if (rc) return rc;
-      ws.pending.push_back({opt_.collect_kop_stat ? stats : nullptr, e, slot});
     }
   }
-  if (!unitary) return normalize();
+  if (!unitary) return sink.normalize();
   return QSG_OK;
+}
+
+namespace {
+
+// Launches every op on the workspace's stream (RunOnce on the engine).
+struct StreamSink {
+  TrajWorkspace& ws;
+  float* state;
+  unsigned n;
+
+  int set_zero() { return qsg_set_state_zero(ws.ctx, state, n); }
+  int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
+           ptrdiff_t) {
+    if (ctl)
+      return apply_gate_ex(ws.ctx, state, n, qs.data(), qs.size(),
+                           ctl->cqs.data(), ctl->cqs.size(), ctl->cvals, m32,
+                           nullptr);
+    return apply_gate_ex(ws.ctx, state, n, qs.data(), qs.size(), nullptr, 0,
+                         0, m32, nullptr);
+  }
+  int measure(uint64_t mask, double u, uint64_t* bits) {
+    return qsg_measure(ws.ctx, state, n, mask, u, 1, bits);
+  }
+  int normalize() {
+    unsigned np = 0;
+    int e = traj_channel_stats(ws.ctx, state, n, 0, nullptr, ws.partial, &np);
+    if (e) return e;
+    e = traj_choose(ws.ctx, ws.partial, np, nullptr, 0, 0, ws.dlog, ws.dmat);
+    if (e) return e;
+    return traj_apply(ws.ctx, state, n, 0, nullptr, ws.dmat);
+  }
+  int channel(const std::vector<unsigned>& qs, const TrajChannelDev* dev,
+              double cp0, double r, uint64_t* stats, size_t op) {
+    if (ws.log_off >= ws.log_cap) {
+      const int e = ws.resolve();
+      if (e) return e;
+    }
+    const size_t slot = ws.log_off++;
+    unsigned np = 0;
+    int e = traj_channel_stats(ws.ctx, state, n, qs.size(), qs.data(),
+                               ws.partial, &np);
+    if (e) return e;
+    e = traj_choose(ws.ctx, ws.partial, np, dev, cp0, r, ws.dlog + slot,
+                    ws.dmat);
+    if (e) return e;
+    e = traj_apply(ws.ctx, state, n, qs.size(), qs.data(), ws.dmat);
+    if (e) return e;
+    ws.pending.push_back({stats, op, slot});
+    return QSG_OK;
+  }
+};
+
+uint64_t mask_of(const std::vector<unsigned>& qs) {
+  uint64_t m = 0;
+  for (unsigned q : qs) m |= uint64_t{1} << q;
+  return m;
+}
+
+// Appends packed-batch ops (batch_dev.h) instead of launching.
+struct ProgramSink {
+  std::vector<BatchOp>* ops;
+  std::vector<float>* extra;
+  std::vector<std::pair<size_t, size_t>>* extra_refs;
+  std::vector<TrajectoryRunner::LogRef>* log_refs;
+  const float* dev_mats;
+  const std::vector<size_t>* mat_off;
+
+  int set_zero() {
+    BatchOp o{};
+    o.kind = kBatchSetZero;
+    ops->push_back(o);
+    return QSG_OK;
+  }
+  int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
+           ptrdiff_t base) {
+    if (qs.empty() || qs.size() > kBatchMaxK ||
+        (ctl && ctl->cqs.size() > kBatchMaxControls))
+      return unsupported("packed batch: block too large");
+    BatchOp o{};
+    o.kind = kBatchGate;
+    o.tmask = mask_of(qs);
+    if (ctl) {
+      o.cmask = mask_of(ctl->cqs);
+      for (size_t i = 0; i < ctl->cqs.size(); ++i)
+        if ((ctl->cvals >> i) & 1) o.cvals |= uint64_t{1} << ctl->cqs[i];
+    }
+    if (base >= 0) {
+      o.mat = dev_mats + (*mat_off)[size_t(base)];
+    } else {
+      extra_refs->push_back({ops->size(), extra->size()});
+      const size_t nf = size_t(2) << (2 * qs.size());
+      extra->insert(extra->end(), m32, m32 + nf);
+    }
+    ops->push_back(o);
+    return QSG_OK;
+  }
+  int measure(uint64_t, double, uint64_t*) {
+    return unsupported("packed batch: measurements run on streams");
+  }
+  int normalize() {
+    BatchOp o{};
+    o.kind = kBatchNormalize;
+    ops->push_back(o);
+    return QSG_OK;
+  }
+  int channel(const std::vector<unsigned>& qs, const TrajChannelDev* dev,
+              double cp0, double r, uint64_t* stats, size_t op) {
+    if (qs.size() > kTrajMaxChannelQubits)
+      return unsupported("packed batch: channel on too many qubits");
+    BatchOp o{};
+    o.kind = kBatchChannel;
+    o.tmask = mask_of(qs);
+    o.ch = dev;
+    o.cp0 = cp0;
+    o.r = r;
+    ops->push_back(o);
+    log_refs->push_back({stats, op});
+    return QSG_OK;
+  }
+};
+
+}  // namespace
+
+int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
+                              uint64_t* stats) const {
+  const int rc = upload(ws.ctx);
+  if (rc) return rc;
+  StreamSink sink{ws, state, nc_.num_qubits};
+  return walk(rep, stats, sink);
+}
+
+bool TrajectoryRunner::packable() const {
+  for (const PlanOp& p : base_.ops) {
+    if (p.kind == OpKind::kMeasure) return false;
+    if (p.qs.size() > kBatchMaxK) return false;
+    if (p.kind == OpKind::kControlled && p.cqs.size() > kBatchMaxControls)
+      return false;
+  }
+  // A recomputed block holds the members of a fused block, so it has no
+  // more targets than the block.
+  return true;
+}
+
+int TrajectoryRunner::build_program(
+    uint64_t rep, uint64_t* stats, std::vector<BatchOp>* ops,
+    std::vector<float>* extra,
+    std::vector<std::pair<size_t, size_t>>* extra_refs,
+    std::vector<LogRef>* log_refs) const {
+  if (!dev_mats_ && !base_.ops.empty())
+    return invalid("packed batch: runner matrices not uploaded");
+  ProgramSink sink{ops, extra, extra_refs, log_refs, dev_mats_, &mat_off_};
+  return walk(rep, stats, sink);
 }
 
 // ---------------------------------------------------------------------------

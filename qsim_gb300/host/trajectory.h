@@ -23,6 +23,7 @@
 #include <memory>
 #include <vector>
 
+#include "batch_dev.h"
 #include "engine.h"
 
 namespace qsg {
@@ -141,8 +142,32 @@ class TrajectoryRunner {
   // use for the given context's device).
   int upload(qsg_ctx* ctx) const;
 
+  // True when every trajectory of this runner can run inside the packed
+  // batch kernel: no measurements, fused blocks of at most kBatchMaxK
+  // targets, at most kBatchMaxControls controls.
+  bool packable() const;
+  // upload() plus the fused plan's matrices, which packed programs point to.
+  int upload_packed(qsg_ctx* ctx) const;
+
+  // Compiles trajectory `rep` into packed-batch ops (see batch_dev.h):
+  // appends to `ops`; matrices of blocks that differ from the fused plan go
+  // to `extra` (float offsets are kept in `extra_refs` as (op index, offset)
+  // pairs for the caller to turn into device pointers); CHANNEL ops get log
+  // slots log_base, log_base + 1, ... and (stats, op) pairs in `log_refs`.
+  // Requires upload() for the device first.
+  struct LogRef {
+    uint64_t* stats;
+    size_t op;
+  };
+  int build_program(uint64_t rep, uint64_t* stats, std::vector<BatchOp>* ops,
+                    std::vector<float>* extra,
+                    std::vector<std::pair<size_t, size_t>>* extra_refs,
+                    std::vector<LogRef>* log_refs) const;
+
  private:
   TrajectoryRunner() = default;
+  template <class Sink>
+  int walk(uint64_t rep, uint64_t* stats, Sink& sink) const;
   struct Channel;
   NoisyCircuit nc_;
   TrajectoryOptions opt_;
@@ -151,6 +176,8 @@ class TrajectoryRunner {
   std::vector<Channel> chans_;
   std::vector<std::vector<Op>> kop_ops_;  // per channel, per kop: one op
   mutable TrajChannelDev* dev_table_ = nullptr;
+  mutable float* dev_mats_ = nullptr;     // fused plan's matrices
+  std::vector<size_t> mat_off_;           // per plan op: float offset
   mutable int dev_device_ = -1;
   size_t num_dev_channels_ = 0;
 };
@@ -179,6 +206,31 @@ struct BatchOptions {
 int run_trajectory_batch(int device, std::vector<BatchItem>& items,
                          const BatchOptions& opt, double* wall_s,
                          uint64_t* launches);
+
+struct PackedOptions {
+  unsigned ctas_per_sm = 0;   // persistent CTAs per SM (0: 4, or fewer if
+                              // the slot buffers do not fit)
+  unsigned max_qubits = 30;   // larger circuits run on the stream path
+  unsigned host_threads = 0;  // threads compiling programs (0: all cores)
+  unsigned tile_kib = 0;      // tile buffers per CTA: 32, 64, 96 (0: 32)
+  bool overlap = false;       // run the stream path while the kernel runs
+  BatchOptions streams;       // the stream path for the other items
+};
+
+struct PackedStats {
+  uint64_t packed_items = 0, stream_items = 0, ops = 0;
+  unsigned ctas = 0, tile_kib = 0;
+  double build_s = 0, upload_s = 0, kernel_s = 0, stream_s = 0;
+};
+
+// Runs the items that fit the packed kernel (packable runners of at most
+// max_qubits qubits) as one persistent launch over a packed batch, largest
+// circuits first, and the others on the stream path, after the launch or,
+// with opt.overlap, concurrently with it.  Per-item latency is
+// the item's device time inside the persistent kernel (%globaltimer).
+int run_trajectory_batch_packed(int device, std::vector<BatchItem>& items,
+                                const PackedOptions& opt, double* wall_s,
+                                uint64_t* launches, PackedStats* stats);
 
 }  // namespace host
 }  // namespace qsg

@@ -1,0 +1,34 @@
+"""Host-side logic of the trajectory autotuner (no GPU): the candidate set,
+workload signatures and the result cache."""
+import json
+
+from qsim_gb300 import autotune as AT
+
+
+def test_candidates_cover_every_mode():
+    c = AT.candidates(24, fs=(3, 4))
+    assert {x["max_fused_size"] for x in c} == {3, 4}
+    assert any(x["split"] == 0 for x in c)          # stream path only
+    assert any(x["split"] == 24 for x in c)         # all in the packed kernel
+    assert any(0 < x["split"] < 24 for x in c)      # split, both at once
+    for x in c:
+        if x["split"]:
+            assert x["ctas_per_sm"] >= 1 and x["tile_kib"] in (32, 64, 96)
+    # Splits at or above the largest circuit collapse into "all packed".
+    assert all(x["split"] in (0, 14) for x in AT.candidates(14))
+
+
+def test_signature_depends_on_workload_only():
+    a = AT.signature([12, 13, 24], 32, "noise")
+    assert a == AT.signature([24, 12, 13], 32, "noise")
+    assert a != AT.signature([12, 13, 24], 16, "noise")
+    assert a != AT.signature([12, 13, 24], 32, "other")
+
+
+def test_cache_round_trip(tmp_path, monkeypatch):
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("QSG_AUTOTUNE_CACHE", str(path))
+    assert AT._load() == {}
+    AT._store({"k": {"best": {"split": 0}, "table": []}})
+    assert json.loads(path.read_text())["k"]["best"] == {"split": 0}
+    assert AT._load()["k"]["table"] == []
