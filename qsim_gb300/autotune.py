@@ -120,7 +120,7 @@ def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
     make_runners(f) returns the runners (one per circuit, in the order of
     `qubits`) fused at max_fused_size f; the batch is every circuit times
     `reps` repetitions.  Candidates are timed on `sample_reps` repetitions
-    per circuit (default reps / 4, at least 1), after one warm-up run each.
+    per circuit (default reps / 8, at least 1), after one warm-up run each.
     Returns {"best": cfg, "table": [(cfg, traj/s), ...], "cached": bool,
     "tune_s": seconds}."""
     key = _device_key(device) + "/" + signature(qubits, reps, tag)

@@ -11,24 +11,29 @@
 //     [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im), and `in` the
 //     tile's 64 groups x 128 real components.  One CTA tile = 64 groups x 64
 //     members = 4096 amplitudes (32 KiB).
-//   * Split TF32: A = A_hi + A_lo and B = B_hi + B_lo with every part
-//     pre-rounded to TF32; D = A_hi B_hi + A_hi B_lo + A_lo B_hi (3 x 16
-//     MMAs of M=128, N=64, K=8), FP32 accumulation.  The dropped A_lo B_lo
-//     term and the rounding of the lo parts leave ~2^-21 relative error per
-//     product, the FP32 level of the CUDA-core path.
-//   * Tensor memory holds the gate (A_hi, A_lo: 2 x 128 columns, loaded once
-//     per CTA) and two 64-column accumulators, so the MMAs of tile i run
-//     while the epilogue of tile i-1 drains the other accumulator.
+//   * Split FP16 with a power-of-two scale: the tile is multiplied by
+//     sigma = 2^(floor(n/2) - 4), which brings the amplitudes of a state of
+//     norm <= 1 (|psi_i| <= 1, typically 2^(-n/2)) into the normal FP16
+//     range with room for |psi_i| <= 32; then A = A_hi + A_lo and
+//     B = B_hi + B_lo with every part an FP16 number, and
+//     D = A_hi B_hi + A_hi B_lo + A_lo B_hi (3 x 8 MMAs of M=128, N=64,
+//     K=16), FP32 accumulation, D / sigma in the epilogue.  FP16 keeps the
+//     11-bit significand of TF32 and runs at twice its tensor rate; the
+//     dropped A_lo B_lo term and the rounding of the lo parts leave ~2^-21
+//     relative error per product, the FP32 level of the CUDA-core path.
+//   * Tensor memory holds the gate (A_hi, A_lo: 2 x 64 columns of FP16
+//     pairs, loaded once per CTA) and four 64-column accumulators, so the
+//     MMAs of tile i run while the epilogue drains tiles i-1..i-3.
 //   * Shared memory: three raw tile buffers fed by 16-byte cp.async in tile
-//     order (three tiles in flight per SM), and two operand buffers (hi, lo)
-//     in the canonical no-swizzle K-major layout (8-row x 16-byte core
-//     matrices; LBO = 128 B along K, SBO = 4 KiB between 8-row blocks),
-//     written by a split pass with conflict-free 128-bit stores.
+//     order, and four operand buffers (B_hi, B_lo: 16 KiB each) in the
+//     canonical no-swizzle K-major layout (8-row x 16-byte core matrices;
+//     LBO = 128 B along K, SBO = 2 KiB between 8-row blocks), written by a
+//     split pass with conflict-free 128-bit stores.
 //   * One thread issues the MMAs and commits them to an mbarrier; every wait
 //     is bounded by a clock budget and sets an error flag instead of hanging.
 //     The epilogue reads D with tcgen05.ld, pairs re/im lanes with a shuffle,
-//     stages the tile in shared memory and stores it with coalesced 128-bit
-//     writes.
+//     stages the tile in its own operand buffer and stores it with coalesced
+//     128-bit writes.
 //
 // All tile addressing is bitwise linear: a tile index e (12 bits) maps each
 // of its bits to one state bit, one group bit or one member bit, so every
@@ -38,6 +43,8 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "common.cuh"
 #include "internal.h"
@@ -60,42 +67,39 @@ constexpr int kReal = 2 * kD;          // real dimension (128) = M = K
 constexpr int kGroups = 64;            // N
 constexpr int kTileBits = 12;          // 64 groups x 64 members
 constexpr int kTileAmps = 1 << kTileBits;
-constexpr uint32_t kARowFloats = kReal;                  // A row length
-constexpr uint32_t kOperandFloats = 2 * kReal * kReal;   // A_hi | A_lo
+constexpr uint32_t kAWords = kReal / 2;                 // FP16 pairs per A row
+constexpr uint32_t kOperandBytes = 2 * kReal * kAWords * 4;  // A_hi | A_lo
 constexpr uint32_t kTileBytes = kTileAmps * 8;           // 32 KiB
 constexpr uint32_t kLBO = 128;                           // K-adjacent cores
-constexpr uint32_t kSBOB = (kReal / 4) * 128;            // 4 KiB
+constexpr uint32_t kSBOB = (kReal / 8) * 128;            // 2 KiB
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kTmemAhi = 0, kTmemAlo = 128, kTmemD = 256;  // columns
+constexpr uint32_t kTmemAhi = 0, kTmemAlo = 64, kTmemD = 128;  // columns
 constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
 constexpr int kRawStages = 3;
+constexpr int kNB = 4;                 // operand buffers = accumulators
 constexpr int kUnitsPerRole = kTileAmps / 2 / kProdThreads;  // 8 (= epilogue)
+constexpr int kSplitPerRole = kTileAmps / 4 / kProdThreads;  // 4 quads
 
 // Shared-memory map (bytes).
 constexpr uint32_t kOffRaw = 0;                                  // 3 x 32 KiB
-constexpr uint32_t kOffOp = kOffRaw + kRawStages * kTileBytes;    // 2 x 64 KiB
-constexpr uint32_t kOpBytes = 2 * kTileBytes;                     // hi | lo
+constexpr uint32_t kOffOp = kOffRaw + kRawStages * kTileBytes;    // 4 x 32 KiB
+constexpr uint32_t kBImgBytes = kGroups * kReal * 2;              // 16 KiB
+constexpr uint32_t kOpBytes = 2 * kBImgBytes;                     // hi | lo
 // The epilogue stages its output tile in the operand buffer of that tile
 // (its MMAs have completed when the accumulator is full).
-constexpr uint32_t kOffTabG = kOffOp + 2 * kOpBytes;    // 8 x u64 unit goff
-constexpr uint32_t kOffTabSplitE = kOffTabG + 64;       // 8 x u32 raw index
-constexpr uint32_t kOffTabSplitO = kOffTabSplitE + 32;  // 8 x u32 op offset
-constexpr uint32_t kOffTabGrpE = kOffTabSplitO + 32;    // 64 x u32 group e
+constexpr uint32_t kOffTabG = kOffOp + kNB * kOpBytes;  // 8 x u64 unit goff
+constexpr uint32_t kOffTabSplitE = kOffTabG + 64;       // 4 x u32 raw index
+constexpr uint32_t kOffTabSplitO = kOffTabSplitE + 16;  // 4 x u32 op offset
+constexpr uint32_t kOffTabGrpE = kOffTabSplitO + 16;    // 64 x u32 group e
 constexpr uint32_t kOffTabRd = kOffTabGrpE + 256;       // 8 x u32 stage read
 constexpr uint32_t kOffTabWr = kOffTabRd + 32;          // 8 x u32 raw write
-constexpr uint32_t kOffBar = kOffTabWr + 32;            // 9 mbarriers
-constexpr uint32_t kOffFlag = kOffBar + 80;             // failure flag
+constexpr uint32_t kNumBars = 4 * kNB + 1;
+constexpr uint32_t kOffBar = kOffTabWr + 32;            // mbarriers
+constexpr uint32_t kOffFlag = kOffBar + 8 * kNumBars;   // failure flag
 constexpr uint32_t kOffTmem = kOffFlag + 16;
 constexpr uint32_t kSmemBytes = kOffTmem + 16;
 
 static_assert(kSmemBytes <= 232448, "shared memory budget");
-
-// Byte offset of real element (row, k) in a K-major no-swizzle operand with
-// rows of `kReal` K-elements.
-__host__ __device__ constexpr uint32_t kmajor_off(uint32_t row, uint32_t k,
-                                                  uint32_t sbo) {
-  return (row / 8) * sbo + (k / 4) * kLBO + (row % 8) * 16 + (k % 4) * 4;
-}
 
 // Tile geometry of a 6-target gate on n >= 12 qubits.
 struct TcGeom {
@@ -110,16 +114,21 @@ struct TcGeom {
   // XOR swizzles of tile indices, X(e) = OR_i bit(e, src[i]) << dst[i] with
   // src >= 4 and dst < 4, so that the accesses of a half-warp fall on
   // distinct banks.  `out`: epilogue staging (8-byte writes by member x
-  // group-bit-3 lanes, 16-byte linear reads).  `raw`: raw tile buffer
-  // (16-byte cp.async writes, 8-byte split reads); it never touches bit 0.
+  // group-bit-4 lanes, 16-byte linear reads).  `raw`: raw tile buffer
+  // (16-byte cp.async writes, 8-byte split reads by group-bits-0..2 x
+  // member-bit-2 lanes); it never touches bit 0.
   uint32_t out_src[4], out_dst[4], out_n;
   uint32_t raw_src[4], raw_dst[4], raw_n;
 };
 
 struct TcArgs {
   TcGeom g;
-  const float* operands;  // A_hi | A_lo, row-major 128 x 128 each
-  int* error;             // set on a timed-out wait
+  // A_hi | A_lo: 128 rows x 64 words each, a word holding the FP16 values of
+  // columns 2w (low half) and 2w + 1 (high half).
+  const uint32_t* operands;
+  float scale;      // sigma: tile values are split as FP16 after * sigma
+  float inv_scale;  // 1 / sigma, applied to D (both powers of two)
+  int* error;       // set on a timed-out wait
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -137,10 +146,10 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo,
   return d;
 }
 
-// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = 64,
-// M = 128 (A is read from tensor memory).
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) |
-                            (uint32_t(kGroups >> 3) << 17) |
+// Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B =
+// F16 (bits 7-9, 10-12 = 0), both K-major, N = 64 (bits 17-22 = N / 8),
+// M = 128 (bits 24-28 = M / 16); A is read from tensor memory.
+constexpr uint32_t kIdesc = (1u << 4) | (uint32_t(kGroups >> 3) << 17) |
                             (uint32_t(kReal >> 4) << 24);
 
 __device__ __forceinline__ void cp_async8(uint32_t saddr, const void* g) {
@@ -161,12 +170,11 @@ __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ float tf32_round(float x) {
-  // Round to nearest (ties away) at mantissa bit 13: the result is exactly
-  // representable in TF32, so the MMA reads it unchanged.
-  uint32_t u = __float_as_uint(x);
-  u = (u + 0x1000u) & 0xFFFFE000u;
-  return __uint_as_float(u);
+// FP16 pair (lo = first value in the low half) of two floats, round to
+// nearest.
+__device__ __forceinline__ uint32_t pack_half2(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -188,11 +196,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // D[tmem] (+)= A[tmem] * B[smem descriptor].
-__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem,
-                                            uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem,
+                                           uint64_t b, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(
           d_tmem),
       "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate)
       : "memory");
@@ -287,18 +295,18 @@ __device__ __forceinline__ uint32_t tile_e(uint32_t n, uint32_t m,
   return e;
 }
 
-// Split-pass work item idx (11 bits) = (n bits 0-2 | pair p << 3 |
-// n bits 3-5 << 8): the 16-byte operand row chunk of group n, members 2p
-// and 2p+1.  Lanes 0..7 of a warp cover the 8 rows of one core matrix, so
-// the 128-bit operand stores are conflict free.
+// Split-pass work item idx (10 bits) = (n bits 0-2 | quad q << 3 |
+// n bits 3-5 << 7): the 16-byte operand row chunk (8 FP16 K-elements) of
+// group n, members 4q .. 4q+3.  Lanes 0..7 of a warp cover the 8 rows of one
+// core matrix, so the 128-bit operand stores are conflict free.
 __device__ __forceinline__ uint32_t split_n(uint32_t idx) {
-  return (idx & 7) | ((idx >> 8) << 3);
+  return (idx & 7) | ((idx >> 7) << 3);
 }
-__device__ __forceinline__ uint32_t split_p(uint32_t idx) {
-  return (idx >> 3) & 31;
+__device__ __forceinline__ uint32_t split_q(uint32_t idx) {
+  return (idx >> 3) & 15;
 }
-__host__ __device__ __forceinline__ uint32_t op_off(uint32_t n, uint32_t p) {
-  return (n / 8) * kSBOB + p * kLBO + (n % 8) * 16;
+__host__ __device__ __forceinline__ uint32_t op_off(uint32_t n, uint32_t q) {
+  return (n / 8) * kSBOB + q * kLBO + (n % 8) * 16;
 }
 
 __device__ __forceinline__ uint32_t swz_x(uint32_t e, const uint32_t* src,
@@ -378,11 +386,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint32_t* tab_rd = reinterpret_cast<uint32_t*>(smem + kOffTabRd);
   uint32_t* tab_wr = reinterpret_cast<uint32_t*>(smem + kOffTabWr);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kOffBar);
-  uint64_t* op_full = bars + 0;   // [2] producers -> MMA
-  uint64_t* op_free = bars + 2;   // [2] epilogue (staging read out) -> producers
-  uint64_t* acc_full = bars + 4;  // [2] MMA commit -> epilogue
-  uint64_t* acc_free = bars + 6;  // [2] epilogue -> MMA
-  uint64_t* gate_ready = bars + 8;  // epilogue (gate in TMEM) -> MMA
+  uint64_t* op_full = bars + 0;         // [kNB] producers -> MMA
+  uint64_t* op_free = bars + kNB;       // [kNB] epilogue (staging read) -> producers
+  uint64_t* acc_full = bars + 2 * kNB;  // [kNB] MMA commit -> epilogue
+  uint64_t* acc_free = bars + 3 * kNB;  // [kNB] epilogue -> MMA
+  uint64_t* gate_ready = bars + 4 * kNB;  // epilogue (gate in TMEM) -> MMA
   volatile int* flag = reinterpret_cast<volatile int*>(smem + kOffFlag);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kOffTmem);
   const uint32_t sbase = smem_u32(smem);
@@ -394,14 +402,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     tab_g[tid] = tile_goff(uint32_t(tid) << (kRoleBits + 1), g);
     tab_rd[tid] = swz_out(uint32_t(tid) << (kRoleBits + 1), g);
     tab_wr[tid] = swz_raw(uint32_t(tid) << (kRoleBits + 1), g);
-    // Split item idx = rtid + 256 j: j supplies idx bits 8..10 (n bits 3-5).
+  }
+  if (tid < kSplitPerRole) {
+    // Split item idx = rtid + 256 j: j supplies idx bits 8, 9 (n bits 4, 5).
     const uint32_t idx = tid << kRoleBits;
-    tab_se[tid] = swz_raw(tile_e(split_n(idx), 2 * split_p(idx), g), g);
-    tab_so[tid] = op_off(split_n(idx), split_p(idx));
+    tab_se[tid] = swz_raw(tile_e(split_n(idx), 4 * split_q(idx), g), g);
+    tab_so[tid] = op_off(split_n(idx), split_q(idx));
   }
   if (tid < kGroups) tab_ge[tid] = swz_out(tile_e(tid, 0, g), g);
   if (tid == 0) {
-    for (int i = 0; i < 9; ++i) mbar_init(&bars[i], 1);
+    for (uint32_t i = 0; i < kNumBars; ++i) mbar_init(&bars[i], 1);
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -428,12 +438,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t rt = tid;
     const uint64_t my_g = tile_goff(rt << 1, g);
     const uint32_t my_wr = swz_raw(rt << 1, g);
-    const uint32_t my_se = swz_raw(tile_e(split_n(rt), 2 * split_p(rt), g), g);
-    const uint32_t my_so = op_off(split_n(rt), split_p(rt));
-    uint32_t e_m1 = 0;
-    for (int j = 0; j < kTileBits; ++j)
+    const uint32_t my_se = swz_raw(tile_e(split_n(rt), 4 * split_q(rt), g), g);
+    const uint32_t my_so = op_off(split_n(rt), split_q(rt));
+    // Swizzled tile offsets of member bits 0 and 1 (members 4q + 1, + 2).
+    uint32_t e_m1 = 0, e_m2 = 0;
+    for (int j = 0; j < kTileBits; ++j) {
       if (g.tile_is_target[j] && g.target_slot[j] == 0) e_m1 = 1u << j;
+      if (g.tile_is_target[j] && g.target_slot[j] == 1) e_m2 = 1u << j;
+    }
     e_m1 = swz_raw(e_m1, g);
+    e_m2 = swz_raw(e_m2, g);
+    const float sc = a.scale;
     auto issue_loads = [&](uint64_t t, int stage) {
       if (t < g.num_tiles) {
         const float4* gp = reinterpret_cast<const float4*>(
@@ -449,29 +464,51 @@ __global__ void __launch_bounds__(kThreads, 1)
     int i = 0;
     for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
       const int rs = i % kRawStages;
-      const int s = i & 1;
+      const int s = i % kNB;
       cp_wait<kRawStages - 1>();
-      // Operand buffer s is free once the epilogue read tile i-2 out of it
-      // (the ((i-2)/2)-th completion of op_free[s]).
+      // Operand buffer s is free once the epilogue read tile i-kNB out of it
+      // (the ((i-kNB)/kNB)-th completion of op_free[s]).
       bool bad = false;
-      if (i >= 2) bad = !mbar_wait(&op_free[s], ((i - 2) >> 1) & 1, flag);
+      if (i >= kNB) bad = !mbar_wait(&op_free[s], ((i - kNB) / kNB) & 1, flag);
       if (bar_or(1, kProdThreads, bad)) break;
-      // Split the raw tile into hi / lo operand rows (K-major).
+      // Split the raw tile into FP16 hi / lo operand rows (K-major): four
+      // members (8 K-elements, one 16-byte core-matrix row) per item.
       const float2* raw = reinterpret_cast<const float2*>(smem + kOffRaw + rs * kTileBytes);
       const uint32_t obuf = kOffOp + s * kOpBytes;
 #pragma unroll
-      for (int j = 0; j < kUnitsPerRole; ++j) {
+      for (int j = 0; j < kSplitPerRole; ++j) {
         const uint32_t e0 = my_se ^ tab_se[j];
-        const float2 x0 = raw[e0];
-        const float2 x1 = raw[e0 ^ e_m1];
-        float4 h, l;
-        h.x = tf32_round(x0.x); l.x = tf32_round(x0.x - h.x);
-        h.y = tf32_round(x0.y); l.y = tf32_round(x0.y - h.y);
-        h.z = tf32_round(x1.x); l.z = tf32_round(x1.x - h.z);
-        h.w = tf32_round(x1.y); l.w = tf32_round(x1.y - h.w);
+        float x[8];
+        float2 x0, x1, x2, x3;
+        if (e_m1 == 1) {
+          // Members 4q, 4q+1 (and 4q+2, 4q+3) are 16-byte units.
+          const float4* raw4 = reinterpret_cast<const float4*>(raw);
+          const float4 p0 = raw4[e0 >> 1], p1 = raw4[(e0 ^ e_m2) >> 1];
+          x0 = make_float2(p0.x, p0.y);
+          x1 = make_float2(p0.z, p0.w);
+          x2 = make_float2(p1.x, p1.y);
+          x3 = make_float2(p1.z, p1.w);
+        } else {
+          x0 = raw[e0];
+          x1 = raw[e0 ^ e_m1];
+          x2 = raw[e0 ^ e_m2];
+          x3 = raw[e0 ^ e_m1 ^ e_m2];
+        }
+        x[0] = x0.x * sc; x[1] = x0.y * sc; x[2] = x1.x * sc; x[3] = x1.y * sc;
+        x[4] = x2.x * sc; x[5] = x2.y * sc; x[6] = x3.x * sc; x[7] = x3.y * sc;
+        uint4 h, l;
+        uint32_t* hp = &h.x;
+        uint32_t* lp = &l.x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const __half2 hh = __floats2half2_rn(x[2 * c], x[2 * c + 1]);
+          const float2 hf = __half22float2(hh);
+          hp[c] = *reinterpret_cast<const uint32_t*>(&hh);
+          lp[c] = pack_half2(x[2 * c] - hf.x, x[2 * c + 1] - hf.y);
+        }
         const uint32_t o = my_so | tab_so[j];
-        *reinterpret_cast<float4*>(smem + obuf + o) = h;
-        *reinterpret_cast<float4*>(smem + obuf + kTileBytes + o) = l;
+        *reinterpret_cast<uint4*>(smem + obuf + o) = h;
+        *reinterpret_cast<uint4*>(smem + obuf + kBImgBytes + o) = l;
       }
       fence_async_smem();
       bar_sync(1, kProdThreads);
@@ -487,21 +524,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = (32 * quad) << 16;
     const uint32_t row = 32 * quad + lane;
     // Gate into tensor memory: rows of this quadrant, columns of this half
-    // (A_hi and A_lo, 64 columns each).
+    // (A_hi and A_lo, 64 columns of FP16 pairs each).
     {
-      const float* ahi = a.operands + size_t(row) * kARowFloats + 64 * chalf;
-      const float* alo = a.operands + size_t(kReal) * kReal +
-                         size_t(row) * kARowFloats + 64 * chalf;
+      const uint32_t* ahi = a.operands + size_t(row) * kAWords + 32 * chalf;
+      const uint32_t* alo = ahi + size_t(kReal) * kAWords;
       uint32_t r[32];
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
+      for (int q = 0; q < 32; ++q) r[q] = ahi[q];
+      tmem_st32(tmem + lane_base + kTmemAhi + 32 * chalf, r);
 #pragma unroll
-        for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(ahi[32 * c + q]);
-        tmem_st32(tmem + lane_base + kTmemAhi + 64 * chalf + 32 * c, r);
-#pragma unroll
-        for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(alo[32 * c + q]);
-        tmem_st32(tmem + lane_base + kTmemAlo + 64 * chalf + 32 * c, r);
-      }
+      for (int q = 0; q < 32; ++q) r[q] = alo[q];
+      tmem_st32(tmem + lane_base + kTmemAlo + 32 * chalf, r);
       tmem_wait_st();
       tc_fence_before();
       bar_sync(2, kEpiThreads);
@@ -510,10 +543,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint64_t my_g = tile_goff(et << 1, g);
     const uint32_t my_rd = swz_out(et << 1, g);
     const uint32_t my_me = swz_out(tile_e(0, row / 2, g), g);
+    const float inv = a.inv_scale;
     int i = 0;
     for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
-      const int s = i & 1;
-      const bool bad = !mbar_wait(&acc_full[s], (i >> 1) & 1, flag);
+      const int s = i % kNB;
+      const bool bad = !mbar_wait(&acc_full[s], (i / kNB) & 1, flag);
       if (bar_or(2, kEpiThreads, bad)) break;
       tc_fence_after();
       uint32_t v[32];
@@ -531,8 +565,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t send = odd ? v[j] : v[16 + j];
         const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, 1);
         const uint32_t mine = odd ? v[16 + j] : v[j];
-        const float re = __uint_as_float(odd ? recv : mine);
-        const float im = __uint_as_float(odd ? mine : recv);
+        const float re = __uint_as_float(odd ? recv : mine) * inv;
+        const float im = __uint_as_float(odd ? mine : recv) * inv;
         const uint32_t grp = 32 * chalf + (odd ? 16 + j : j);
         stage[my_me ^ tab_ge[grp]] = make_float2(re, im);
       }
@@ -554,27 +588,29 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ======================== MMA issuer =================================
     int i = 0;
     for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
-      const int s = i & 1;
-      if (!mbar_wait(&op_full[s], (i >> 1) & 1, flag)) break;
+      const int s = i % kNB;
+      if (!mbar_wait(&op_full[s], (i / kNB) & 1, flag)) break;
       // The gate must be in tensor memory before the first MMA, and
-      // accumulator s is free once the epilogue drained tile i-2 (the
-      // ((i-2)/2)-th completion of acc_free[s]).
+      // accumulator s is free once the epilogue drained tile i-kNB (the
+      // ((i-kNB)/kNB)-th completion of acc_free[s]).
       if (i == 0) {
         if (!mbar_wait(gate_ready, 0, flag)) break;
-      } else if (i >= 2) {
-        if (!mbar_wait(&acc_free[s], ((i - 2) >> 1) & 1, flag)) break;
+      } else if (i >= kNB) {
+        if (!mbar_wait(&acc_free[s], ((i - kNB) / kNB) & 1, flag)) break;
       }
       tc_fence_after();
       const uint32_t obuf = kOffOp + s * kOpBytes;
       const uint32_t d = tmem + kTmemD + 64 * s;
       const uint64_t dhi = make_desc(sbase + obuf, kLBO, kSBOB);
-      const uint64_t dlo = make_desc(sbase + obuf + kTileBytes, kLBO, kSBOB);
+      const uint64_t dlo = make_desc(sbase + obuf + kBImgBytes, kLBO, kSBOB);
+      // K = 16 FP16 elements per MMA: two core matrices along K (256 B) and
+      // eight tensor-memory columns of A.
 #pragma unroll
-      for (int kk = 0; kk < kReal / 8; ++kk) {
+      for (int kk = 0; kk < kReal / 16; ++kk) {
         const uint64_t ko = uint64_t(kk) * (2 * kLBO >> 4);
-        mma_tf32_ts(d, tmem + kTmemAhi + 8 * kk, dhi + ko, kk > 0);
-        mma_tf32_ts(d, tmem + kTmemAhi + 8 * kk, dlo + ko, 1);
-        mma_tf32_ts(d, tmem + kTmemAlo + 8 * kk, dhi + ko, 1);
+        mma_f16_ts(d, tmem + kTmemAhi + 8 * kk, dhi + ko, kk > 0);
+        mma_f16_ts(d, tmem + kTmemAhi + 8 * kk, dlo + ko, 1);
+        mma_f16_ts(d, tmem + kTmemAlo + 8 * kk, dhi + ko, 1);
       }
       mma_commit(&acc_full[s]);
     }
@@ -630,19 +666,12 @@ static void pad_to_6(unsigned n, const unsigned* qs, unsigned k,
   for (unsigned j = 0; j < 6; ++j) qs6[j] = all[j];
 }
 
-static float tf32_host(float x) {
-  uint32_t u;
-  std::memcpy(&u, &x, 4);
-  u = (u + 0x1000u) & 0xFFFFE000u;
-  float r;
-  std::memcpy(&r, &u, 4);
-  return r;
-}
-
-// A_real (hi, lo), row-major 128 x 128 each: row 2r+pr, column 2c+pc.
+// A_real (hi, lo) as FP16 pairs: 128 rows x 64 words each; row 2r+pr,
+// column 2c+pc of [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im);
+// word w of a row holds columns 2w (low half) and 2w + 1.
 static void build_a_images(const float* m6, unsigned char* out) {
-  float* hi = reinterpret_cast<float*>(out);
-  float* lo = hi + kReal * kReal;
+  uint16_t* hi = reinterpret_cast<uint16_t*>(out);
+  uint16_t* lo = hi + kReal * kReal;
   for (uint32_t r = 0; r < kD; ++r)
     for (uint32_t c = 0; c < kD; ++c) {
       const float mr = m6[2 * (r * kD + c)], mi = m6[2 * (r * kD + c) + 1];
@@ -650,11 +679,11 @@ static void build_a_images(const float* m6, unsigned char* out) {
       for (uint32_t pr = 0; pr < 2; ++pr)
         for (uint32_t pc = 0; pc < 2; ++pc) {
           const float x = v[pr][pc];
-          const float h = tf32_host(x);
-          const float l = tf32_host(x - h);
+          const __half h = __float2half_rn(x);
+          const __half l = __float2half_rn(x - __half2float(h));
           const size_t off = size_t(2 * r + pr) * kReal + (2 * c + pc);
-          hi[off] = h;
-          lo[off] = l;
+          std::memcpy(hi + off, &h, 2);
+          std::memcpy(lo + off, &l, 2);
         }
     }
 }
@@ -716,10 +745,15 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
   // (even lanes keep groups 0..15 of a warp's 32 columns, odd lanes 16..31).
   build({tpos[0], tpos[1], tpos[2], gpos[4]}, 0xF, g.out_src, g.out_dst,
         &g.out_n);
-  // Split reads: half-warp lanes vary group bits 0..2 and member bit 1
-  // (pair bit 0); 16-byte units keep bit 0 in place.
-  build({gpos[0], gpos[1], gpos[2], tpos[1]}, 0xE, g.raw_src, g.raw_dst,
-        &g.raw_n);
+  // Split reads: lanes vary group bits 0..2 and (half-warp) member bit 2;
+  // 16-byte units keep bit 0 in place.  With qubit 0 a target (member bit 0
+  // = tile bit 0) members 4q, 4q+1 are one 16-byte unit read by one LDS.128,
+  // and the quarter-warp lanes (group bits 0..2) must hit distinct units.
+  if (g.tile_is_target[0])
+    build({gpos[0], gpos[1], gpos[2]}, 0xE, g.raw_src, g.raw_dst, &g.raw_n);
+  else
+    build({gpos[0], gpos[1], gpos[2], tpos[2]}, 0xE, g.raw_src, g.raw_dst,
+          &g.raw_n);
 
   std::vector<unsigned> ins(qs6 + kK - h, qs6 + kK);
   std::sort(ins.begin(), ins.end());
@@ -731,7 +765,7 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
 
 }  // namespace tc
 
-size_t tc_operand_bytes(unsigned) { return size_t(tc::kOperandFloats) * 4; }
+size_t tc_operand_bytes(unsigned) { return size_t(tc::kOperandBytes); }
 
 void tc_build_operands(unsigned k, const float* m32, void* host_out) {
   // The plan stores matrices already padded to 6 targets (k == 6).
@@ -778,7 +812,13 @@ int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
     set_error("tensor-core gate without device operands");
     return QSG_ERR_INVALID;
   }
-  a.operands = static_cast<const float*>(operands);
+  a.operands = static_cast<const uint32_t*>(operands);
+  // sigma = 2^(floor(n/2) - 4): amplitudes of a normalised state (about
+  // 2^(-n/2)) land near 2^-4, and |psi_i| up to 32 stays below the FP16
+  // maximum.
+  const int e = int(n / 2) - 4;
+  a.scale = std::ldexp(1.0f, e);
+  a.inv_scale = std::ldexp(1.0f, -e);
   int rc0 = tc_setup();
   if (rc0) return rc0;
   a.error = g_tc_err;
