@@ -476,9 +476,10 @@ def bench_trajectories(num_streams: int, max_fused_size: int = 0,
     upload, device work and the final synchronisation); latency =
     per-trajectory device time.
 
-    mode "auto": the autotuner picks fusion size, the split between the
-    persistent packed kernel and the concurrent stream path, CTAs per SM and
-    tile budget on an eighth of the repetitions (outside the timed run);
+    mode "auto": the autotuner picks the stream path's form (fusion size,
+    tensor cores), the split between the persistent packed kernel and the
+    concurrent stream path, CTAs per SM and tile budget on an eighth of the
+    repetitions (outside the timed run);
     "packed": every circuit in the persistent kernel; "streams": the stream
     path only."""
     import numpy as np
@@ -488,33 +489,35 @@ def bench_trajectories(num_streams: int, max_fused_size: int = 0,
     ns = rng.integers(TRAJ["n_min"], TRAJ["n_max"] + 1, size=TRAJ["circuits"])
     made = {}
 
-    def make_runners(f):
-        if f not in made:
+    def make_runners(f, tensor):
+        if (f, tensor) not in made:
             rs = []
             for i, n in enumerate(ns):
                 c = E.Circuit.chain(int(n), TRAJ["cycles"], 1000 + i)
                 nc = E.NoisyCircuit.make(c, TRAJ["p_depol"], TRAJ["gamma"], 2)
-                rs.append(E.Trajectories(nc, max_fused_size=f))
-            made[f] = rs
-        return made[f]
+                rs.append(E.Trajectories(nc, max_fused_size=f,
+                                         tensor_path=tensor))
+            made[(f, tensor)] = rs
+        return made[(f, tensor)]
 
     t0 = time.perf_counter()
     tune = None
+    tensor = max_fused_size >= 5
     if mode == "auto":
+        forms = AT.FORMS if not max_fused_size else ((max_fused_size, tensor),)
         tune = AT.tune_trajectories(
             make_runners, ns, TRAJ["reps"], tag="chain d12 depol1e-3 ad5e-3",
-            fs=(max_fused_size,) if max_fused_size else (3, 4),
-            num_streams=num_streams, use_cache=False)
+            forms=forms, num_streams=num_streams, use_cache=False)
         cfg = dict(tune["best"])
     elif mode == "packed":
-        cfg = dict(max_fused_size=max_fused_size or 4, split=int(ns.max()),
+        cfg = dict(max_fused_size=4, tensor=False, split=int(ns.max()),
                    ctas_per_sm=ctas_per_sm, tile_kib=tile_kib)
     else:
-        cfg = dict(max_fused_size=max_fused_size or 4, split=0,
+        cfg = dict(max_fused_size=max_fused_size or 4, tensor=tensor, split=0,
                    ctas_per_sm=0, tile_kib=0)
     if split >= 0:
         cfg["split"] = split
-    runners = make_runners(cfg["max_fused_size"])
+    runners = AT.runners_for(make_runners, ns, cfg)
     setup_s = time.perf_counter() - t0
     items = [(i, r) for i in range(len(runners)) for r in range(TRAJ["reps"])]
     AT.run(runners, [(i, 10**6) for i in range(len(runners))], cfg, num_streams)
@@ -637,7 +640,8 @@ def main():
                     help="run only the batched-trajectory workload")
     ap.add_argument("--traj-streams", type=int, default=8)
     ap.add_argument("--traj-f", type=int, default=0,
-                    help="fusion size (0: autotuned among 3, 4)")
+                    help="stream-path fusion size (0: autotuned; 5, 6 use "
+                         "the tensor cores)")
     ap.add_argument("--traj-mode", default="auto",
                     choices=["auto", "packed", "streams"])
     ap.add_argument("--traj-split", type=int, default=-1,

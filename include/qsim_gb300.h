@@ -177,10 +177,12 @@ int qsg_apply_controlled_gate(qsg_ctx* ctx, float* state, unsigned n,
 int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
                           const unsigned* qs, unsigned k, const float* matrix,
                           double* out_re_im);
-/* ApplyGate on the tensor cores (tcgen05, split-TF32, FP32 accumulation):
- * k <= 6 targets, n >= 12; the gate is padded to 6 targets with the
- * identity on the lowest free qubits.  No counterpart in the reference, which
- * applies every gate on CUDA cores (lib/simulator_cuda.h:333-380). */
+/* ApplyGate on the tensor cores (tcgen05, split FP16 with a power-of-two
+ * state scale, FP32 accumulation): k <= 6 targets, n >= 12; the gate is
+ * padded to 6 targets with the identity on the lowest free qubits.  Every
+ * amplitude must satisfy |psi_i| <= 4 (true for any state of norm <= 4).
+ * No counterpart in the reference, which applies every gate on CUDA cores
+ * (lib/simulator_cuda.h:333-380). */
 int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
                       const unsigned* qs, unsigned k, const float* matrix);
 /* Reads and clears the tensor-core kernels' error flag: 1 if a bounded
@@ -380,6 +382,11 @@ typedef struct qsg_traj_options {
   int collect_kop_stat;            /* lib/qtrajectory.h:48-58 */
   int collect_mea_stat;
   int normalize_before_mea_gates;
+  int tensor_path;                 /* fused blocks of >= tc_min_k qubits on
+                                      the tensor cores (padded to 6 targets;
+                                      every trajectory is normalised at the
+                                      end) */
+  unsigned tc_min_k;               /* 0: 5 */
 } qsg_traj_options;
 /* Fuses the noisy circuit once (each channel as its first Kraus operator).
  * QSG_ERR_UNSUPPORTED for a non-unitary channel on more than 2 qubits or

@@ -68,7 +68,7 @@ class SimulatorGB300 {
   // lib/simulator_cuda.h:265-267.
   static unsigned SIMDRegisterSize() { return qsg_simd_register_size(); }
 
-  // Tensor-core application (tcgen05, split TF32) of a gate on <= 6 qubits;
+  // Tensor-core application (tcgen05, split FP16) of a gate on <= 6 qubits;
   // no counterpart in the reference.
   void ApplyGateTensor(const std::vector<unsigned>& qs, const fp_type* matrix,
                        State& state) const {

@@ -156,7 +156,8 @@ class TrajOptions(C.Structure):
     """qsg_traj_options."""
     _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
                 ("collect_kop_stat", C.c_int), ("collect_mea_stat", C.c_int),
-                ("normalize_before_mea_gates", C.c_int)]
+                ("normalize_before_mea_gates", C.c_int),
+                ("tensor_path", C.c_int), ("tc_min_k", C.c_uint)]
 
 
 class BatchOptions(C.Structure):

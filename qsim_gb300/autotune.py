@@ -8,9 +8,11 @@ fused block, several host threads), or both at once with the circuits split
 by qubit count.  The tuner times candidate configurations on a sample of
 the batch and keeps the one with the most trajectories per second:
 
-  * ``max_fused_size``: the fusion block size k of the runners (3 or 4);
-  * ``split``: the largest qubit count sent to the persistent kernel (the
-    rest run concurrently on the stream path);
+  * the stream path's form: fusion block size k (3 or 4 on CUDA cores, or
+    6 with blocks of >= 5 qubits on the tensor cores);
+  * ``split``: the largest qubit count sent to the persistent kernel (whose
+    runners fuse at k = 4 on CUDA cores); the rest run concurrently on the
+    stream path;
   * ``ctas_per_sm`` and ``tile_kib``: the persistent kernel's residency and
     the shared-memory tile budget of its pipelined gate passes.
 
@@ -81,26 +83,41 @@ def _store(db):
         pass  # an unwritable cache only costs a re-tune
 
 
-def candidates(max_n: int, fs=(3, 4)):
-    """Configurations tried: all on the stream path, all in the persistent
-    kernel, and splits by qubit count with both running at once."""
+FORMS = ((3, False), (4, False), (6, True))
+
+
+def candidates(max_n: int, forms=FORMS):
+    """Configurations tried: each stream-path form alone, all circuits in the
+    persistent kernel, and splits by qubit count with both running at
+    once."""
     out = []
-    for f in fs:
-        out.append(dict(max_fused_size=f, split=0, ctas_per_sm=0, tile_kib=0))
-        out.append(dict(max_fused_size=f, split=max_n, ctas_per_sm=2,
-                        tile_kib=32))
+    for f, tc in forms:
+        base = dict(max_fused_size=f, tensor=tc)
+        out.append(dict(base, split=0, ctas_per_sm=0, tile_kib=0))
         for split in (14, 16, 18, 20):
             if split >= max_n:
                 continue
             for per_sm in (1, 2):
-                out.append(dict(max_fused_size=f, split=split,
-                                ctas_per_sm=per_sm, tile_kib=32))
+                out.append(dict(base, split=split, ctas_per_sm=per_sm,
+                                tile_kib=32))
+    out.append(dict(max_fused_size=4, tensor=False, split=max_n,
+                    ctas_per_sm=2, tile_kib=32))
     return out
 
 
+def runners_for(make_runners, qubits, cfg):
+    """Per circuit: the packed kernel's runner (k = 4, CUDA cores) for
+    circuits of at most cfg["split"] qubits, the stream form's otherwise."""
+    packed = make_runners(4, False)
+    other = make_runners(cfg["max_fused_size"], cfg.get("tensor", False))
+    return [packed[i] if int(n) <= cfg["split"] else other[i]
+            for i, n in enumerate(qubits)]
+
+
 def run(runners, items, cfg, num_streams: int = 8, out_states=None):
-    """Runs `items` with configuration `cfg`; returns (per-item stats,
-    latency_ms, wall seconds, launches, info)."""
+    """Runs `items` [(runner index, rep)] with configuration `cfg` (split 0:
+    stream path only); returns (per-item stats, latency_ms, wall seconds,
+    launches, info)."""
     if cfg["split"] == 0:
         per, lat, wall, launches = E.run_trajectory_batch(
             runners, items, num_streams=num_streams, out_states=out_states,
@@ -113,12 +130,13 @@ def run(runners, items, cfg, num_streams: int = 8, out_states=None):
 
 
 def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
-                      sample_reps: int = 0, fs=(3, 4), device: int = 0,
+                      sample_reps: int = 0, forms=FORMS, device: int = 0,
                       num_streams: int = 8, use_cache: bool = True):
     """Chooses the configuration with the most trajectories/s.
 
-    make_runners(f) returns the runners (one per circuit, in the order of
-    `qubits`) fused at max_fused_size f; the batch is every circuit times
+    make_runners(f, tensor) returns the runners (one per circuit, in the
+    order of `qubits`) fused at max_fused_size f, with blocks of >= 5 qubits
+    on the tensor cores when `tensor`; the batch is every circuit times
     `reps` repetitions.  Candidates are timed on `sample_reps` repetitions
     per circuit (default reps / 8, at least 1), after one warm-up run each.
     Returns {"best": cfg, "table": [(cfg, traj/s), ...], "cached": bool,
@@ -131,10 +149,9 @@ def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
     t0 = time.perf_counter()
     sample_reps = sample_reps or max(1, reps // 8)
     max_n = max(int(q) for q in qubits)
-    runners_by_f = {f: make_runners(f) for f in fs}
     table = []
-    for cfg in candidates(max_n, fs):
-        runners = runners_by_f[cfg["max_fused_size"]]
+    for cfg in candidates(max_n, forms):
+        runners = runners_for(make_runners, qubits, cfg)
         items = [(i, 10**6 + r) for i in range(len(runners))
                  for r in range(sample_reps)]
         run(runners, items[:len(runners)], cfg, num_streams)  # warm-up
@@ -145,4 +162,4 @@ def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
         db[key] = {"best": best, "table": table}
         _store(db)
     return {"best": best, "table": table, "cached": False,
-            "tune_s": time.perf_counter() - t0, "runners": runners_by_f}
+            "tune_s": time.perf_counter() - t0}

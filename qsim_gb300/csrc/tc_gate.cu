@@ -12,9 +12,10 @@
 //     tile's 64 groups x 128 real components.  One CTA tile = 64 groups x 64
 //     members = 4096 amplitudes (32 KiB).
 //   * Split FP16 with a power-of-two scale: the tile is multiplied by
-//     sigma = 2^(floor(n/2) - 4), which brings the amplitudes of a state of
-//     norm <= 1 (|psi_i| <= 1, typically 2^(-n/2)) into the normal FP16
-//     range with room for |psi_i| <= 32; then A = A_hi + A_lo and
+//     sigma = 2^min(floor(n/2), 14), which brings the typical amplitude of a
+//     normalised state (2^(-n/2)) near 1, so that both parts of its split
+//     are normal FP16 numbers; amplitudes must satisfy |psi_i| <= 4 (any
+//     state of norm <= 4), the FP16 maximum being 65504.  A = A_hi + A_lo and
 //     B = B_hi + B_lo with every part an FP16 number, and
 //     D = A_hi B_hi + A_hi B_lo + A_lo B_hi (3 x 8 MMAs of M=128, N=64,
 //     K=16), FP32 accumulation, D / sigma in the epilogue.  FP16 keeps the
@@ -813,10 +814,11 @@ int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
     return QSG_ERR_INVALID;
   }
   a.operands = static_cast<const uint32_t*>(operands);
-  // sigma = 2^(floor(n/2) - 4): amplitudes of a normalised state (about
-  // 2^(-n/2)) land near 2^-4, and |psi_i| up to 32 stays below the FP16
+  // sigma = 2^min(floor(n/2), 14): amplitudes of a normalised state (about
+  // 2^(-n/2)) land near 1, where the lo parts of the split are normal FP16
+  // numbers (relative error ~2^-23), and |psi_i| <= 4 stays below the FP16
   // maximum.
-  const int e = int(n / 2) - 4;
+  const int e = std::min(int(n / 2), 14);
   a.scale = std::ldexp(1.0f, e);
   a.inv_scale = std::ldexp(1.0f, -e);
   int rc0 = tc_setup();

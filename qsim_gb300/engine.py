@@ -331,10 +331,12 @@ class Trajectories:
     def __init__(self, noisy: NoisyCircuit, max_fused_size: int = 4,
                  seeds: int = 0, collect_kop_stat: bool = True,
                  collect_mea_stat: bool = True,
-                 normalize_before_mea_gates: bool = True):
+                 normalize_before_mea_gates: bool = True,
+                 tensor_path: bool = False, tc_min_k: int = 5):
         self.noisy = noisy
         o = N.TrajOptions(max_fused_size, seeds, int(collect_kop_stat),
-                          int(collect_mea_stat), int(normalize_before_mea_gates))
+                          int(collect_mea_stat), int(normalize_before_mea_gates),
+                          int(tensor_path), tc_min_k)
         h = C.c_void_p()
         check(N.lib.qsg_traj_create(noisy.h, C.byref(o), C.byref(h)))
         self.h = h

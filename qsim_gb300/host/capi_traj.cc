@@ -188,6 +188,8 @@ int qsg_traj_create(const qsg_noisy* h, const qsg_traj_options* opts,
     o.collect_kop_stat = opts->collect_kop_stat != 0;
     o.collect_mea_stat = opts->collect_mea_stat != 0;
     o.normalize_before_mea_gates = opts->normalize_before_mea_gates != 0;
+    o.tensor_path = opts->tensor_path != 0;
+    if (opts->tc_min_k) o.tc_min_k = opts->tc_min_k;
   }
   auto* t = new (std::nothrow) qsg_traj();
   if (!t) return QSG_ERR_OOM;

@@ -255,12 +255,13 @@ std::vector<float> to_f32(const Mat& m) {
 }  // namespace
 
 TrajectoryRunner::~TrajectoryRunner() {
-  if (dev_table_ || dev_mats_) {
+  if (dev_table_ || dev_mats_ || dev_tc_) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(dev_device_);
     if (dev_table_) cudaFree(dev_table_);
     if (dev_mats_) cudaFree(dev_mats_);
+    if (dev_tc_) cudaFree(dev_tc_);
     cudaSetDevice(cur);
   }
 }
@@ -367,20 +368,57 @@ int TrajectoryRunner::create(const NoisyCircuit& nc,
   FuseOptions fo;
   fo.max_fused_size = opt.max_fused_size;
   fo.seeds = opt.seeds ? opt.seeds : 12;
-  fo.tensor_path = false;
+  fo.tensor_path = opt.tensor_path;
+  fo.tc_min_k = opt.tc_min_k;
   r->base_ = fuse(slots, fo);
   for (auto& p : r->base_.ops) std::sort(p.members.begin(), p.members.end());
-  size_t off = 0;
+  size_t off = 0, toff = 0;
   r->mat_off_.assign(r->base_.ops.size(), 0);
+  r->tc_off_.assign(r->base_.ops.size(), size_t(-1));
   for (size_t i = 0; i < r->base_.ops.size(); ++i) {
+    const PlanOp& p = r->base_.ops[i];
     r->mat_off_[i] = off;
-    off += r->base_.ops[i].m32.size();
+    off += p.m32.size();
+    if (p.kind == OpKind::kGate && p.path == Path::kTensor) {
+      r->tc_off_[i] = toff;
+      toff += (tc_operand_bytes(p.qs.size()) + 1023) & ~size_t(1023);
+      r->has_tc_ = true;
+    }
   }
   *out = std::move(r);
   return QSG_OK;
 }
 
+int TrajectoryRunner::upload_tc(qsg_ctx* ctx) const {
+  if (!has_tc_ || dev_tc_) return QSG_OK;
+  int rc = tc_setup();
+  if (rc) return rc;
+  size_t total = 0;
+  for (size_t i = 0; i < base_.ops.size(); ++i)
+    if (tc_off_[i] != size_t(-1))
+      total = tc_off_[i] + ((tc_operand_bytes(base_.ops[i].qs.size()) + 1023) &
+                            ~size_t(1023));
+  std::vector<unsigned char> host(total);
+  for (size_t i = 0; i < base_.ops.size(); ++i)
+    if (tc_off_[i] != size_t(-1))
+      tc_build_operands(base_.ops[i].qs.size(), base_.ops[i].m32.data(),
+                        host.data() + tc_off_[i]);
+  void* p = nullptr;
+  rc = dev_alloc(ctx, total, &p);
+  if (rc) return rc;
+  rc = dev_upload(ctx, p, host.data(), total);
+  if (rc) {
+    dev_free(ctx, p);
+    return rc;
+  }
+  dev_tc_ = p;
+  dev_device_ = ctx_device(ctx);
+  return QSG_OK;
+}
+
 int TrajectoryRunner::upload(qsg_ctx* ctx) const {
+  int rc0 = upload_tc(ctx);
+  if (rc0) return rc0;
   if (num_dev_channels_ == 0 || dev_table_) return QSG_OK;
   std::vector<TrajChannelDev> table(num_dev_channels_);
   for (size_t c = 0; c < chans_.size(); ++c) {
@@ -607,12 +645,16 @@ int TrajectoryRunner::walk(uint64_t rep, uint64_t* stats, Sink& sink) const {
       if (present == 0) continue;
       if (p.kind == OpKind::kControlled) {
         rc = sink.gate(p.qs, &nc_.ops[p.members[0]].op, p.m32.data(),
-                       ptrdiff_t(pi));
+                       ptrdiff_t(pi), nullptr);
         if (rc) return rc;
         continue;
       }
       if (present == p.members.size() && all_default) {
-        rc = sink.gate(p.qs, nullptr, p.m32.data(), ptrdiff_t(pi));
+        rc = sink.gate(p.qs, nullptr, p.m32.data(), ptrdiff_t(pi),
+                       tc_off_[pi] == size_t(-1)
+                           ? nullptr
+                           : static_cast<const unsigned char*>(dev_tc_) +
+                                 tc_off_[pi]);
         if (rc) return rc;
         continue;
       }
@@ -622,7 +664,7 @@ int TrajectoryRunner::walk(uint64_t rep, uint64_t* stats, Sink& sink) const {
       std::sort(qs.begin(), qs.end());
       qs.erase(std::unique(qs.begin(), qs.end()), qs.end());
       std::vector<float> m32 = to_f32(block_matrix_ops(ptrs, qs));
-      rc = sink.gate(qs, nullptr, m32.data(), -1);
+      rc = sink.gate(qs, nullptr, m32.data(), -1, nullptr);
       if (rc) return rc;
     }
     if (s + 1 < nseg) {
@@ -635,7 +677,7 @@ int TrajectoryRunner::walk(uint64_t rep, uint64_t* stats, Sink& sink) const {
       if (rc) return rc;
     }
   }
-  if (!unitary) return sink.normalize();
+  if (!unitary || has_tc_) return sink.normalize();
   return QSG_OK;
 }
 
@@ -649,7 +691,10 @@ struct StreamSink {
 
   int set_zero() { return qsg_set_state_zero(ws.ctx, state, n); }
   int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
-           ptrdiff_t) {
+           ptrdiff_t, const void* tc_operands) {
+    if (tc_operands)
+      return apply_gate_tc(ws.ctx, state, n, qs.data(), qs.size(), m32,
+                           tc_operands);
     if (ctl)
       return apply_gate_ex(ws.ctx, state, n, qs.data(), qs.size(),
                            ctl->cqs.data(), ctl->cqs.size(), ctl->cvals, m32,
@@ -711,7 +756,9 @@ struct ProgramSink {
     return QSG_OK;
   }
   int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
-           ptrdiff_t base) {
+           ptrdiff_t base, const void* tc_operands) {
+    if (tc_operands)
+      return unsupported("packed batch: tensor-core blocks run on streams");
     if (qs.empty() || qs.size() > kBatchMaxK ||
         (ctl && ctl->cqs.size() > kBatchMaxControls))
       return unsupported("packed batch: block too large");
@@ -769,6 +816,7 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
 }
 
 bool TrajectoryRunner::packable() const {
+  if (has_tc_) return false;
   for (const PlanOp& p : base_.ops) {
     if (p.kind == OpKind::kMeasure) return false;
     if (p.qs.size() > kBatchMaxK) return false;

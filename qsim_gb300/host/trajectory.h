@@ -86,6 +86,11 @@ struct TrajectoryOptions {
   bool collect_kop_stat = true;            // lib/qtrajectory.h:48-58
   bool collect_mea_stat = true;
   bool normalize_before_mea_gates = true;
+  // Fused blocks of >= tc_min_k qubits on the tensor cores (padded to six
+  // targets).  Their FP32 accumulation loses ~1e-6 of norm per pass, so
+  // every trajectory is normalised at the end.
+  bool tensor_path = false;
+  unsigned tc_min_k = 5;
 };
 
 // Per-op statistics: entry i holds the Kraus-operator index chosen for op i
@@ -141,6 +146,8 @@ class TrajectoryRunner {
   // Device table of the channels sampled on the device (uploaded on first
   // use for the given context's device).
   int upload(qsg_ctx* ctx) const;
+  // Tensor-core operands of the fused blocks on that path.
+  int upload_tc(qsg_ctx* ctx) const;
 
   // True when every trajectory of this runner can run inside the packed
   // batch kernel: no measurements, fused blocks of at most kBatchMaxK
@@ -178,6 +185,9 @@ class TrajectoryRunner {
   mutable TrajChannelDev* dev_table_ = nullptr;
   mutable float* dev_mats_ = nullptr;     // fused plan's matrices
   std::vector<size_t> mat_off_;           // per plan op: float offset
+  mutable void* dev_tc_ = nullptr;        // tensor-core operands
+  std::vector<size_t> tc_off_;            // per plan op (or size_t(-1))
+  bool has_tc_ = false;
   mutable int dev_device_ = -1;
   size_t num_dev_channels_ = 0;
 };

@@ -158,15 +158,20 @@ def test_autotuned_configurations_agree(ss):
     reaches the same states; the tuner returns one of them."""
     from qsim_gb300 import autotune as AT
     sizes = [6, 9, 12, 15, 17]
+    made = {}
 
-    def make(f):
-        return [E.Trajectories(E.NoisyCircuit.make(E.Circuit.chain(n, 6, 40 + n),
-                                                    0.01, 0.03, 2),
-                               max_fused_size=f) for n in sizes]
-    runners = make(4)
+    def make(f, tensor):
+        if (f, tensor) not in made:
+            made[(f, tensor)] = [
+                E.Trajectories(E.NoisyCircuit.make(E.Circuit.chain(n, 6, 40 + n),
+                                                   0.01, 0.03, 2),
+                               max_fused_size=f, tensor_path=tensor)
+                for n in sizes]
+        return made[(f, tensor)]
     items = [(i % len(sizes), 500 + i) for i in range(30)]
     ref = None
-    for cfg in AT.candidates(max(sizes), fs=(4,)):
+    for cfg in AT.candidates(max(sizes), forms=((4, False), (6, True))):
+        runners = AT.runners_for(make, sizes, cfg)
         outs = [ss.Create(sizes[r]) for r, _ in items]
         per, lat, wall, launches, info = AT.run(runners, items, cfg, 4, outs)
         states = [ss.to_numpy(o) for o in outs]
@@ -179,7 +184,32 @@ def test_autotuned_configurations_agree(ss):
                 same += 1
                 assert rel_l2(sa, sb) < STATE_TOL, cfg
         assert same >= 0.95 * len(items), cfg
-    tune = AT.tune_trajectories(make, sizes, 4, fs=(3, 4), num_streams=4,
+    tune = AT.tune_trajectories(make, sizes, 4, num_streams=4,
                                 use_cache=False)
     assert tune["best"] in [c for c, _ in tune["table"]]
     assert all(v > 0 for _, v in tune["table"])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if int(load_golden(c)["n"]) >= 12])
+def test_tensor_core_trajectories_match_reference(case, ss):
+    """Trajectories whose fused blocks run on the tensor cores (blocks of
+    >= 2 qubits, padded to six targets) make the reference's choices and
+    reach its FP64 states within relative L2 1e-5."""
+    from qsim_gb300 import api
+    ctx = api.Context()
+    d = load_golden(case)
+    n = int(d["n"])
+    t = E.Trajectories(build_noisy(d), max_fused_size=6, tensor_path=True,
+                       tc_min_k=2)
+    ref32, ref64 = ref_samples(d, "32"), ref_samples(d, "64")
+    st = ss.Create(n)
+    agree = 0
+    for i, rep in enumerate(range(int(d["r0"]), int(d["r1"]))):
+        stats = t.run(ctx, st, rep)
+        got = [int(x) for x in E.Trajectories.samples(stats)]
+        agree += got == [int(x) for x in ref32[i]]
+        if got == [int(x) for x in ref64[i]]:
+            s = ss.to_numpy(st)
+            want = d["f64"][i].astype(np.complex128)
+            assert rel_l2(s, want) < STATE_TOL, (case, rep, rel_l2(s, want))
+    assert agree >= MIN_AGREE[case] * len(ref32), (case, agree, len(ref32))

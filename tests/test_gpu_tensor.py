@@ -1,7 +1,7 @@
-"""Tensor-core (tcgen05, split-TF32) gate path against the FP64 oracle.
+"""Tensor-core (tcgen05, split FP16 with a state scale) gate path against the FP64 oracle.
 
 Tolerance: relative L2 <= 1e-5 per gate and per circuit, the same bar as the
-CUDA-core path (split TF32 with FP32 accumulation keeps ~2^-21 relative error
+CUDA-core path (split FP16 with FP32 accumulation keeps ~2^-22 relative error
 per product); fidelity >= 1 - 1e-6 against FP64."""
 import numpy as np
 import pytest
@@ -84,7 +84,7 @@ def test_tc_padded_gates(eng, oracle):
 
 def test_tc_non_unitary_matrix(eng, oracle):
     """M[i] = i + 1 (tests/simulator_testfixture.h:1146-1212 pattern) on a
-    uniform state: large entries exercise the split-TF32 accuracy."""
+    uniform state: large entries exercise the split-FP16 accuracy."""
     q, E, N, ctx, ss, sim = eng
     n = 12
     st = ss.Create(n)
