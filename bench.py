@@ -256,17 +256,28 @@ def run_engine(args, world, rank, local, dist):
             plan.replay(ctx)
         return ctx.timer_stop() / steps
 
+    def kernels_per_run(plan):
+        # Kernels of one run of the plan (its fused ops plus, for unitary
+        # tensor-core plans, the norm-restoration kernels), counted by the
+        # library; the run itself precedes the timed region.
+        before = ctx.launches()
+        plan.run(ctx, st)
+        ctx.sync()
+        return ctx.launches() - before
+
     results = {}
     # Kernels launched before the headline's timed region (for the ncu
-    # launch-list window): SetStateZero is two kernels, each plan op one.
+    # launch-list window): SetStateZero is two kernels.
     launches_before = 0
+    kernels = {}
     form_steps = max(1, args.steps // 2)
     for name, plan in forms.items():
+        kernels[name] = kernels_per_run(plan)
         results[name] = time_form(plan, form_steps, 1)
-        launches_before += (1 + form_steps) * (len(plan) + 2)
+        launches_before += kernels[name] + (1 + form_steps) * (kernels[name] + 2)
     best = min(results, key=results.get)
     head = forms[best]
-    launches_before += args.warmup * (len(head) + 2)
+    launches_before += args.warmup * (kernels[best] + 2)
 
     # Headline timed region: K steps of the best form.
     head.capture(ctx, st)
@@ -274,7 +285,7 @@ def run_engine(args, world, rank, local, dist):
         ss.SetStateZero(st)
         head.replay(ctx)
     ctx.sync()
-    launches_per_step = len(head) + 2  # plan ops + fill + set-one kernels
+    launches_per_step = kernels[best] + 2  # plan + fill + set-one kernels
     barrier(dist)
     clk = ClockSampler(local)
     ctx.timer_start()
@@ -343,26 +354,28 @@ def run_engine(args, world, rank, local, dist):
     N.lib.qsg_host_free(hbuf)
     e2e = max_over_ranks(dist, statistics.median(e2e_times))
 
-    # Learned planner on the 32-qubit 5x6+2 grid depth-24 circuit (32 GiB).
+    # Learned planner on the 32-qubit 5x6+2 grid depth-24 circuit (32 GiB),
+    # and batched trajectories (replicas for N > 1: every rank runs the
+    # batch): the autotuned configuration, with the stream path alone at
+    # f = 4 (one launch per fused block) beside it.
     del st
-    learned = bench_learned_planner(ctx, ss, model, dist)
-
-    # Batched trajectories (replicas for N > 1: every rank runs the batch).
-    # Headline: one persistent kernel over the packed batch; the stream path
-    # (one launch per fused op, concurrent host threads) is timed beside it.
-    traj = bench_trajectories(args.traj_streams, args.traj_f,
-                              mode=args.traj_mode,
-                              ctas_per_sm=args.traj_ctas_per_sm,
-                              tile_kib=args.traj_tile_kib,
-                              split=args.traj_split)
-    traj["wall_s"] = max_over_ranks(dist, traj["wall_s"])
-    traj["value"] = world * traj["trajectories"] / traj["wall_s"]
-    # The stream path alone at f = 4 (one launch per fused block) beside it.
-    alt = bench_trajectories(args.traj_streams, 4, mode="streams")
-    traj["streams_only"] = {"value": alt["value"], "wall_s": alt["wall_s"],
-                            "latency_ms_p50": alt["latency_ms_p50"],
-                            "latency_ms_p99": alt["latency_ms_p99"],
-                            "gpu_launches": alt["gpu_launches"]}
+    if args.headline_only:
+        learned = {"skipped": "--headline-only"}
+        traj = {"skipped": "--headline-only"}
+    else:
+        learned = bench_learned_planner(ctx, ss, model, dist)
+        traj = bench_trajectories(args.traj_streams, args.traj_f,
+                                  mode=args.traj_mode,
+                                  ctas_per_sm=args.traj_ctas_per_sm,
+                                  tile_kib=args.traj_tile_kib,
+                                  split=args.traj_split)
+        traj["wall_s"] = max_over_ranks(dist, traj["wall_s"])
+        traj["value"] = world * traj["trajectories"] / traj["wall_s"]
+        alt = bench_trajectories(args.traj_streams, 4, mode="streams")
+        traj["streams_only"] = {"value": alt["value"], "wall_s": alt["wall_s"],
+                                "latency_ms_p50": alt["latency_ms_p50"],
+                                "latency_ms_p99": alt["latency_ms_p99"],
+                                "gpu_launches": alt["gpu_launches"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -635,6 +648,8 @@ def main():
     ap.add_argument("--cpu-ops", type=int, default=4,
                     help="fused ops timed on the CPU for the baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the planner and trajectory sections")
     ap.add_argument("--distinct-replicas", action="store_true")
     ap.add_argument("--traj-only", action="store_true",
                     help="run only the batched-trajectory workload")
