@@ -97,7 +97,8 @@ constexpr uint32_t kOffTabWr = kOffTabRd + 32;          // 8 x u32 raw write
 constexpr uint32_t kNumBars = 4 * kNB + 1;
 constexpr uint32_t kOffBar = kOffTabWr + 32;            // mbarriers
 constexpr uint32_t kOffFlag = kOffBar + 8 * kNumBars;   // failure flag
-constexpr uint32_t kOffTmem = kOffFlag + 16;
+constexpr uint32_t kOffNorm = kOffFlag + 16;             // 16 x f64 + carry
+constexpr uint32_t kOffTmem = kOffNorm + 16 * 8 + 16;
 constexpr uint32_t kSmemBytes = kOffTmem + 16;
 
 static_assert(kSmemBytes <= 232448, "shared memory budget");
@@ -130,6 +131,13 @@ struct TcArgs {
   float scale;      // sigma: tile values are split as FP16 after * sigma
   float inv_scale;  // 1 / sigma, applied to D (both powers of two)
   int* error;       // set on a timed-out wait
+  // Norm carry of unitary plans (null: off).  prev: the previous tensor-core
+  // pass's per-CTA (sum |input|^2, sum |output|^2), prev_count CTAs; this
+  // pass scales its input by sqrt(sum in / sum out) of that pass, undoing
+  // the norm its FP32 accumulation lost, and writes its own sums to out.
+  const double* prev;
+  uint32_t prev_count;
+  double* out;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -449,7 +457,26 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     e_m1 = swz_raw(e_m1, g);
     e_m2 = swz_raw(e_m2, g);
-    const float sc = a.scale;
+    // Norm carry: the previous pass's (sum in, sum out), reduced by each
+    // producer warp in the same order (identical results in every warp).
+    float carry = 1.f;
+    if (a.prev) {
+      double pin = 0, pout = 0;
+      for (uint32_t i = lane; i < a.prev_count; i += 32) {
+        pin += a.prev[2 * i];
+        pout += a.prev[2 * i + 1];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        pin += __shfl_xor_sync(0xffffffffu, pin, o);
+        pout += __shfl_xor_sync(0xffffffffu, pout, o);
+      }
+      if (pout > 0) carry = float(sqrt(pin / pout));
+    }
+    const float sc = a.scale * carry;
+    // sum |input|^2 over this thread's items (unscaled): FP32 per tile,
+    // Kahan-compensated FP32 across tiles (FP64 issue is scarce on GB300).
+    float sin_s = 0.f, sin_c = 0.f;
     auto issue_loads = [&](uint64_t t, int stage) {
       if (t < g.num_tiles) {
         const float4* gp = reinterpret_cast<const float4*>(
@@ -476,6 +503,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // members (8 K-elements, one 16-byte core-matrix row) per item.
       const float2* raw = reinterpret_cast<const float2*>(smem + kOffRaw + rs * kTileBytes);
       const uint32_t obuf = kOffOp + s * kOpBytes;
+      float tile_in = 0.f;
 #pragma unroll
       for (int j = 0; j < kSplitPerRole; ++j) {
         const uint32_t e0 = my_se ^ tab_se[j];
@@ -495,6 +523,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           x2 = raw[e0 ^ e_m2];
           x3 = raw[e0 ^ e_m1 ^ e_m2];
         }
+        if (a.out) {
+          tile_in = fmaf(x0.x, x0.x, fmaf(x0.y, x0.y, tile_in));
+          tile_in = fmaf(x1.x, x1.x, fmaf(x1.y, x1.y, tile_in));
+          tile_in = fmaf(x2.x, x2.x, fmaf(x2.y, x2.y, tile_in));
+          tile_in = fmaf(x3.x, x3.x, fmaf(x3.y, x3.y, tile_in));
+        }
         x[0] = x0.x * sc; x[1] = x0.y * sc; x[2] = x1.x * sc; x[3] = x1.y * sc;
         x[4] = x2.x * sc; x[5] = x2.y * sc; x[6] = x3.x * sc; x[7] = x3.y * sc;
         uint4 h, l;
@@ -511,12 +545,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         *reinterpret_cast<uint4*>(smem + obuf + o) = h;
         *reinterpret_cast<uint4*>(smem + obuf + kBImgBytes + o) = l;
       }
+      if (a.out) {
+        const float y = tile_in - sin_c;
+        const float t2 = sin_s + y;
+        sin_c = (t2 - sin_s) - y;
+        sin_s = t2;
+      }
       fence_async_smem();
       bar_sync(1, kProdThreads);
       if (rt == 0) mbar_arrive(&op_full[s]);
       issue_loads(t + kRawStages * step, rs);  // raw[rs] is consumed
     }
     cp_wait<0>();
+    if (a.out) {
+      // The input this pass applies the gate to is carry * input.
+      double sum_in = (double(sin_s) - double(sin_c)) * double(carry) *
+                      double(carry);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        sum_in += __shfl_xor_sync(0xffffffffu, sum_in, o);
+      if (lane == 0)
+        reinterpret_cast<double*>(smem + kOffNorm)[warp] = sum_in;
+    }
   } else if (warp < kProdWarps + kEpiWarps) {
     // ======================== epilogue ===================================
     const uint32_t et = tid - kProdThreads;
@@ -545,6 +595,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t my_rd = swz_out(et << 1, g);
     const uint32_t my_me = swz_out(tile_e(0, row / 2, g), g);
     const float inv = a.inv_scale;
+    // sum |output|^2 over this thread's outputs: FP32 per tile, Kahan FP32
+    // across tiles.
+    float sout_s = 0.f, sout_c = 0.f;
     int i = 0;
     for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
       const int s = i % kNB;
@@ -559,6 +612,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (et == 0) mbar_arrive(&acc_free[s]);  // accumulator s drained
       float2* stage = reinterpret_cast<float2*>(smem + kOffOp + s * kOpBytes);
       const bool odd = lane & 1;
+      float fo = 0.f;
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         // Of this warp's 32 columns, even lanes (re rows) keep the first 16
@@ -570,6 +624,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         const float im = __uint_as_float(odd ? mine : recv) * inv;
         const uint32_t grp = 32 * chalf + (odd ? 16 + j : j);
         stage[my_me ^ tab_ge[grp]] = make_float2(re, im);
+        fo = fmaf(re, re, fmaf(im, im, fo));
+      }
+      {
+        const float y = fo - sout_c;
+        const float t2 = sout_s + y;
+        sout_c = (t2 - sout_s) - y;
+        sout_s = t2;
       }
       bar_sync(2, kEpiThreads);
       const uint64_t base = expand_outer_tc(t, g);
@@ -584,6 +645,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       bar_sync(2, kEpiThreads);
       if (et == 0) mbar_arrive(&op_free[s]);  // operand buffer s free
+    }
+    if (a.out) {
+      double sum_out = double(sout_s) - double(sout_c);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        sum_out += __shfl_xor_sync(0xffffffffu, sum_out, o);
+      if (lane == 0)
+        reinterpret_cast<double*>(smem + kOffNorm)[kProdWarps + ew] = sum_out;
     }
   } else if (lane == 0) {
     // ======================== MMA issuer =================================
@@ -619,6 +688,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   // ---- tear-down -----------------------------------------------------------
   __syncthreads();
+  if (a.out && tid == 0) {
+    const double* nsum = reinterpret_cast<const double*>(smem + kOffNorm);
+    double si = 0, so = 0;
+    for (int w = 0; w < kProdWarps; ++w) si += nsum[w];
+    for (int w = 0; w < kEpiWarps; ++w) so += nsum[kProdWarps + w];
+    a.out[2 * blockIdx.x] = si;
+    a.out[2 * blockIdx.x + 1] = so;
+  }
   if (warp == mma_warp) {
     if (*flag) {
       if (lane == 0) atomicExch(a.error, 1);
@@ -797,8 +874,27 @@ int tc_setup() {
   return QSG_OK;
 }
 
+unsigned tc_grid(qsg_ctx* ctx, unsigned n) {
+  if (n < unsigned(tc::kTileBits)) return 0;
+  const uint64_t tiles = uint64_t{1} << (n - tc::kTileBits);
+  return unsigned(std::min<uint64_t>(tiles, uint64_t(ctx->num_sms)));
+}
+
+int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
+                        const unsigned* qs, unsigned k, const float* m32,
+                        const void* operands, const double* prev,
+                        unsigned prev_count, double* out);
+
 int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
                   unsigned k, const float* m32, const void* operands) {
+  return apply_gate_tc_carry(ctx, state, n, qs, k, m32, operands, nullptr, 0,
+                             nullptr);
+}
+
+int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
+                        const unsigned* qs, unsigned k, const float* m32,
+                        const void* operands, const double* prev,
+                        unsigned prev_count, double* out) {
   using namespace tc;
   if (k != kK) {
     set_error("tensor-core gates are planned with 6 targets (got %u)", k);
@@ -824,6 +920,9 @@ int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
   int rc0 = tc_setup();
   if (rc0) return rc0;
   a.error = g_tc_err;
+  a.prev = prev;
+  a.prev_count = prev ? prev_count : 0;
+  a.out = out;
   const uint64_t grid = std::min<uint64_t>(a.g.num_tiles, ctx->num_sms);
   tc_gate_kernel<<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
       reinterpret_cast<float2*>(state), a);

@@ -175,22 +175,28 @@ int PlanRuntime::launch_op(size_t i, float* state) {
 
 int PlanRuntime::launch_all(float* state) {
   const unsigned n = plan.num_qubits;
-  double* before = norm_buf;
-  double* after = norm_buf ? norm_buf + size_t(traj_max_parts(ctx)) * 4 : nullptr;
-  unsigned nb = 0, na = 0;
-  int rc;
-  if (restore_norm) {
-    rc = traj_channel_stats(ctx, state, n, 0, nullptr, before, &nb);
-    if (rc) return rc;
-  }
+  // Unitary tensor-core plans carry the norm from pass to pass: each
+  // tensor-core pass writes its (sum in, sum out) partials into one half of
+  // norm_buf and rescales its input by the previous pass's ratio, read from
+  // the other half.
+  const size_t half = size_t(traj_max_parts(ctx)) * 4;
+  const double* prev = nullptr;
+  unsigned prev_count = 0;
+  int which = 0;
   for (size_t i = 0; i < plan.ops.size(); ++i) {
-    rc = launch_op(i, state);
-    if (rc) return rc;
-  }
-  if (restore_norm) {
-    rc = traj_channel_stats(ctx, state, n, 0, nullptr, after, &na);
-    if (rc) return rc;
-    rc = norm_restore(ctx, state, n, before, nb, after, na);
+    const PlanOp& op = plan.ops[i];
+    int rc;
+    if (restore_norm && op.kind == OpKind::kGate && op.path == Path::kTensor) {
+      double* out = norm_buf + which * half;
+      rc = apply_gate_tc_carry(ctx, state, n, op.qs.data(), op.qs.size(),
+                               op.m32.data(), tc_operands(i), prev, prev_count,
+                               out);
+      prev = out;
+      prev_count = tc_grid(ctx, n);
+      which ^= 1;
+    } else {
+      rc = launch_op(i, state);
+    }
     if (rc) return rc;
   }
   return QSG_OK;

@@ -13,6 +13,16 @@ namespace qsg {
 // the device operands built by tc_build_operands.  Defined in tc_gate.cu.
 int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
                   unsigned k, const float* m32, const void* operands);
+// The same with the norm carry of unitary plans: `prev` (null for the first
+// tensor-core pass) holds the previous pass's per-CTA (sum |in|^2,
+// sum |out|^2) from `prev_count` CTAs, whose ratio rescales this pass's
+// input; this pass writes its own sums to `out` (tc_grid(n) pairs).
+int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
+                        const unsigned* qs, unsigned k, const float* m32,
+                        const void* operands, const double* prev,
+                        unsigned prev_count, double* out);
+// CTAs of a tensor-core pass on n qubits.
+unsigned tc_grid(qsg_ctx* ctx, unsigned n);
 // Size in bytes of the device operands of a k-qubit tensor-core gate, and
 // their construction from the interleaved FP32 matrix.
 size_t tc_operand_bytes(unsigned k);
@@ -40,12 +50,13 @@ struct PlanRuntime {
   void* graph_exec = nullptr;        // cudaGraphExec_t
   float* captured_state = nullptr;
   int device = -1;                   // device of dmat / tc_buf / norm_buf
-  // Tensor-core plans of unitary gates rescale the state to its input norm
-  // after the last launch: the tensor cores' FP32 accumulation rounds
-  // toward zero and shrinks the norm by ~6e-7 per pass.
+  // Tensor-core plans of unitary gates keep the norm: the tensor cores'
+  // FP32 accumulation rounds toward zero and shrinks the norm by ~6e-7 per
+  // pass, so each tensor-core pass rescales its input by the norm ratio the
+  // previous one measured (only the last pass's loss remains).
   bool restore_norm = false;
   bool uploaded = false;
-  double* norm_buf = nullptr;        // two sets of norm partials
+  double* norm_buf = nullptr;        // two sets of per-CTA norm sums
 
   PlanRuntime() = default;
   PlanRuntime(const PlanRuntime&) = delete;
