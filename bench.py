@@ -338,7 +338,7 @@ def run_engine(args, world, rank, local, dist):
     N.check(N.lib.qsg_host_alloc(nbytes_state, C.byref(hbuf)))
     samples = np.zeros(1000, dtype=np.uint64)
     h2d = sum(8 * (1 << (2 * len(o["qs"]))) for o in head.ops())
-    e2e_times = []
+    e2e_times, phases = [], []
     for i in range(args.warmup + args.steps):
         ctx.sync()
         barrier(dist)
@@ -347,12 +347,17 @@ def run_engine(args, world, rank, local, dist):
         head.run(ctx, st)
         N.check(N.lib.qsg_sample(ctx.h, st.get(), n, 1000, 1,
                                  samples.ctypes.data_as(N.P_u64)))
+        t1 = time.perf_counter()   # the samples synchronise the stream
         N.check(N.lib.qsg_copy_d2h(ctx.h, hbuf, st.get(), n))
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_times.append(dt)
+            phases.append((t1 - t0, dt - (t1 - t0)))
     N.lib.qsg_host_free(hbuf)
     e2e = max_over_ranks(dist, statistics.median(e2e_times))
+    e2e_phase = {"run_and_sample_s": statistics.median(p[0] for p in phases),
+                 "state_d2h_s": statistics.median(p[1] for p in phases)}
+    e2e_phase["d2h_gbs"] = nbytes_state / e2e_phase["state_d2h_s"] / 1e9
 
     # Learned planner on the 32-qubit 5x6+2 grid depth-24 circuit (32 GiB),
     # and batched trajectories (replicas for N > 1: every rank runs the
@@ -362,8 +367,10 @@ def run_engine(args, world, rank, local, dist):
     if args.headline_only:
         learned = {"skipped": "--headline-only"}
         traj = {"skipped": "--headline-only"}
+        expect = {"skipped": "--headline-only"}
     else:
         learned = bench_learned_planner(ctx, ss, model, dist)
+        expect = bench_expectations(ctx, ss, dist)
         traj = bench_trajectories(args.traj_streams, args.traj_f,
                                   mode=args.traj_mode,
                                   ctas_per_sm=args.traj_ctas_per_sm,
@@ -403,15 +410,86 @@ def run_engine(args, world, rank, local, dist):
                                       "count": launches_per_step * args.steps},
                        "passes": {k: len(v) for k, v in forms.items()}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": nbytes_state + 8 * 1000},
+                    "d2h_bytes_per_step": nbytes_state + 8 * 1000,
+                    "phases": e2e_phase},
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "trajectories": traj,
             "learned_planner": learned,
+            "expectations": expect,
         }
         print(json.dumps(line), flush=True)
+
+
+EXPECT = dict(n=28, layers=40, controlled=8, seed=3, strings=64, weight=6,
+              pauli_seed=5)
+
+
+def bench_expectations(ctx, ss, dist):
+    """28-qubit layered circuit (U3 on every qubit, CZ/CNOT on random
+    disjoint pairs, 8 gates with 1-2 controls per layer, 40 layers) and 64
+    Pauli strings of weight 1..6: seconds per circuit run (plain f = 4 plan
+    from a CUDA graph) and per expectation value, on the one-pass monomial
+    kernel and, for comparison, on the dense tile kernel (the same operator
+    with one off-pattern entry of 1e-30, which the monomial test rejects)."""
+    import numpy as np
+    from qsim_gb300 import engine as E
+    import qsim_gb300 as q
+    sim = q.Simulator(ctx=ctx)
+    paulis = {"I": np.eye(2), "X": np.array([[0, 1], [1, 0]]),
+              "Y": np.array([[0, -1j], [1j, 0]]), "Z": np.diag([1, -1])}
+
+    def pauli_matrix(letters):
+        # letters[j] acts on the string's j-th (sorted) qubit = index bit j.
+        m = np.eye(1, dtype=np.complex128)
+        for p in letters:
+            m = np.kron(paulis[p], m)
+        return m
+
+    c = E.Circuit.layered_u3(EXPECT["n"], EXPECT["layers"], EXPECT["controlled"],
+                             EXPECT["seed"])
+    n = c.num_qubits
+    st = ss.Create(n)
+    plan = E.Plan(c, max_fused_size=4)
+    plan.capture(ctx, st)
+    ss.SetStateZero(st)
+    plan.replay(ctx)
+    ctx.sync()
+    barrier(dist)
+    ctx.timer_start()
+    ss.SetStateZero(st)
+    plan.replay(ctx)
+    circuit_s = max_over_ranks(dist, ctx.timer_stop() / 1e3)
+    strings = E.pauli_sum(n, EXPECT["strings"], EXPECT["weight"],
+                          EXPECT["pauli_seed"])
+    mats = []
+    for qs, letters, coeff in strings:
+        m = np.ascontiguousarray(pauli_matrix(letters).astype(np.complex64))
+        md = m.copy()
+        md[0, int(np.flatnonzero(m[0] == 0)[0])] += np.complex64(1e-30)
+        mats.append((qs, coeff, m.view(np.float32), md.view(np.float32)))
+    out = {}
+    for name, idx in (("monomial", 2), ("dense", 3)):
+        for qs, _, *mm in mats[:2]:
+            sim.ExpectationValue(qs, mm[idx - 2], st)   # warm-up
+        ctx.sync()
+        t0 = time.perf_counter()
+        total = 0.0
+        for qs, coeff, *mm in mats:
+            total += coeff * sim.ExpectationValue(qs, mm[idx - 2], st).real
+        dt = time.perf_counter() - t0
+        out[name] = {"s_per_ev": dt / len(mats), "pauli_sum": total,
+                     "gbs": 8.0 * (1 << n) / (dt / len(mats)) / 1e9}
+    return {
+        "workload": f"layered U3 ({n} qubits) 40 layers, 8 controlled gates "
+                    f"per layer, seed 3; {len(mats)} Pauli strings of weight "
+                    "1..6",
+        "circuit_s_per_run": circuit_s, "passes": len(plan),
+        "ev": out,
+        "ev_speedup": out["dense"]["s_per_ev"] / out["monomial"]["s_per_ev"],
+    }
 
 
 LEARN_GRID = dict(rows=5, cols=6, extra=2, cycles=24, seed=1)

@@ -1,0 +1,188 @@
+// ExpectationValue of monomial operators in one read pass.
+//
+// The reference evaluates <psi|M|psi> with the dense 2^k x 2^k matrix
+// (ExpectationValueH/L_Kernel, lib/simulator_cuda_kernels.h:482-693), also
+// for the Pauli strings that lib/expect.h:105-151 fuses into <= 6-qubit
+// gates.  A Pauli string (and any product of Pauli and diagonal gates) has
+// one nonzero per row, at column r ^ xm: M psi at index i is d[r(i)] times
+// psi at i ^ X, where r(i) are the bits of i on the target qubits and X is
+// xm spread onto them.  So
+//
+//   <psi|M|psi> = sum_i conj(psi_i) d[r(i)] psi_(i ^ X),
+//
+// a bandwidth-bound pass: each thread reads a 16-byte unit (two amplitudes)
+// and, when X flips qubits above qubit 0, its partner unit, and adds both
+// units' terms, so every amplitude is read once (8 N bytes).  Products are
+// FP32; partial sums FP32 over a thread's units of one step, FP64 across
+// steps and threads, as in the other reductions here.
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+#include "internal.h"
+#include "matring.cuh"
+
+namespace qsg {
+
+namespace {
+
+constexpr int kEvThreads = 256;
+constexpr int kEvUnroll = 4;
+
+struct MonoArgs {
+  float2 d[64];        // d[r] = M[r][r ^ xm]
+  uint32_t qpos[6];    // target qubits (bit j of r <-> qpos[j])
+  uint32_t k;
+  uint32_t x0;         // bit 0 of X (qubit 0 flipped)
+  uint64_t ux;         // X >> 1: partner unit offset (0: the unit itself)
+  uint32_t ub;         // lowest set bit of ux (when ux != 0)
+};
+
+__device__ __forceinline__ uint32_t row_of(uint64_t i, const MonoArgs& a) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+    if (j < int(a.k)) r |= uint32_t((i >> a.qpos[j]) & 1) << j;
+  return r;
+}
+
+// conj(p) * d * q, FP32.
+__device__ __forceinline__ void term(float& er, float& ei, float2 p, float2 d,
+                                     float2 q) {
+  const float tr = d.x * q.x - d.y * q.y;
+  const float ti = d.x * q.y + d.y * q.x;
+  er = fmaf(p.x, tr, fmaf(p.y, ti, er));
+  ei = fmaf(p.x, ti, fmaf(-p.y, tr, ei));
+}
+
+__global__ void __launch_bounds__(kEvThreads)
+    mono_ev_kernel(const float4* __restrict__ s, uint64_t work,
+                   const __grid_constant__ MonoArgs a,
+                   double2* __restrict__ partial) {
+  double ar = 0, ai = 0;
+  const uint64_t tile = uint64_t(kEvThreads) * kEvUnroll;
+  for (uint64_t b0 = blockIdx.x * tile; b0 < work;
+       b0 += uint64_t(gridDim.x) * tile) {
+    float4 x[kEvUnroll], y[kEvUnroll];
+    uint64_t u[kEvUnroll];
+#pragma unroll
+    for (int j = 0; j < kEvUnroll; ++j) {
+      const uint64_t w = b0 + j * kEvThreads + threadIdx.x;
+      // Work item w -> unit u with bit ub of u clear (ux != 0), or u = w.
+      uint64_t uu = w;
+      if (a.ux) {
+        const uint64_t lo = w & ((uint64_t{1} << a.ub) - 1);
+        uu = lo | ((w ^ lo) << 1);
+      }
+      u[j] = uu;
+      x[j] = w < work ? s[uu] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (a.ux)
+        y[j] = w < work ? s[uu ^ a.ux] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float fr = 0.f, fi = 0.f;
+#pragma unroll
+    for (int j = 0; j < kEvUnroll; ++j) {
+      const uint64_t w = b0 + j * kEvThreads + threadIdx.x;
+      if (w >= work) continue;
+      const uint64_t i0 = 2 * u[j];
+      const float2 p0 = make_float2(x[j].x, x[j].y);
+      const float2 p1 = make_float2(x[j].z, x[j].w);
+      if (a.ux == 0) {
+        // Partner of amplitude i0 + t is i0 + (t ^ x0), in the same unit.
+        const float2 q0 = a.x0 ? p1 : p0, q1 = a.x0 ? p0 : p1;
+        term(fr, fi, p0, a.d[row_of(i0, a)], q0);
+        term(fr, fi, p1, a.d[row_of(i0 + 1, a)], q1);
+      } else {
+        const uint64_t k0 = 2 * (u[j] ^ a.ux);
+        const float2 r0 = make_float2(y[j].x, y[j].y);
+        const float2 r1 = make_float2(y[j].z, y[j].w);
+        const float2 q0 = a.x0 ? r1 : r0, q1 = a.x0 ? r0 : r1;
+        const float2 v0 = a.x0 ? p1 : p0, v1 = a.x0 ? p0 : p1;
+        term(fr, fi, p0, a.d[row_of(i0, a)], q0);
+        term(fr, fi, p1, a.d[row_of(i0 + 1, a)], q1);
+        term(fr, fi, r0, a.d[row_of(k0, a)], v0);
+        term(fr, fi, r1, a.d[row_of(k0 + 1, a)], v1);
+      }
+    }
+    ar += double(fr);
+    ai += double(fi);
+  }
+  __shared__ double red[2][kEvThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, o);
+    ai += __shfl_down_sync(0xffffffffu, ai, o);
+  }
+  if (threadIdx.x % 32 == 0) {
+    red[0][threadIdx.x / 32] = ar;
+    red[1][threadIdx.x / 32] = ai;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sr = 0, si = 0;
+    for (int i = 0; i < kEvThreads / 32; ++i) {
+      sr += red[0][i];
+      si += red[1][i];
+    }
+    partial[blockIdx.x] = make_double2(sr, si);
+  }
+}
+
+}  // namespace
+
+bool monomial_xor(unsigned k, const float* m, uint32_t* xm, float* d) {
+  const unsigned dim = 1u << k;
+  for (unsigned r = 0; r < dim; ++r) {
+    int col = -1;
+    for (unsigned c = 0; c < dim; ++c) {
+      const float re = m[2 * (r * dim + c)], im = m[2 * (r * dim + c) + 1];
+      if (re != 0.f || im != 0.f) {
+        if (col >= 0) return false;
+        col = int(c);
+      }
+    }
+    // An all-zero row fits any pattern: take the one row 0 fixed.
+    const uint32_t x = col < 0 ? (r == 0 ? 0u : *xm) : uint32_t(col) ^ r;
+    if (r == 0) *xm = x;
+    else if (x != *xm) return false;
+    d[2 * r] = col < 0 ? 0.f : m[2 * (r * dim + col)];
+    d[2 * r + 1] = col < 0 ? 0.f : m[2 * (r * dim + col) + 1];
+  }
+  return true;
+}
+
+int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
+                         const unsigned* qs, unsigned k, uint32_t xm,
+                         const float* d, double* out_re_im) {
+  QSG_CHECK_ARG(k >= 1 && k <= 6 && n >= 1, "monomial EV: bad sizes");
+  MonoArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.k = k;
+  uint64_t X = 0;
+  for (unsigned j = 0; j < k; ++j) {
+    a.qpos[j] = qs[j];
+    if ((xm >> j) & 1) X |= uint64_t{1} << qs[j];
+  }
+  for (unsigned r = 0; r < (1u << k); ++r)
+    a.d[r] = make_float2(d[2 * r], d[2 * r + 1]);
+  a.x0 = uint32_t(X & 1);
+  a.ux = X >> 1;
+  a.ub = a.ux ? unsigned(__builtin_ctzll(a.ux)) : 0;
+  const uint64_t units = n == 0 ? 1 : (uint64_t{1} << (n - 1));
+  const uint64_t work = a.ux ? units / 2 : units;
+  const uint64_t per_block = uint64_t(kEvThreads) * kEvUnroll;
+  uint64_t grid = (work + per_block - 1) / per_block;
+  grid = std::min<uint64_t>(grid, uint64_t(ctx->num_sms) * 8);
+  if (grid < 1) grid = 1;
+  void* p = nullptr;
+  int rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
+  if (rc) return rc;
+  double2* partial = static_cast<double2*>(p);
+  mono_ev_kernel<<<unsigned(grid), kEvThreads, 0, ctx->stream>>>(
+      reinterpret_cast<const float4*>(state), work, a, partial);
+  QSG_LAUNCHED(ctx);
+  return reduce_partials_d2(ctx, partial, grid, out_re_im);
+}
+
+}  // namespace qsg

@@ -300,6 +300,11 @@ int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
     return QSG_ERR_UNSUPPORTED;
   }
   QSG_CHECK_ARG(valid_qubits(qs, k, n), "qsg_expectation_value: bad qs");
+  // Pauli strings and other monomial operators: one read pass.
+  uint32_t xm = 0;
+  float d[2 * 64];
+  if (monomial_xor(k, matrix, &xm, d))
+    return expectation_monomial(ctx, state, n, qs, k, xm, d, out_re_im);
   return dispatch<1>(ctx, const_cast<float*>(state), n, qs, k, nullptr, 0, 0,
                      matrix, out_re_im);
 }
