@@ -216,13 +216,29 @@ __global__ void __launch_bounds__(kScanThreads)
     chunk_sum_kernel(const float2* __restrict__ s, uint32_t cb,
                      uint64_t nchunks, double* __restrict__ out) {
   __shared__ double red[kScanThreads / 32];
-  const uint32_t camps = 1u << cb;
+  // 16-byte units (two amplitudes), all of a thread's units of a chunk in
+  // flight at once (16 for a full 2^13-amplitude chunk).
+  constexpr int kU = kChunkAmps / 2 / kScanThreads;
+  const uint32_t units = cb == 0 ? 1 : (1u << (cb - 1));
   for (uint64_t m = blockIdx.x; m < nchunks; m += gridDim.x) {
-    const float2* c = s + (m << cb);
     float f = 0.f;
-    for (uint32_t i = threadIdx.x; i < camps; i += kScanThreads) {
-      float2 a = c[i];
-      f += fmaf(a.x, a.x, a.y * a.y);
+    if (cb == 0) {
+      if (threadIdx.x == 0) {
+        const float2 a = s[m];
+        f = fmaf(a.x, a.x, a.y * a.y);
+      }
+    } else {
+      const float4* c = reinterpret_cast<const float4*>(s + (m << cb));
+      float4 v[kU];
+#pragma unroll
+      for (int j = 0; j < kU; ++j) {
+        const uint32_t i = threadIdx.x + j * kScanThreads;
+        v[j] = i < units ? c[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int j = 0; j < kU; ++j)
+        f += fmaf(v[j].x, v[j].x, v[j].y * v[j].y) +
+             fmaf(v[j].z, v[j].z, v[j].w * v[j].w);
     }
     double d = f;
     for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
@@ -373,29 +389,57 @@ __device__ __forceinline__ uint64_t lower_bound_d(const double* r, uint64_t m,
   return lo;
 }
 
-// Resolves the samples that fall into each chunk.  Sample j belongs to
-// chunk c iff incl[c-1] <= r[j] < incl[c]; inside the chunk its index is the
-// first k with r[j] < incl[c-1] + CDF(k).  Samples with r[j] >= incl[last]
-// get 2^n - 1 (lib/statespace_basic.h:222-224).
+// Sample j belongs to chunk c iff incl[c-1] <= r[j] < incl[c], i.e. c is
+// the first chunk with r[j] < incl[c] (nchunks if none: the sample gets
+// 2^n - 1, lib/statespace_basic.h:222-224).  One thread per sample.
+__global__ void sample_locate_kernel(const double* __restrict__ incl,
+                                     uint64_t nchunks,
+                                     const double* __restrict__ r, uint64_t m,
+                                     uint32_t* __restrict__ chunk_of) {
+  for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < m;
+       j += uint64_t(gridDim.x) * blockDim.x) {
+    const double x = r[j];
+    uint64_t lo = 0, hi = nchunks;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) / 2;
+      if (x < incl[mid]) hi = mid; else lo = mid + 1;
+    }
+    chunk_of[j] = uint32_t(lo);
+  }
+}
+
+// One CTA per sample; the CTA of the first sample of each chunk's run (the
+// samples are sorted, so a chunk's samples are consecutive) builds that
+// chunk's CDF and resolves the whole run: inside the chunk a sample's index
+// is the first k with r[j] < incl[c-1] + CDF(k).  Only chunks that hold
+// samples are read.
 __global__ void __launch_bounds__(kScanThreads)
-    sample_chunk_kernel(const float2* __restrict__ s, uint32_t cb,
-                        uint64_t nchunks, const double* __restrict__ incl,
-                        const double* __restrict__ r, uint64_t m,
-                        uint64_t last_index, uint64_t* __restrict__ out) {
+    sample_resolve_kernel(const float2* __restrict__ s, uint32_t cb,
+                          uint64_t nchunks, const double* __restrict__ incl,
+                          const double* __restrict__ r, uint64_t m,
+                          const uint32_t* __restrict__ chunk_of,
+                          uint64_t last_index, uint64_t* __restrict__ out) {
   __shared__ float p[kPadAmps];
   __shared__ double seg[kScanThreads + 1];
-  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const uint64_t lo = c == 0 ? 0 : lower_bound_d(r, m, incl[c - 1]);
-    const uint64_t hi = lower_bound_d(r, m, incl[c]);
-    if (c == nchunks - 1) {
-      for (uint64_t j = hi + threadIdx.x; j < m; j += blockDim.x)
-        out[j] = last_index;
+  for (uint64_t j = blockIdx.x; j < m; j += gridDim.x) {
+    const uint32_t c = chunk_of[j];
+    if (j > 0 && chunk_of[j - 1] == c) continue;  // uniform across the block
+    // End of the run: first j' > j with chunk_of[j'] != c.
+    uint64_t lo = j + 1, hi = m;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) / 2;
+      if (chunk_of[mid] == c) lo = mid + 1; else hi = mid;
     }
-    if (lo >= hi) continue;  // uniform across the block
+    const uint64_t end = lo;
+    if (c >= nchunks) {
+      for (uint64_t t = j + threadIdx.x; t < end; t += blockDim.x)
+        out[t] = last_index;
+      continue;
+    }
     chunk_cdf_build(s, cb, c, p, seg);
     const double base = c == 0 ? 0.0 : incl[c - 1];
-    for (uint64_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
-      out[j] = (c << cb) + chunk_cdf_find(p, seg, 1u << cb, base, r[j]);
+    for (uint64_t t = j + threadIdx.x; t < end; t += blockDim.x)
+      out[t] = (uint64_t(c) << cb) + chunk_cdf_find(p, seg, 1u << cb, base, r[t]);
     __syncthreads();
   }
 }
@@ -797,21 +841,26 @@ int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
   const size_t ubytes = num_samples * sizeof(double);
   double *sums, *incl;
   void* extra = nullptr;
-  int rc = chunk_prefix(ctx, state, n, 2 * ubytes + num_samples * 8 + 64,
+  int rc = chunk_prefix(ctx, state, n,
+                        2 * ubytes + num_samples * 8 + num_samples * 4 + 64,
                         &sums, &incl, &extra);
   if (rc) return rc;
   double* du = static_cast<double*>(extra);
   double* dr = du + num_samples;
   uint64_t* dout = reinterpret_cast<uint64_t*>(dr + num_samples);
+  uint32_t* dchunk = reinterpret_cast<uint32_t*>(dout + num_samples);
   QSG_CUDA(cudaMemcpyAsync(du, sorted_u, ubytes, cudaMemcpyHostToDevice,
                            ctx->stream));
   scale_uniforms_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
                           ctx->stream>>>(du, num_samples, incl, nc, dr);
   QSG_LAUNCHED(ctx);
-  const unsigned grid = (unsigned)std::min<uint64_t>(nc, ctx->num_sms * 8ull);
-  sample_chunk_kernel<<<grid, kScanThreads, 0, ctx->stream>>>(
+  sample_locate_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
+                         ctx->stream>>>(incl, nc, dr, num_samples, dchunk);
+  QSG_LAUNCHED(ctx);
+  const unsigned grid = (unsigned)std::min<uint64_t>(num_samples, 1u << 20);
+  sample_resolve_kernel<<<grid, kScanThreads, 0, ctx->stream>>>(
       reinterpret_cast<const float2*>(state), cb, nc, incl, dr, num_samples,
-      (uint64_t{1} << n) - 1, dout);
+      dchunk, (uint64_t{1} << n) - 1, dout);
   QSG_LAUNCHED(ctx);
   QSG_CUDA(cudaMemcpyAsync(out_bitstrings, dout, num_samples * 8,
                            cudaMemcpyDeviceToHost, ctx->stream));
