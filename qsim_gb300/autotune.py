@@ -8,8 +8,11 @@ fused block, several host threads), or both at once with the circuits split
 by qubit count.  The tuner times candidate configurations on a sample of
 the batch and keeps the one with the most trajectories per second:
 
-  * the stream path's form: fusion block size k (3 or 4 on CUDA cores, or
-    6 with blocks of >= 5 qubits on the tensor cores);
+  * the stream path's form: fusion block size k (3 or 4 on CUDA cores),
+    and ``tc_from``: circuits of at least that many qubits fuse at k = 6
+    with blocks of >= 5 qubits on the tensor cores (a tensor-core pass
+    needs 4096-amplitude tiles on every SM to pay off, so small circuits
+    stay on CUDA cores);
   * ``split``: the largest qubit count sent to the persistent kernel (whose
     runners fuse at k = 4 on CUDA cores); the rest run concurrently on the
     stream path;
@@ -87,31 +90,48 @@ FORMS = ((3, False), (4, False), (6, True))
 
 
 def candidates(max_n: int, forms=FORMS):
-    """Configurations tried: each stream-path form alone, all circuits in the
-    persistent kernel, and splits by qubit count with both running at
-    once."""
+    """Configurations tried: each CUDA-core stream form alone or with the
+    largest circuits on the tensor cores (tc_from), with or without the
+    small circuits in the persistent kernel (split), and all circuits in the
+    persistent kernel.  forms: (k, tensor) pairs; a tensor form enables the
+    tc_from tiers."""
+    cuda_fs = [f for f, tc in forms if not tc]
+    tc_ok = any(tc for _, tc in forms)
+    tc_froms = [0] + ([t for t in (20, 22, 24) if t <= max_n] if tc_ok else [])
+    splits = [0] + [t for t in (14, 16) if t < max_n]
     out = []
-    for f, tc in forms:
-        base = dict(max_fused_size=f, tensor=tc)
-        out.append(dict(base, split=0, ctas_per_sm=0, tile_kib=0))
-        for split in (14, 16, 18, 20):
-            if split >= max_n:
-                continue
-            for per_sm in (1, 2):
-                out.append(dict(base, split=split, ctas_per_sm=per_sm,
-                                tile_kib=32))
-    out.append(dict(max_fused_size=4, tensor=False, split=max_n,
+    for f in cuda_fs or [4]:
+        for tc_from in tc_froms:
+            for split in splits:
+                for per_sm in ((1, 2) if split else (0,)):
+                    out.append(dict(max_fused_size=f, tensor=False,
+                                    tc_from=tc_from, split=split,
+                                    ctas_per_sm=per_sm,
+                                    tile_kib=32 if split else 0))
+    out.append(dict(max_fused_size=4, tensor=False, tc_from=0, split=max_n,
                     ctas_per_sm=2, tile_kib=32))
     return out
 
 
 def runners_for(make_runners, qubits, cfg):
     """Per circuit: the packed kernel's runner (k = 4, CUDA cores) for
-    circuits of at most cfg["split"] qubits, the stream form's otherwise."""
+    circuits of at most cfg["split"] qubits, a tensor-core runner (k = 6)
+    for circuits of at least cfg["tc_from"] qubits (0: none), the stream
+    form's otherwise."""
     packed = make_runners(4, False)
     other = make_runners(cfg["max_fused_size"], cfg.get("tensor", False))
-    return [packed[i] if int(n) <= cfg["split"] else other[i]
-            for i, n in enumerate(qubits)]
+    tc_from = cfg.get("tc_from", 0)
+    tcr = make_runners(6, True) if tc_from else None
+    out = []
+    for i, n in enumerate(qubits):
+        n = int(n)
+        if tc_from and n >= tc_from and n > cfg["split"]:
+            out.append(tcr[i])
+        elif n <= cfg["split"]:
+            out.append(packed[i])
+        else:
+            out.append(other[i])
+    return out
 
 
 def run(runners, items, cfg, num_streams: int = 8, out_states=None):

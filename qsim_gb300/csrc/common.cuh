@@ -79,6 +79,16 @@ struct qsg_ctx {
   // Device operands of single tensor-core gate calls.
   void* tc_slot = nullptr;
   size_t tc_slot_size = 0;
+
+  // Ring of tensor-core operand slots (64 KiB each) for gates whose operands
+  // are built on the host per call, fed asynchronously from pinned staging
+  // slots guarded by events.
+  static constexpr int kTcRingSlots = 8;
+  unsigned char* tc_ring_dev = nullptr;
+  unsigned char* tc_ring_host = nullptr;
+  cudaEvent_t tc_ring_ev[kTcRingSlots] = {};
+  bool tc_ring_used[kTcRingSlots] = {};
+  int tc_ring_next = 0;
 };
 
 namespace qsg {

@@ -167,6 +167,7 @@ int qsg_ctx_destroy(qsg_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   matring_release(ctx);
+  tcring_release(ctx);
   if (ctx->scratch) cudaFree(ctx->scratch);
   if (ctx->tc_slot) cudaFree(ctx->tc_slot);
   if (ctx->hscratch) cudaFreeHost(ctx->hscratch);

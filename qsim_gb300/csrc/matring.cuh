@@ -19,5 +19,7 @@ int reduce_partials_d2(qsg_ctx* ctx, const double2* partial, uint64_t count,
 
 // Releases the ring buffers of a context.
 void matring_release(qsg_ctx* ctx);
+// Releases the tensor-core operand ring of a context (tc_gate.cu).
+void tcring_release(qsg_ctx* ctx);
 
 }  // namespace qsg

@@ -69,7 +69,9 @@ constexpr int kGroups = 64;            // N
 constexpr int kTileBits = 12;          // 64 groups x 64 members
 constexpr int kTileAmps = 1 << kTileBits;
 constexpr uint32_t kAWords = kReal / 2;                 // FP16 pairs per A row
-constexpr uint32_t kOperandBytes = 2 * kReal * kAWords * 4;  // A_hi | A_lo
+// Operands in memory: the padded 64 x 64 complex FP32 gate, row-major
+// interleaved; the kernel converts it to the FP16 A images itself.
+constexpr uint32_t kOperandBytes = kD * kD * 8;          // 32 KiB
 constexpr uint32_t kTileBytes = kTileAmps * 8;           // 32 KiB
 constexpr uint32_t kLBO = 128;                           // K-adjacent cores
 constexpr uint32_t kSBOB = (kReal / 8) * 128;            // 2 KiB
@@ -125,9 +127,8 @@ struct TcGeom {
 
 struct TcArgs {
   TcGeom g;
-  // A_hi | A_lo: 128 rows x 64 words each, a word holding the FP16 values of
-  // columns 2w (low half) and 2w + 1 (high half).
-  const uint32_t* operands;
+  // The padded 6-qubit gate, 64 x 64 complex FP32, row-major interleaved.
+  const float2* operands;
   float scale;      // sigma: tile values are split as FP16 after * sigma
   float inv_scale;  // 1 / sigma, applied to D (both powers of two)
   int* error;       // set on a timed-out wait
@@ -575,17 +576,26 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = (32 * quad) << 16;
     const uint32_t row = 32 * quad + lane;
     // Gate into tensor memory: rows of this quadrant, columns of this half
-    // (A_hi and A_lo, 64 columns of FP16 pairs each).
+    // (A_hi and A_lo, 64 columns of FP16 pairs each).  Row 2r + pr of the
+    // real form [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im); word w
+    // holds columns 2w, 2w + 1, i.e. (Mr, -Mi) or (Mi, Mr) of M[r][w], split
+    // into FP16 hi and lo parts.
     {
-      const uint32_t* ahi = a.operands + size_t(row) * kAWords + 32 * chalf;
-      const uint32_t* alo = ahi + size_t(kReal) * kAWords;
-      uint32_t r[32];
+      const float2* mrow = a.operands + size_t(row / 2) * kD + 32 * chalf;
+      const bool im_row = row & 1;
+      uint32_t hw[32], lw[32];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) r[q] = ahi[q];
-      tmem_st32(tmem + lane_base + kTmemAhi + 32 * chalf, r);
-#pragma unroll
-      for (int q = 0; q < 32; ++q) r[q] = alo[q];
-      tmem_st32(tmem + lane_base + kTmemAlo + 32 * chalf, r);
+      for (int q = 0; q < 32; ++q) {
+        const float2 m = mrow[q];
+        const float x0 = im_row ? m.y : m.x;
+        const float x1 = im_row ? m.x : -m.y;
+        const __half2 h = __floats2half2_rn(x0, x1);
+        const float2 hf = __half22float2(h);
+        hw[q] = *reinterpret_cast<const uint32_t*>(&h);
+        lw[q] = pack_half2(x0 - hf.x, x1 - hf.y);
+      }
+      tmem_st32(tmem + lane_base + kTmemAhi + 32 * chalf, hw);
+      tmem_st32(tmem + lane_base + kTmemAlo + 32 * chalf, lw);
       tmem_wait_st();
       tc_fence_before();
       bar_sync(2, kEpiThreads);
@@ -744,28 +754,6 @@ static void pad_to_6(unsigned n, const unsigned* qs, unsigned k,
   for (unsigned j = 0; j < 6; ++j) qs6[j] = all[j];
 }
 
-// A_real (hi, lo) as FP16 pairs: 128 rows x 64 words each; row 2r+pr,
-// column 2c+pc of [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im);
-// word w of a row holds columns 2w (low half) and 2w + 1.
-static void build_a_images(const float* m6, unsigned char* out) {
-  uint16_t* hi = reinterpret_cast<uint16_t*>(out);
-  uint16_t* lo = hi + kReal * kReal;
-  for (uint32_t r = 0; r < kD; ++r)
-    for (uint32_t c = 0; c < kD; ++c) {
-      const float mr = m6[2 * (r * kD + c)], mi = m6[2 * (r * kD + c) + 1];
-      const float v[2][2] = {{mr, -mi}, {mi, mr}};
-      for (uint32_t pr = 0; pr < 2; ++pr)
-        for (uint32_t pc = 0; pc < 2; ++pc) {
-          const float x = v[pr][pc];
-          const __half h = __float2half_rn(x);
-          const __half l = __float2half_rn(x - __half2float(h));
-          const size_t off = size_t(2 * r + pr) * kReal + (2 * c + pc);
-          std::memcpy(hi + off, &h, 2);
-          std::memcpy(lo + off, &l, 2);
-        }
-    }
-}
-
 static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
   std::memset(&g, 0, sizeof(g));
   if (n < kTileBits) return false;
@@ -846,9 +834,10 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
 size_t tc_operand_bytes(unsigned) { return size_t(tc::kOperandBytes); }
 
 void tc_build_operands(unsigned k, const float* m32, void* host_out) {
-  // The plan stores matrices already padded to 6 targets (k == 6).
+  // The plan stores matrices already padded to 6 targets (k == 6); the
+  // kernel converts them to its FP16 operand images.
   (void)k;
-  tc::build_a_images(m32, static_cast<unsigned char*>(host_out));
+  std::memcpy(host_out, m32, tc::kOperandBytes);
 }
 
 // Pads a gate to 6 targets for the tensor-core path (plan construction).
@@ -857,6 +846,58 @@ void tc_pad_gate(unsigned n, const unsigned* qs, unsigned k, const float* m32,
   std::vector<float> m6;
   tc::pad_to_6(n, qs, k, m32, qs6, m6);
   std::memcpy(m6_out, m6.data(), m6.size() * sizeof(float));
+}
+
+// Applies a gate given as a host matrix on the tensor cores: pads it to six
+// targets, builds its FP16 operands in a pinned staging slot of the
+// context's ring and uploads them asynchronously; the slot is reused only
+// after its copy has completed (event), and later copies into the same
+// device slot are ordered after this launch on the stream.
+int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
+                  unsigned k, const float* m32, const void* operands);
+
+int apply_gate_tc_host(qsg_ctx* ctx, float* state, unsigned n,
+                       const unsigned* qs, unsigned k, const float* m32) {
+  using namespace tc;
+  constexpr size_t kSlot = (kOperandBytes + 1023) & ~size_t(1023);
+  if (!ctx->tc_ring_dev) {
+    void* d = nullptr;
+    void* h = nullptr;
+    QSG_CUDA(cudaMalloc(&d, kSlot * qsg_ctx::kTcRingSlots));
+    QSG_CUDA(cudaMallocHost(&h, kSlot * qsg_ctx::kTcRingSlots));
+    ctx->tc_ring_dev = static_cast<unsigned char*>(d);
+    ctx->tc_ring_host = static_cast<unsigned char*>(h);
+    for (int i = 0; i < qsg_ctx::kTcRingSlots; ++i)
+      QSG_CUDA(cudaEventCreateWithFlags(&ctx->tc_ring_ev[i],
+                                        cudaEventDisableTiming));
+  }
+  unsigned qs6[6];
+  std::vector<float> m6;
+  pad_to_6(n, qs, k, m32, qs6, m6);
+  const int slot = ctx->tc_ring_next;
+  ctx->tc_ring_next = (slot + 1) % qsg_ctx::kTcRingSlots;
+  if (ctx->tc_ring_used[slot])
+    QSG_CUDA(cudaEventSynchronize(ctx->tc_ring_ev[slot]));
+  unsigned char* h = ctx->tc_ring_host + slot * kSlot;
+  unsigned char* d = ctx->tc_ring_dev + slot * kSlot;
+  std::memcpy(h, m6.data(), kOperandBytes);
+  QSG_CUDA(cudaMemcpyAsync(d, h, kOperandBytes, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  QSG_CUDA(cudaEventRecord(ctx->tc_ring_ev[slot], ctx->stream));
+  ctx->tc_ring_used[slot] = true;
+  return apply_gate_tc(ctx, state, n, qs6, 6, m6.data(), d);
+}
+
+void tcring_release(qsg_ctx* ctx) {
+  for (int i = 0; i < qsg_ctx::kTcRingSlots; ++i) {
+    if (ctx->tc_ring_ev[i]) cudaEventDestroy(ctx->tc_ring_ev[i]);
+    ctx->tc_ring_ev[i] = nullptr;
+    ctx->tc_ring_used[i] = false;
+  }
+  if (ctx->tc_ring_dev) cudaFree(ctx->tc_ring_dev);
+  if (ctx->tc_ring_host) cudaFreeHost(ctx->tc_ring_host);
+  ctx->tc_ring_dev = nullptr;
+  ctx->tc_ring_host = nullptr;
 }
 
 static int* g_tc_err = nullptr;
@@ -909,7 +950,7 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
     set_error("tensor-core gate without device operands");
     return QSG_ERR_INVALID;
   }
-  a.operands = static_cast<const uint32_t*>(operands);
+  a.operands = static_cast<const float2*>(operands);
   // sigma = 2^min(floor(n/2), 14): amplitudes of a normalised state (about
   // 2^(-n/2)) land near 1, where the lo parts of the split are normal FP16
   // numbers (relative error ~2^-23), and |psi_i| <= 4 stays below the FP16
@@ -962,21 +1003,9 @@ int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
     set_error("tensor-core path needs n >= %d qubits", tc::kTileBits);
     return QSG_ERR_UNSUPPORTED;
   }
-  unsigned qs6[6];
-  std::vector<float> m6(2 * tc::kD * tc::kD);
-  tc_pad_gate(n, qs, k, matrix, qs6, m6.data());
-  // Operands for a single call: synchronous upload into a context-owned
-  // buffer (the stream is drained first, so the previous call's operands
-  // are no longer read).
-  static thread_local std::vector<unsigned char> host;
-  host.resize(tc_operand_bytes(6));
-  tc_build_operands(6, m6.data(), host.data());
-  void* dev = nullptr;
-  int rc = get_tc_operand_slot(ctx, host.size(), &dev);
-  if (rc) return rc;
-  QSG_CUDA(cudaStreamSynchronize(ctx->stream));
-  QSG_CUDA(cudaMemcpy(dev, host.data(), host.size(), cudaMemcpyHostToDevice));
-  return apply_gate_tc(ctx, state, n, qs6, 6, m6.data(), dev);
+  // Operands built on the host and uploaded through the context's ring
+  // (asynchronous; the call does not wait for the stream).
+  return apply_gate_tc_host(ctx, state, n, qs, k, matrix);
 }
 
 int qsg_tc_error(qsg_ctx* ctx, int* out) {

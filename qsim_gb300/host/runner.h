@@ -23,6 +23,10 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
                         unsigned prev_count, double* out);
 // CTAs of a tensor-core pass on n qubits.
 unsigned tc_grid(qsg_ctx* ctx, unsigned n);
+// A gate given as a host matrix (k <= 6, n >= 12) on the tensor cores, its
+// operands built per call and uploaded through the context's ring.
+int apply_gate_tc_host(qsg_ctx* ctx, float* state, unsigned n,
+                       const unsigned* qs, unsigned k, const float* m32);
 // Size in bytes of the device operands of a k-qubit tensor-core gate, and
 // their construction from the interleaved FP32 matrix.
 size_t tc_operand_bytes(unsigned k);

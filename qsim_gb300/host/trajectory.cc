@@ -688,6 +688,8 @@ struct StreamSink {
   TrajWorkspace& ws;
   float* state;
   unsigned n;
+  unsigned tc_min_k;  // recomputed blocks of >= tc_min_k qubits on tcgen05
+                      // (0: never)
 
   int set_zero() { return qsg_set_state_zero(ws.ctx, state, n); }
   int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
@@ -695,6 +697,11 @@ struct StreamSink {
     if (tc_operands)
       return apply_gate_tc(ws.ctx, state, n, qs.data(), qs.size(), m32,
                            tc_operands);
+    // A block recomputed for a non-default Kraus choice or cut at a channel
+    // takes the tensor cores like the plan's own blocks: a 5- or 6-qubit
+    // CUDA-core pass costs several tensor-core passes.
+    if (!ctl && tc_min_k && qs.size() >= tc_min_k && n >= 12)
+      return apply_gate_tc_host(ws.ctx, state, n, qs.data(), qs.size(), m32);
     if (ctl)
       return apply_gate_ex(ws.ctx, state, n, qs.data(), qs.size(),
                            ctl->cqs.data(), ctl->cqs.size(), ctl->cvals, m32,
@@ -811,7 +818,8 @@ int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
                               uint64_t* stats) const {
   const int rc = upload(ws.ctx);
   if (rc) return rc;
-  StreamSink sink{ws, state, nc_.num_qubits};
+  StreamSink sink{ws, state, nc_.num_qubits,
+                  has_tc_ ? std::max(opt_.tc_min_k, 1u) : 0u};
   return walk(rep, stats, sink);
 }
 

@@ -7,7 +7,9 @@ from qsim_gb300 import autotune as AT
 
 def test_candidates_cover_every_mode():
     c = AT.candidates(24)
-    assert {(x["max_fused_size"], x["tensor"]) for x in c} == set(AT.FORMS)
+    assert {x["max_fused_size"] for x in c} == {3, 4}
+    assert {x["tc_from"] for x in c} == {0, 20, 22, 24}
+    assert not any(x["tc_from"] for x in AT.candidates(24, forms=((4, False),)))
     assert any(x["split"] == 0 for x in c)          # stream path only
     assert any(x["split"] == 24 for x in c)         # all in the packed kernel
     assert any(0 < x["split"] < 24 for x in c)      # split, both at once
@@ -22,11 +24,11 @@ def test_runners_follow_the_split():
     made = {}
 
     def make(f, tensor):
-        return made.setdefault((f, tensor), [(f, tensor, i) for i in range(3)])
-    cfg = dict(max_fused_size=6, tensor=True, split=16, ctas_per_sm=1,
-               tile_kib=32)
-    rs = AT.runners_for(make, [12, 16, 20], cfg)
-    assert rs == [(4, False, 0), (4, False, 1), (6, True, 2)]
+        return made.setdefault((f, tensor), [(f, tensor, i) for i in range(4)])
+    cfg = dict(max_fused_size=3, tensor=False, tc_from=22, split=16,
+               ctas_per_sm=1, tile_kib=32)
+    rs = AT.runners_for(make, [12, 16, 20, 24], cfg)
+    assert rs == [(4, False, 0), (4, False, 1), (3, False, 2), (6, True, 3)]
 
 
 def test_signature_depends_on_workload_only():

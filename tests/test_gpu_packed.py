@@ -170,7 +170,11 @@ def test_autotuned_configurations_agree(ss):
         return made[(f, tensor)]
     items = [(i % len(sizes), 500 + i) for i in range(30)]
     ref = None
-    for cfg in AT.candidates(max(sizes), forms=((4, False), (6, True))):
+    extra = [dict(max_fused_size=4, tensor=False, tc_from=12, split=9,
+                  ctas_per_sm=1, tile_kib=32),
+             dict(max_fused_size=3, tensor=False, tc_from=15, split=0,
+                  ctas_per_sm=0, tile_kib=0)]
+    for cfg in AT.candidates(max(sizes), forms=((4, False), (6, True))) + extra:
         runners = AT.runners_for(make, sizes, cfg)
         outs = [ss.Create(sizes[r]) for r, _ in items]
         per, lat, wall, launches, info = AT.run(runners, items, cfg, 4, outs)
