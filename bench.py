@@ -652,6 +652,8 @@ def kernel_case(spec: str, n: int, reps: int):
       tc:q0,..                tensor-core kernel (random unitary)
       ctrl:q0,..:c0,..        controlled gate, controls all 1
       ev:q0,..                ExpectationValue (tile kernel, mode 1)
+      evp:q0,..:PAULIS        ExpectationValue of a Pauli string (letters
+                              X, Y, Z, I per qubit; one-pass kernel)
       norm | ip | multiply    reductions / elementwise pass
       sample                  1000 samples (chunk sums, prefix, search)
       collapse:mask           Collapse on bits = 0 of `mask` (hex)
@@ -663,7 +665,7 @@ def kernel_case(spec: str, n: int, reps: int):
     parts = spec.split(":")
     kind = parts[0]
     qs = [int(x) for x in parts[1].split(",")] if len(parts) > 1 and kind in (
-        "gate", "tc", "ctrl", "ev") else []
+        "gate", "tc", "ctrl", "ev", "evp") else []
     cqs = [int(x) for x in parts[2].split(",")] if kind == "ctrl" else []
     ctx = q.Context(0)
     ss, sim = q.StateSpace(ctx=ctx), q.Simulator(ctx=ctx)
@@ -677,6 +679,12 @@ def kernel_case(spec: str, n: int, reps: int):
     rng = np.random.default_rng(0)
     u, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) +
                         1j * rng.normal(size=(1 << k, 1 << k)))
+    if kind == "evp":
+        pm = {"I": np.eye(2), "X": np.array([[0, 1], [1, 0]]),
+              "Y": np.array([[0, -1j], [1j, 0]]), "Z": np.diag([1, -1])}
+        u = np.eye(1)
+        for letter in parts[2]:
+            u = np.kron(pm[letter], u)
     m = np.ascontiguousarray(u.astype(np.complex64)).view(np.float32)
     out2 = (Cx.c_double * 2)()
     smp = np.zeros(1000, dtype=np.uint64)
@@ -690,7 +698,7 @@ def kernel_case(spec: str, n: int, reps: int):
             N.check(N.lib.qsg_apply_controlled_gate(
                 ctx.h, st.get(), n, N.u32_array(qs), k, N.u32_array(cqs),
                 len(cqs), (1 << len(cqs)) - 1, m.ctypes.data_as(N.P_f32)))
-        elif kind == "ev":
+        elif kind in ("ev", "evp"):
             N.check(N.lib.qsg_expectation_value(
                 ctx.h, st.get(), n, N.u32_array(qs), k,
                 m.ctypes.data_as(N.P_f32), out2))

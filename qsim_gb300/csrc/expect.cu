@@ -10,7 +10,10 @@
 //
 //   <psi|M|psi> = sum_i conj(psi_i) d[r(i)] psi_(i ^ X),
 //
-// a bandwidth-bound pass: each thread reads a 16-byte unit (two amplitudes)
+// a bandwidth-bound pass (for Pauli strings d[r] is a constant times the sign
+// (-1)^popcount(i & zmask), one AND and one popcount per amplitude; other
+// monomials look d up by the target bits of i): each thread reads a 16-byte
+// unit (two amplitudes)
 // and, when X flips qubits above qubit 0, its partner unit, and adds both
 // units' terms, so every amplitude is read once (8 N bytes).  Products are
 // FP32; partial sums FP32 over a thread's units of one step, FP64 across
@@ -32,6 +35,8 @@ constexpr int kEvUnroll = 4;
 
 struct MonoArgs {
   float2 d[64];        // d[r] = M[r][r ^ xm]
+  float2 c0;           // SIGNED form: d[r] = c0 (-1)^popcount(r & zm)
+  uint64_t zmask;      // SIGNED form: zm spread onto the state bits
   uint32_t qpos[6];    // target qubits (bit j of r <-> qpos[j])
   uint32_t k;
   uint32_t x0;         // bit 0 of X (qubit 0 flipped)
@@ -56,6 +61,19 @@ __device__ __forceinline__ void term(float& er, float& ei, float2 p, float2 d,
   ei = fmaf(p.x, ti, fmaf(-p.y, tr, ei));
 }
 
+// d for amplitude index i: the table entry of i's target bits, or for a
+// Pauli-type operator (SIGNED) c0 with the sign of popcount(i & zmask).
+template <bool SIGNED>
+__device__ __forceinline__ float2 dval(uint64_t i, const MonoArgs& a) {
+  if constexpr (SIGNED) {
+    const bool neg = (__popcll(i & a.zmask) & 1) != 0;
+    return neg ? make_float2(-a.c0.x, -a.c0.y) : a.c0;
+  } else {
+    return a.d[row_of(i, a)];
+  }
+}
+
+template <bool SIGNED>
 __global__ void __launch_bounds__(kEvThreads)
     mono_ev_kernel(const float4* __restrict__ s, uint64_t work,
                    const __grid_constant__ MonoArgs a,
@@ -91,18 +109,18 @@ __global__ void __launch_bounds__(kEvThreads)
       if (a.ux == 0) {
         // Partner of amplitude i0 + t is i0 + (t ^ x0), in the same unit.
         const float2 q0 = a.x0 ? p1 : p0, q1 = a.x0 ? p0 : p1;
-        term(fr, fi, p0, a.d[row_of(i0, a)], q0);
-        term(fr, fi, p1, a.d[row_of(i0 + 1, a)], q1);
+        term(fr, fi, p0, dval<SIGNED>(i0, a), q0);
+        term(fr, fi, p1, dval<SIGNED>(i0 + 1, a), q1);
       } else {
         const uint64_t k0 = 2 * (u[j] ^ a.ux);
         const float2 r0 = make_float2(y[j].x, y[j].y);
         const float2 r1 = make_float2(y[j].z, y[j].w);
         const float2 q0 = a.x0 ? r1 : r0, q1 = a.x0 ? r0 : r1;
         const float2 v0 = a.x0 ? p1 : p0, v1 = a.x0 ? p0 : p1;
-        term(fr, fi, p0, a.d[row_of(i0, a)], q0);
-        term(fr, fi, p1, a.d[row_of(i0 + 1, a)], q1);
-        term(fr, fi, r0, a.d[row_of(k0, a)], v0);
-        term(fr, fi, r1, a.d[row_of(k0 + 1, a)], v1);
+        term(fr, fi, p0, dval<SIGNED>(i0, a), q0);
+        term(fr, fi, p1, dval<SIGNED>(i0 + 1, a), q1);
+        term(fr, fi, r0, dval<SIGNED>(k0, a), v0);
+        term(fr, fi, r1, dval<SIGNED>(k0 + 1, a), v1);
       }
     }
     ar += double(fr);
@@ -166,6 +184,23 @@ int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
   }
   for (unsigned r = 0; r < (1u << k); ++r)
     a.d[r] = make_float2(d[2 * r], d[2 * r + 1]);
+  // Pauli-type phases: d[r] = d[0] (-1)^popcount(r & zm), zm read off the
+  // single-bit rows.
+  bool signed_form = d[0] != 0.f || d[1] != 0.f;
+  uint32_t zm = 0;
+  for (unsigned j = 0; signed_form && j < k; ++j) {
+    const float* dj = d + 2 * (1u << j);
+    if (dj[0] == -d[0] && dj[1] == -d[1]) zm |= 1u << j;
+    else if (!(dj[0] == d[0] && dj[1] == d[1])) signed_form = false;
+  }
+  for (unsigned r = 0; signed_form && r < (1u << k); ++r) {
+    const float sgn = (__builtin_popcount(r & zm) & 1) ? -1.f : 1.f;
+    if (d[2 * r] != sgn * d[0] || d[2 * r + 1] != sgn * d[1])
+      signed_form = false;
+  }
+  a.c0 = make_float2(d[0], d[1]);
+  for (unsigned j = 0; j < k; ++j)
+    if ((zm >> j) & 1) a.zmask |= uint64_t{1} << qs[j];
   a.x0 = uint32_t(X & 1);
   a.ux = X >> 1;
   a.ub = a.ux ? unsigned(__builtin_ctzll(a.ux)) : 0;
@@ -179,8 +214,12 @@ int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
   int rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
   if (rc) return rc;
   double2* partial = static_cast<double2*>(p);
-  mono_ev_kernel<<<unsigned(grid), kEvThreads, 0, ctx->stream>>>(
-      reinterpret_cast<const float4*>(state), work, a, partial);
+  if (signed_form)
+    mono_ev_kernel<true><<<unsigned(grid), kEvThreads, 0, ctx->stream>>>(
+        reinterpret_cast<const float4*>(state), work, a, partial);
+  else
+    mono_ev_kernel<false><<<unsigned(grid), kEvThreads, 0, ctx->stream>>>(
+        reinterpret_cast<const float4*>(state), work, a, partial);
   QSG_LAUNCHED(ctx);
   return reduce_partials_d2(ctx, partial, grid, out_re_im);
 }

@@ -334,10 +334,17 @@ __global__ void __launch_bounds__(1024)
   __shared__ double ws[32];
   const uint64_t per = (nchunks + blockDim.x - 1) / blockDim.x;
   const uint64_t beg = threadIdx.x * per;
+  // Loads in batches of 8 independent reads; the sum keeps index order.
   double s = 0;
-  for (uint64_t j = 0; j < per; ++j) {
-    uint64_t i = beg + j;
-    if (i < nchunks) s += sums[i];
+  for (uint64_t j0 = 0; j0 < per; j0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t i = beg + j0 + q;
+      v[q] = (j0 + q < per && i < nchunks) ? sums[i] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += v[q];
   }
   double x = s;
   const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
@@ -359,11 +366,20 @@ __global__ void __launch_bounds__(1024)
   }
   __syncthreads();
   double run = ws[w] + xe;
-  for (uint64_t j = 0; j < per; ++j) {
-    uint64_t i = beg + j;
-    if (i < nchunks) {
-      run += sums[i];
-      incl[i] = run;
+  for (uint64_t j0 = 0; j0 < per; j0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t i = beg + j0 + q;
+      v[q] = (j0 + q < per && i < nchunks) ? sums[i] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t i = beg + j0 + q;
+      if (j0 + q < per && i < nchunks) {
+        run += v[q];
+        incl[i] = run;
+      }
     }
   }
 }
