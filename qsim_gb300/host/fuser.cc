@@ -391,12 +391,32 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
 
 }  // namespace
 
+// Seed windows tried by the multi-start search: the greedy rule is not
+// monotonic in the window (on the 30-qubit depth-20 grid circuit at f = 6,
+// windows of 3 and 4 gates give 36 blocks, 12 gives 37, 5 gives 41).
+constexpr unsigned kStartWindows[] = {2, 3, 4, 6, 8};
+
 Plan fuse(const Circuit& c, const FuseOptions& opt) {
   const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
-  if (!opt.cost) return fuse_greedy(c, opt, f, false);
+  if (!opt.cost) {
+    Plan best = fuse_greedy(c, opt, f, false);
+    // Tensor-core plans cost about the same per block, so their run time is
+    // their block count: keep the greedy result with the fewest blocks.
+    if (opt.tensor_path) {
+      for (unsigned w : kStartWindows) {
+        if (w == opt.seeds) continue;
+        FuseOptions o = opt;
+        o.seeds = w;
+        Plan p = fuse_greedy(c, o, f, false);
+        if (p.ops.size() < best.ops.size()) best = std::move(p);
+      }
+    }
+    return best;
+  }
   // Learned planner: candidate plans for every block-size limit up to f,
-  // grown by gate count and by predicted time per gate, each block on its
-  // predicted-faster path; the plan of lowest predicted total time wins.
+  // grown by gate count and by predicted time per gate (for limits >= 5
+  // also with a 3-gate seed window), each block on its predicted-faster
+  // path; the plan of lowest predicted total time wins.
   // The fixed-size plans of the gate-count rule are among the candidates.
   Plan best;
   double best_t = 0;
@@ -404,12 +424,17 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
   for (unsigned ff = 1; ff <= f; ++ff) {
     for (int pg = 0; pg < 2; ++pg) {
       if (ff == 1 && pg) continue;
-      Plan p = fuse_greedy(c, opt, ff, pg != 0);
-      const double t = plan_cost(c, p, *opt.cost);
-      if (!have || t < best_t) {
-        best = std::move(p);
-        best_t = t;
-        have = true;
+      for (unsigned w : {opt.seeds, 3u}) {
+        if (w == 3u && (opt.seeds == 3u || ff < 5)) continue;
+        FuseOptions o = opt;
+        o.seeds = w;
+        Plan p = fuse_greedy(c, o, ff, pg != 0);
+        const double t = plan_cost(c, p, *opt.cost);
+        if (!have || t < best_t) {
+          best = std::move(p);
+          best_t = t;
+          have = true;
+        }
       }
     }
   }
