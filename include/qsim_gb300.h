@@ -450,6 +450,44 @@ int qsg_traj_run_packed(int device, qsg_traj* const* runners,
                         double* wall_s, uint64_t* launches,
                         qsg_packed_info* info);
 
+/* ---- unitary calculator (lib/unitaryspace_basic.h,
+ * lib/unitary_calculator_basic.h) ----------------------------------------
+ * A unitary of n qubits (n <= 20) is stored as the reference stores it:
+ * entry (i, j) at complex index i * 2^n + j, interleaved (re, im).  The
+ * reference's ApplyGate (unitary_calculator_basic.h:126-184) mixes the
+ * entries of every row over the column bits at qs, so the unitary is a
+ * 2n-qubit state and its gates are the state-vector gates on qubits < n:
+ * the same GB300 kernels run it.  From the identity, entry (i, j) after
+ * gates G1..Gm is (Gm ... G1)[j][i], as in the reference. */
+/* UnitarySpaceBasic::MinSize (unitaryspace_basic.h:49-51), in floats (at
+ * least 64). */
+uint64_t qsg_unitary_min_size(unsigned num_qubits);
+/* CreateUnitary (unitaryspace.h:41-47): device buffer of MinSize floats. */
+int qsg_unitary_create(qsg_ctx* ctx, unsigned num_qubits, float** out);
+int qsg_unitary_free(qsg_ctx* ctx, float* u);
+/* SetIdentity / SetAllZeros (unitaryspace_basic.h:53-74). */
+int qsg_unitary_set_identity(qsg_ctx* ctx, float* u, unsigned n);
+int qsg_unitary_set_all_zeros(qsg_ctx* ctx, float* u, unsigned n);
+/* GetEntry / SetEntry (unitaryspace_basic.h:76-96). */
+int qsg_unitary_get_entry(qsg_ctx* ctx, const float* u, unsigned n,
+                          uint64_t i, uint64_t j, float* re_im);
+int qsg_unitary_set_entry(qsg_ctx* ctx, float* u, unsigned n, uint64_t i,
+                          uint64_t j, float re, float im);
+/* UnitaryCalculatorBasic::ApplyGate / ApplyControlledGate
+ * (unitary_calculator_basic.h:51-117): qubits < n, k <= 6. */
+int qsg_unitary_apply_gate(qsg_ctx* ctx, float* u, unsigned n,
+                           const unsigned* qs, unsigned k,
+                           const float* matrix);
+int qsg_unitary_apply_controlled_gate(qsg_ctx* ctx, float* u, unsigned n,
+                                      const unsigned* qs, unsigned k,
+                                      const unsigned* cqs, unsigned c,
+                                      uint64_t cvals, const float* matrix);
+/* Applies every op of a fused plan (of an n-qubit circuit) to the unitary;
+ * a plan's tensor-core blocks (circuits of >= 12 qubits) run on tcgen05.
+ * No counterpart in the reference, which applies gates one by one.  Plans
+ * with measurements are rejected. */
+int qsg_unitary_run_plan(qsg_ctx* ctx, qsg_plan* p, float* u, unsigned n);
+
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,
  * qsg_timer_stop records a second one, synchronises and returns the elapsed

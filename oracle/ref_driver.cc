@@ -27,6 +27,10 @@
 //       .ev   : per EV line: <k> <q...> <floats> -> complex<double> on the
 //               f32 state (SIMD) then on the f64 state (basic)
 //       .meta : norm, number of fused ops
+//   unitary <gates> <out>
+//       the full unitary of UnitaryCalculatorBasic<For,double> applied to
+//       the identity (matrix and controlled gates, in order): 4^n complex
+//       doubles, entry (i, j) at i * 2^n + j (the reference's layout).
 //   text <circuit.txt> <out-prefix>
 //       reference text format through CircuitQsimParser, FP64 state (.f64)
 //   fuse <gates> <max_fused_size>
@@ -73,6 +77,8 @@
 #include "simmux.h"
 #include "simulator_basic.h"
 #include "statespace_basic.h"
+#include "unitary_calculator_basic.h"
+#include "unitaryspace_basic.h"
 
 using namespace qsim;
 
@@ -411,8 +417,29 @@ static int CmdText(int argc, char** argv) {
   return 0;
 }
 
+static int CmdUnitary(int argc, char** argv) {
+  if (argc < 4) return 2;
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  using UC = unitary::UnitaryCalculatorBasic<For, double>;
+  using US = UC::UnitarySpace;
+  US us(1);
+  UC uc(1);
+  auto u = us.CreateUnitary(n);
+  us.SetIdentity(u);
+  for (const auto& g : specs) {
+    std::vector<double> m(g.m.begin(), g.m.end());
+    if (g.kind == 'g') uc.ApplyGate(g.qs, m.data(), u);
+    else if (g.kind == 'c')
+      uc.ApplyControlledGate(g.qs, g.cqs, g.cvals, m.data(), u);
+  }
+  WriteRaw(argv[3], u.get(), sizeof(double) * US::MinSize(n));
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
+  if (std::string(argv[1]) == "unitary") return CmdUnitary(argc, argv);
   std::string cmd = argv[1];
   if (cmd == "text") return CmdText(argc, argv);
   if (cmd == "fuse") return CmdFuse(argc, argv);

@@ -121,6 +121,17 @@ SIGNATURES = {
     "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                  vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                  P_u64]),
+    "qsg_unitary_min_size": (u64, [u32]),
+    "qsg_unitary_create": (i32, [vp, u32, C.POINTER(vp)]),
+    "qsg_unitary_free": (i32, [vp, vp]),
+    "qsg_unitary_set_identity": (i32, [vp, vp, u32]),
+    "qsg_unitary_set_all_zeros": (i32, [vp, vp, u32]),
+    "qsg_unitary_get_entry": (i32, [vp, vp, u32, u64, u64, P_f32]),
+    "qsg_unitary_set_entry": (i32, [vp, vp, u32, u64, u64, f32, f32]),
+    "qsg_unitary_apply_gate": (i32, [vp, vp, u32, P_u32, u32, P_f32]),
+    "qsg_unitary_apply_controlled_gate": (i32, [vp, vp, u32, P_u32, u32, P_u32,
+                                                u32, u64, P_f32]),
+    "qsg_unitary_run_plan": (i32, [vp, vp, vp, u32]),
     "qsg_traj_run_packed": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                   vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                   P_u64, vp]),

@@ -299,6 +299,37 @@ int qsg_plan_run(qsg_ctx* ctx, qsg_plan* p, float* state, unsigned seed,
   return rc;
 }
 
+int qsg_unitary_run_plan(qsg_ctx* ctx, qsg_plan* p, float* u, unsigned n) {
+  if (!ctx || !p || !u) return invalid("null argument");
+  PlanRuntime& rt = p->rt;
+  if (rt.plan.num_qubits != n || n > 20)
+    return invalid("qsg_unitary_run_plan: plan and unitary sizes differ");
+  // The unitary is a 2n-qubit state whose gates act on qubits < n (the
+  // reference's row-wise application, lib/unitary_calculator_basic.h).
+  int rc = rt.upload(ctx);
+  if (rc) return rc;
+  rc = rt.prepare_tc();
+  if (rc) return rc;
+  for (size_t i = 0; i < rt.plan.ops.size(); ++i) {
+    const PlanOp& op = rt.plan.ops[i];
+    if (op.kind == OpKind::kMeasure)
+      return invalid("qsg_unitary_run_plan: plans with measurements");
+    if (op.kind == OpKind::kGate && op.path == Path::kTensor) {
+      rc = apply_gate_tc(ctx, u, 2 * n, op.qs.data(), op.qs.size(),
+                         op.m32.data(), rt.tc_operands(i));
+    } else {
+      const float* dm = (rt.dmat && rt.dmat_off[i] != size_t(-1))
+                            ? rt.dmat + rt.dmat_off[i]
+                            : nullptr;
+      rc = apply_gate_ex(ctx, u, 2 * n, op.qs.data(), op.qs.size(),
+                         op.cqs.data(), op.cqs.size(), op.cvals,
+                         op.m32.data(), dm);
+    }
+    if (rc) return rc;
+  }
+  return QSG_OK;
+}
+
 int qsg_plan_capture(qsg_ctx* ctx, qsg_plan* p, float* state) {
   if (!ctx || !p || !state) return invalid("null argument");
   return p->rt.capture(ctx, state);

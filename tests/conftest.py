@@ -129,6 +129,23 @@ class Oracle:
     def collapse(self, s, n, mask, bits):
         self.L.orc_collapse_f64(self._dp(s), n, mask, bits)
 
+    def unitary(self, n, ops):
+        """The reference's UnitaryCalculatorBasic from the identity
+        (lib/unitary_calculator_basic.h:126-259): entry (i, j) at index
+        i * 2^n + j, each gate applied to every row over the column bits at
+        its qubits, i.e. the oracle's state-vector gate on qubits < n of a
+        2n-qubit state.  Returns the (2^n, 2^n) complex128 matrix."""
+        d = 1 << n
+        u = np.zeros(d * d, dtype=np.complex128)
+        u[np.arange(d) * d + np.arange(d)] = 1.0
+        for o in ops:
+            if o["kind"] == 0:
+                self.apply_gate(u, 2 * n, o["qs"], o["m"])
+            elif o["kind"] == 1:
+                self.apply_controlled_gate(u, 2 * n, o["qs"], o["cqs"],
+                                           o["cvals"], o["m"])
+        return u.reshape(d, d)
+
     def run_ops(self, n, ops):
         s = self.zero_state(n)
         for o in ops:
@@ -166,14 +183,17 @@ def _gate_list_cases():
     out = []
     for p in glob.glob(os.path.join(GOLDEN, "*.npz")):
         with np.load(p) as z:
-            if "kinds" in z.files and "op_channel" not in z.files:
+            if ("kinds" in z.files and "op_channel" not in z.files
+                    and "u64" not in z.files):
                 out.append(os.path.basename(p)[:-4])
     return sorted(out)
 
 
 # Golden cases that hold a gate list (no channels) and the reference's
-# outputs for it.
+# state-vector outputs for it (the unitary cases hold a unitary instead).
 GOLDEN_CASES = _gate_list_cases()
+UNITARY_CASES = sorted(os.path.basename(p)[:-4]
+                       for p in glob.glob(os.path.join(GOLDEN, "unitary*.npz")))
 
 
 PAULI = {

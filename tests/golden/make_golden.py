@@ -409,11 +409,53 @@ def traj_cases():
               0, 8, states_c64=True)
 
 
+def unitary_case(name, n, ops):
+    """The reference's UnitaryCalculatorBasic<double> from the identity:
+    4^n complex entries, entry (i, j) at i * 2^n + j."""
+    with tempfile.TemporaryDirectory() as td:
+        gl = os.path.join(td, "gates.txt")
+        write_gate_list(gl, n, ops)
+        out = os.path.join(td, "u.f64")
+        subprocess.run([DRIVER, "unitary", gl, out], check=True)
+        u = np.fromfile(out, dtype=np.float64).view(np.complex128)
+        data = dict(n=np.int32(n), u64=u, **pack_ops(ops))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+
+
+def small_gate_list(rng, n, ngates, kmax, ctrl_frac):
+    """Gates of 1..kmax targets; with probability ctrl_frac 1..2 controls
+    (targets + controls <= n)."""
+    ops = []
+    for t in range(ngates):
+        k = int(rng.integers(1, kmax + 1))
+        if n - k >= 1 and rng.random() < ctrl_frac:
+            c = int(rng.integers(1, min(2, n - k) + 1))
+            picks = rng.choice(n, size=k + c, replace=False).tolist()
+            ops.append(dict(kind="c", time=t, qs=sorted(picks[:k]),
+                            cqs=sorted(picks[k:]),
+                            cvals=int(rng.integers(0, 1 << c)),
+                            m=random_unitary(rng, k)))
+        else:
+            qs = sorted(rng.choice(n, size=k, replace=False).tolist())
+            ops.append(dict(kind="g", time=t, qs=qs, m=random_unitary(rng, k)))
+    return ops
+
+
+def unitary_cases():
+    rng = np.random.default_rng(7070)
+    unitary_case("unitary3", 3, small_gate_list(rng, 3, 10, 2, 0.3))
+    unitary_case("unitary5", 5, small_gate_list(rng, 5, 24, 3, 0.3))
+    unitary_case("unitary7", 7, small_gate_list(rng, 7, 30, 4, 0.2))
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
     if sys.argv[1:] == ["traj"]:
         traj_cases()
+        return
+    if sys.argv[1:] == ["unitary"]:
+        unitary_cases()
         return
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
     mt_case()
@@ -439,6 +481,7 @@ def main():
     run_case("rand14_k2", 14, ops, 2, 4000, 1,
              measure=(17, 6, [0, 5, 13]))
     traj_cases()
+    unitary_cases()
 
 
 if __name__ == "__main__":

@@ -42,6 +42,15 @@ def test_reference_runner_compiles_with_gb300_factory(tmp_path):
                  extra=("-I" + os.path.join(REF, "lib"),))
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lib")),
+                    reason="qsim checkout (reference headers) not present")
+def test_reference_apply_gate_compiles_with_gb300_unitary(tmp_path):
+    """lib/gate_appl.h's ApplyGate(calculator, gate, unitary) and the
+    text-format parser instantiate with UnitaryCalculatorGB300."""
+    compile_prog("dropin_unitary.cc", str(tmp_path / "dropin_unitary"),
+                 extra=("-I" + os.path.join(REF, "lib"),))
+
+
 @pytest.mark.gpu
 def test_adapter_program_matches_reference(tmp_path, oracle):
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
