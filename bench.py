@@ -368,9 +368,14 @@ def run_engine(args, world, rank, local, dist):
         learned = {"skipped": "--headline-only"}
         traj = {"skipped": "--headline-only"}
         expect = {"skipped": "--headline-only"}
+        unitary = {"skipped": "--headline-only"}
+        cache = {"skipped": "--headline-only"}
     else:
         learned = bench_learned_planner(ctx, ss, model, dist)
         expect = bench_expectations(ctx, ss, dist)
+        unitary = bench_unitary(ctx, dist, cpu=(rank == 0 and world == 1
+                                                and not args.no_cpu))
+        cache = bench_plan_cache(ctx, ss, dist)
         traj = bench_trajectories(args.traj_streams, args.traj_f,
                                   mode=args.traj_mode,
                                   ctas_per_sm=args.traj_ctas_per_sm,
@@ -419,6 +424,8 @@ def run_engine(args, world, rank, local, dist):
             "trajectories": traj,
             "learned_planner": learned,
             "expectations": expect,
+            "unitary": unitary,
+            "plan_cache": cache,
         }
         print(json.dumps(line), flush=True)
 
@@ -490,6 +497,102 @@ def bench_expectations(ctx, ss, dist):
         "ev": out,
         "ev_speedup": out["dense"]["s_per_ev"] / out["monomial"]["s_per_ev"],
     }
+
+
+def bench_plan_cache(ctx, ss, dist):
+    """The headline circuit run through the fused-plan cache: the first run
+    (fusion at f = 6 on the tensor-core path, CUDA-graph capture, replay)
+    against later runs (key + hash + graph launch), wall seconds per run
+    with the state zeroed and the device synchronised, and the host time of
+    a cached call alone.  The reference fuses on every QSimRunner::Run."""
+    from qsim_gb300 import engine as E
+    c = E.Circuit.grid(GRID["rows"], GRID["cols"], GRID["extra"],
+                       GRID["cycles"], GRID["seed"])
+    n = c.num_qubits
+    st = ss.Create(n)
+    opts = dict(max_fused_size=6, tensor_path=True)
+    t0 = time.perf_counter()
+    E.Plan(c, **opts)
+    fuse_s = time.perf_counter() - t0
+    pc = E.PlanCache()
+    barrier(dist)
+    ss.SetStateZero(st)
+    ctx.sync()
+    t0 = time.perf_counter()
+    _, hit0 = pc.run(ctx, c, st, **opts)
+    ctx.sync()
+    first_s = time.perf_counter() - t0
+    hits, host = [], []
+    for _ in range(3):
+        ss.SetStateZero(st)
+        ctx.sync()
+        t0 = time.perf_counter()
+        _, hit = pc.run(ctx, c, st, **opts)
+        t1 = time.perf_counter()
+        ctx.sync()
+        hits.append(time.perf_counter() - t0)
+        host.append(t1 - t0)
+        assert hit and not hit0
+    del st
+    return {"workload": "the headline circuit through qsg_plan_cache_run "
+                        "(tensor-core f = 6)",
+            "fuse_s": fuse_s, "first_run_s": first_s,
+            "hit_run_s": max_over_ranks(dist, statistics.median(hits)),
+            "hit_host_call_ms": statistics.median(host) * 1e3,
+            "stats": pc.stats()}
+
+
+UNITARY_GRID = dict(rows=2, cols=7, extra=0, cycles=14, seed=1)
+
+
+def bench_unitary(ctx, dist, cpu: bool):
+    """Unitary of the 14-qubit 2x7 grid depth-14 circuit (2^28 complex64
+    entries, 2 GiB > L2): seconds per unitary (SetIdentity + the fused plan
+    applied by the unitary calculator) for the CUDA-core f = 4 plan and the
+    tensor-core f = 6 plan, GB/s per pass (16 bytes per entry), and on rank
+    0 the oracle's OpenMP FP32 port of the same gate passes on the host
+    (the first fused ops of the f = 4 plan, extrapolated by op count)."""
+    from qsim_gb300 import engine as E
+    from qsim_gb300 import unitary as U
+    g = UNITARY_GRID
+    c = E.Circuit.grid(g["rows"], g["cols"], g["extra"], g["cycles"], g["seed"])
+    n = c.num_qubits
+    us, calc = U.UnitarySpace(ctx=ctx), U.UnitaryCalculator(ctx=ctx)
+    u = us.CreateUnitary(n)
+    entries = 1 << (2 * n)
+    forms = {"plain_f4": E.Plan(c, max_fused_size=4),
+             "tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True)}
+    out = {}
+    for name, plan in forms.items():
+        us.SetIdentity(u)
+        calc.RunPlan(plan, u)       # warm-up (operand upload, attributes)
+        ctx.sync()
+        times = []
+        for _ in range(3):
+            barrier(dist)
+            ctx.timer_start()
+            us.SetIdentity(u)
+            calc.RunPlan(plan, u)
+            times.append(ctx.timer_stop() / 1e3)
+        t = max_over_ranks(dist, statistics.median(times))
+        out[name] = {"s_per_unitary": t, "passes": len(plan),
+                     "gbs_per_pass": 16.0 * entries * len(plan) / t / 1e9}
+    res = {"workload": f"unitary of the {n}-qubit 2x7 grid depth-14 circuit "
+                       f"(seed 1), {entries} complex64 entries",
+           "forms": out,
+           "best": min(out, key=lambda k: out[k]["s_per_unitary"])}
+    us_best = out[res["best"]]["s_per_unitary"]
+    del u
+    if cpu:
+        ops = forms["plain_f4"].ops()
+        t, done, threads = cpu_sample(2 * n, ops, 4)
+        v = t * len(ops) / done
+        res["cpu_baseline"] = {
+            "value": v, "unit": "s/unitary", "cores": threads, "kind": "port",
+            "sample": f"first {done} of {len(ops)} fused ops (f=4 plan) on "
+                      f"the 2 GiB FP32 host unitary, extrapolated by op count"}
+        res["speedup_vs_cpu"] = v / us_best
+    return res
 
 
 LEARN_GRID = dict(rows=5, cols=6, extra=2, cycles=24, seed=1)

@@ -289,6 +289,38 @@ int qsg_plan_replay(qsg_ctx* ctx, qsg_plan* p);
 int qsg_plan_profile(qsg_ctx* ctx, qsg_plan* p, float* state, float* op_ms,
                      uint64_t cap);
 
+/* ---- fused-plan cache ----------------------------------------------------
+ * QSimRunner::Run (lib/run_qsim.h:225-289) fuses the circuit on every call,
+ * after CircuitQsimParser::FromStream (lib/circuit_qsim_parser.h:52-153) for
+ * a text circuit.  A cache keys the fused plan by the circuit's operations
+ * (qsg_plan_cache_run) or by the text and maxtime (qsg_plan_cache_run_text)
+ * together with the fusion options; keys are hashed and compared in full.  A
+ * hit skips parsing and fusion.  A plan without measurements is captured as
+ * a CUDA graph on its first run on a state and replayed on later runs on the
+ * same state and context; plans with measurements run op by op with
+ * measurements from std::mt19937(seed) (as qsg_plan_run).  *hit is 1 when
+ * the plan came from the cache.  Beyond `capacity` plans (0: unbounded) the
+ * least recently used is dropped.  Runs are asynchronous on the context
+ * stream, like qsg_plan_run without measurements.  A cost model is keyed by
+ * its handle: after training a model further, call qsg_plan_cache_clear. */
+typedef struct qsg_plan_cache qsg_plan_cache;
+int qsg_plan_cache_create(unsigned capacity, qsg_plan_cache** out);
+int qsg_plan_cache_destroy(qsg_plan_cache* cache);
+int qsg_plan_cache_clear(qsg_plan_cache* cache);
+int qsg_plan_cache_stats(qsg_plan_cache* cache, uint64_t* hits,
+                         uint64_t* misses, uint64_t* evictions,
+                         uint64_t* captures, uint64_t* size);
+int qsg_plan_cache_run(qsg_ctx* ctx, qsg_plan_cache* cache,
+                       const qsg_circuit* circuit,
+                       const qsg_fuse_options* opts, float* state,
+                       unsigned seed, uint64_t* mbits, uint64_t mbits_cap,
+                       uint64_t* num_meas, int* hit);
+int qsg_plan_cache_run_text(qsg_ctx* ctx, qsg_plan_cache* cache,
+                            const char* text, unsigned maxtime,
+                            const qsg_fuse_options* opts, float* state,
+                            unsigned seed, uint64_t* mbits,
+                            uint64_t mbits_cap, uint64_t* num_meas, int* hit);
+
 /* ---- learned fusion planner --------------------------------------------
  * No counterpart in the reference (its fuser, lib/fuser_mqubit.h:282-526,
  * fuses up to a fixed max_fused_size).  A perceptron with 16 inputs, two

@@ -104,6 +104,14 @@ SIGNATURES = {
     "qsg_plan_capture": (i32, [vp, vp, vp]),
     "qsg_plan_replay": (i32, [vp, vp]),
     "qsg_plan_profile": (i32, [vp, vp, vp, P_f32, u64]),
+    "qsg_plan_cache_create": (i32, [u32, C.POINTER(vp)]),
+    "qsg_plan_cache_destroy": (i32, [vp]),
+    "qsg_plan_cache_clear": (i32, [vp]),
+    "qsg_plan_cache_stats": (i32, [vp, P_u64, P_u64, P_u64, P_u64, P_u64]),
+    "qsg_plan_cache_run": (i32, [vp, vp, vp, vp, vp, u32, P_u64, u64, P_u64,
+                                 C.POINTER(C.c_int)]),
+    "qsg_plan_cache_run_text": (i32, [vp, vp, C.c_char_p, u32, vp, vp, u32,
+                                      P_u64, u64, P_u64, C.POINTER(C.c_int)]),
     "qsg_noisy_create": (i32, [u32, C.POINTER(vp)]),
     "qsg_noisy_destroy": (i32, [vp]),
     "qsg_noisy_info": (i32, [vp, P_u32, P_u64, P_u64]),

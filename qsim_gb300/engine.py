@@ -160,6 +160,64 @@ def pauli_sum(n, count, max_weight, seed):
     return out
 
 
+class PlanCache:
+    """Fused plans keyed by circuit content (qsg_plan_cache): a repeated
+    circuit, given as a Circuit or as qsim text, skips parsing and fusion,
+    and a plan without measurements replays the CUDA graph captured on its
+    first run on the same state."""
+
+    def __init__(self, capacity: int = 64):
+        h = C.c_void_p()
+        check(N.lib.qsg_plan_cache_create(capacity, C.byref(h)))
+        self.h = h
+        self._ctxs = []   # device buffers of cached plans belong to these
+
+    @staticmethod
+    def _opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model):
+        if cost_model is not None and hasattr(cost_model, "h"):
+            cost_model = cost_model.h.value
+        return N.FuseOptions(max_fused_size, seeds, int(tensor_path), tc_min_k,
+                             cost_model)
+
+    def run(self, ctx, circuit, state, seed: int = 1, max_meas: int = 1024,
+            max_fused_size: int = 4, tensor_path: bool = False,
+            tc_min_k: int = 5, seeds: int = 0, cost_model=None,
+            maxtime: int = 0xFFFFFFFF):
+        """QSimRunner::Run of `circuit` (a Circuit, or qsim text as str) on
+        `state`; returns (measured bits, hit)."""
+        if not any(c is ctx for c in self._ctxs):
+            self._ctxs.append(ctx)
+        o = self._opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model)
+        bits = np.zeros(max_meas, dtype=np.uint64)
+        nm, hit = C.c_uint64(), C.c_int()
+        if isinstance(circuit, str):
+            check(N.lib.qsg_plan_cache_run_text(
+                ctx.h, self.h, circuit.encode(), maxtime, C.byref(o),
+                state.get(), seed, bits.ctypes.data_as(N.P_u64), max_meas,
+                C.byref(nm), C.byref(hit)))
+        else:
+            check(N.lib.qsg_plan_cache_run(
+                ctx.h, self.h, circuit.h, C.byref(o), state.get(), seed,
+                bits.ctypes.data_as(N.P_u64), max_meas, C.byref(nm),
+                C.byref(hit)))
+        return bits[:nm.value], bool(hit.value)
+
+    def stats(self):
+        v = [C.c_uint64() for _ in range(5)]
+        check(N.lib.qsg_plan_cache_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("hits", "misses", "evictions", "captures", "size"),
+                        (x.value for x in v)))
+
+    def clear(self):
+        check(N.lib.qsg_plan_cache_clear(self.h))
+
+    def __del__(self):
+        try:
+            N.lib.qsg_plan_cache_destroy(self.h)
+        except Exception:
+            pass
+
+
 class Plan:
     """Fused plan (MultiQubitGateFuser output) ready to run on the GPU."""
 

@@ -23,6 +23,25 @@ namespace qsg {
 void set_error_msg(const char* msg);
 }
 
+namespace qsg {
+namespace host {
+
+bool fuse_options_from(const qsg_fuse_options* o, FuseOptions* out) {
+  FuseOptions fo;
+  if (o) {
+    fo.max_fused_size = o->max_fused_size;
+    fo.seeds = o->seeds ? o->seeds : fo.seeds;
+    fo.tensor_path = o->tensor_path != 0;
+    fo.tc_min_k = o->tc_min_k ? o->tc_min_k : fo.tc_min_k;
+    fo.cost = qsg::cost_model_from_handle(o->cost_model);
+  }
+  *out = fo;
+  return fo.max_fused_size >= 1 && fo.max_fused_size <= 6;
+}
+
+}  // namespace host
+}  // namespace qsg
+
 namespace {
 
 int invalid(const char* msg) {
@@ -223,14 +242,7 @@ int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* o,
   if (!c || !out) return invalid("null argument");
   *out = nullptr;
   FuseOptions fo;
-  if (o) {
-    fo.max_fused_size = o->max_fused_size;
-    fo.seeds = o->seeds ? o->seeds : fo.seeds;
-    fo.tensor_path = o->tensor_path != 0;
-    fo.tc_min_k = o->tc_min_k ? o->tc_min_k : fo.tc_min_k;
-    fo.cost = qsg::cost_model_from_handle(o->cost_model);
-  }
-  if (fo.max_fused_size < 1 || fo.max_fused_size > 6)
+  if (!fuse_options_from(o, &fo))
     return invalid("max_fused_size must be 1..6");
   auto* p = new qsg_plan();
   p->rt.plan = fuse(c->c, fo);
