@@ -370,12 +370,15 @@ def run_engine(args, world, rank, local, dist):
         expect = {"skipped": "--headline-only"}
         unitary = {"skipped": "--headline-only"}
         cache = {"skipped": "--headline-only"}
+        hyb = {"skipped": "--headline-only"}
     else:
         learned = bench_learned_planner(ctx, ss, model, dist)
         expect = bench_expectations(ctx, ss, dist)
         unitary = bench_unitary(ctx, dist, cpu=(rank == 0 and world == 1
                                                 and not args.no_cpu))
         cache = bench_plan_cache(ctx, ss, dist)
+        hyb = bench_hybrid(ctx, dist, cpu=(rank == 0 and world == 1
+                                           and not args.no_cpu))
         traj = bench_trajectories(args.traj_streams, args.traj_f,
                                   mode=args.traj_mode,
                                   ctas_per_sm=args.traj_ctas_per_sm,
@@ -426,6 +429,7 @@ def run_engine(args, world, rank, local, dist):
             "expectations": expect,
             "unitary": unitary,
             "plan_cache": cache,
+            "hybrid": hyb,
         }
         print(json.dumps(line), flush=True)
 
@@ -540,6 +544,113 @@ def bench_plan_cache(ctx, ss, dist):
             "hit_run_s": max_over_ranks(dist, statistics.median(hits)),
             "hit_host_call_ms": statistics.median(host) * 1e3,
             "stats": pc.stats()}
+
+
+HYBRID = dict(rows=4, cols=8, extra=0, cycles=14, seed=1, prefix_gates=4,
+              bitstrings=1000, batch_bits=16)
+
+
+def bench_hybrid(ctx, dist, cpu: bool):
+    """One qsimh job on the 32-qubit 4x8 grid depth-14 circuit cut into
+    column halves (16 + 16 qubits, 12 fSim gates on the cut): the first 4
+    cut gates fixed by the job's prefix, the other 8 (16 path bits = 65536
+    paths) summed for 1000 bitstring amplitudes.  Wall seconds of the whole
+    qsg_hybrid_run call (split, fusion, device runs, amplitude read-back),
+    CUDA-core f = 4 and tensor-core f = 6.  CPU baseline: the oracle's
+    OpenMP FP32 gate application over each part's post-checkpoint gates
+    (fused to <= 2 qubits, as the reference's qsimh runner fuses), which the
+    reference runs once per path (lib/hybrid.h:381-433), timed on sample
+    paths and multiplied by the path count."""
+    import numpy as np
+    from qsim_gb300 import engine as E, hybrid
+    h = HYBRID
+    c = E.Circuit.grid(h["rows"], h["cols"], h["extra"], h["cycles"], h["seed"])
+    n = c.num_qubits
+    parts = [0 if (q % h["cols"]) < h["cols"] // 2 else 1 for q in range(n)]
+    rng = np.random.default_rng(11)
+    bits = rng.integers(0, 1 << n, h["bitstrings"], dtype=np.uint64)
+    out = {}
+    for name, kw in (("plain_f4", dict(max_fused_size=4)),
+                     ("tc_f6", dict(max_fused_size=6, tensor_path=True))):
+        args = dict(num_prefix_gatexs=h["prefix_gates"],
+                    max_batch_bits=h["batch_bits"], **kw)
+        hybrid.run(ctx, c, parts, bits[:8], **args)       # warm-up
+        times = []
+        for _ in range(2):
+            barrier(dist)
+            t0 = time.perf_counter()
+            amps, info = hybrid.run(ctx, c, parts, bits, **args)
+            times.append(time.perf_counter() - t0)
+        t = max_over_ranks(dist, min(times))
+        out[name] = {"s_per_job": t, "paths_per_s": info["paths_run"] / t,
+                     "amplitudes_norm2": float(np.sum(np.abs(amps) ** 2))}
+    best = min(out, key=lambda k: out[k]["s_per_job"])
+    res = {"workload": f"qsimh job: {n}-qubit 4x8 grid depth 14 (seed 1), "
+                       f"parts = column halves, {info['num_gatexs']} gates on "
+                       f"the cut, {h['prefix_gates']} fixed by the prefix, "
+                       f"{info['paths_run']} paths, {len(bits)} amplitudes",
+           "info": info, "forms": out, "best": best}
+    if cpu:
+        res["cpu_baseline"] = hybrid_cpu_sample(c, parts, h["prefix_gates"],
+                                                info["paths_run"])
+        res["speedup_vs_cpu"] = (res["cpu_baseline"]["value"]
+                                 / out[best]["s_per_job"])
+    return res
+
+
+def hybrid_cpu_sample(c, parts, num_prefix, paths, max_paths=16):
+    """The reference's per-path work (both parts' gates after the root
+    checkpoint, one path at a time) on the host cores with the oracle's
+    OpenMP FP32 gate application; seconds per job = mean per path x paths."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from conftest import Oracle
+    import hybrid_oracle as HO
+    from qsim_gb300 import engine as E
+    orc = Oracle()
+    ops = c.ops()
+    for i, o in enumerate(ops):
+        o["schmidt"] = c.schmidt(i) if len(o["qs"]) == 2 else []
+    n0, n1, _, part_ops, cuts = HO.split_lattice(c.num_qubits, ops, parts)
+    P = C.POINTER
+    rng = np.random.default_rng(2)
+    t_total, done = 0.0, 0
+    for _ in range(max_paths):
+        for p, np_ in ((0, n0), (1, n1)):
+            st = np.zeros(2 << np_, dtype=np.float32)
+            st[0] = 1.0
+            first = next(i for i, o in enumerate(part_ops[p])
+                         if o["cut"] >= num_prefix)
+            # One path's gates, fused into <= 2-qubit blocks as the
+            # reference's qsimh runner does (BasicGateFuser).
+            pc = E.Circuit(np_)
+            for o in part_ops[p][first:]:
+                if o["cut"] < 0:
+                    pc.add_gate(o["time"], o["qs"], o["m"])
+                else:
+                    g = cuts[o["cut"]]
+                    pc.add_gate(o["time"], [g["q"][p]],
+                                g["f"][p][int(rng.integers(g["terms"]))])
+            mats = [(o["qs"], np.ascontiguousarray(
+                np.asarray(o["m"], np.complex64)).view(np.float32))
+                for o in E.Plan(pc, max_fused_size=2).ops()]
+            t0 = time.perf_counter()
+            for qs, m in mats:
+                qa = (C.c_uint * len(qs))(*qs)
+                orc.L.orc_apply_gate_f32(st.ctypes.data_as(P(C.c_float)), np_,
+                                         qa, len(qs),
+                                         m.ctypes.data_as(P(C.c_float)))
+            t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > 15.0:
+            break
+    per_path = t_total / done
+    return {"value": per_path * paths, "unit": "s/job",
+            "cores": orc.L.orc_num_threads(), "kind": "port",
+            "sample": f"{done} sample paths (both parts' post-checkpoint "
+                      f"gates fused into <= 2-qubit blocks, oracle OpenMP "
+                      f"FP32 port), x {paths} paths"}
 
 
 UNITARY_GRID = dict(rows=2, cols=7, extra=0, cycles=14, seed=1)

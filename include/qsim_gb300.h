@@ -520,6 +520,50 @@ int qsg_unitary_apply_controlled_gate(qsg_ctx* ctx, float* u, unsigned n,
  * with measurements are rejected. */
 int qsg_unitary_run_plan(qsg_ctx* ctx, qsg_plan* p, float* u, unsigned n);
 
+/* ---- hybrid Schrodinger-Feynman simulation (qsimh) ----------------------
+ * QSimHRunner::Run (lib/run_qsimh.h:43-104) over HybridSimulator
+ * (lib/hybrid.h): the qubits are cut into parts[q] = 0 or 1; two-qubit gates
+ * across the cut are replaced by their operator Schmidt terms (named gates
+ * id2, cz, cnot/cx, sw, is, fs, cp, as lib/gates_qsim.h); the amplitudes of
+ * `bitstrings` (bit q = qubit q) are summed over the paths of the cut gates
+ * with the first num_prefix_gatexs gates' terms fixed by `prefix` and the
+ * rest summed, and ADDED to results (interleaved complex double, as the
+ * reference adds to its results vector).  Only one- and two-qubit matrix
+ * gates are allowed (QSG_ERR_UNSUPPORTED otherwise).  The paths of the
+ * suffix gates (after the num_root_gatexs root gates) run as one batch on
+ * the device: up to max_batch_bits path bits (0: as many as fit in 45 % of
+ * free HBM), the others loop on the host like the root paths.  All paths
+ * are summed whatever the split, so the split changes speed only. */
+typedef struct qsg_hybrid_options {
+  uint64_t prefix;
+  unsigned num_prefix_gatexs;
+  unsigned num_root_gatexs;
+  unsigned max_fused_size;   /* 0: 4 */
+  int tensor_path;           /* fused blocks of >= 5 qubits on tcgen05 */
+  unsigned max_batch_bits;   /* 0: by free memory */
+} qsg_hybrid_options;
+typedef struct qsg_hybrid_info {
+  unsigned num_qubits0, num_qubits1;
+  unsigned num_ops0, num_ops1;  /* per part, cut gates included */
+  unsigned num_gatexs;          /* gates on the cut */
+  unsigned prefix_bits, root_bits, suffix_bits;
+  unsigned batch_bits;          /* suffix path bits run as one batch */
+  uint64_t paths_run;
+} qsg_hybrid_info;
+/* HybridSimulator::SplitLattice: counts only (no GPU). */
+int qsg_hybrid_split(const qsg_circuit* c, const unsigned* parts,
+                     unsigned num_parts, qsg_hybrid_info* info);
+int qsg_hybrid_run(qsg_ctx* ctx, const qsg_circuit* c, const unsigned* parts,
+                   unsigned num_parts, const qsg_hybrid_options* opts,
+                   const uint64_t* bitstrings, uint64_t num_bitstrings,
+                   double* results, qsg_hybrid_info* info);
+/* Operator Schmidt terms of circuit op i (two-qubit named gates): terms[16 t
+ * .. 16 t + 7] = factor on the op's first (lower) qubit, then 8 values of the
+ * factor on its second qubit, each a 2x2 row-major interleaved complex
+ * matrix; *num_terms = 0 for other ops.  terms may be NULL. */
+int qsg_circuit_get_schmidt(const qsg_circuit* c, uint64_t i,
+                            unsigned* num_terms, double* terms);
+
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,
  * qsg_timer_stop records a second one, synchronises and returns the elapsed

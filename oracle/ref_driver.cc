@@ -46,6 +46,12 @@
 //       (SimulatorBasic).  Writes per repetition the count and the
 //       stat.samples (.stat32 / .stat64, uint64) and the final state in
 //       normal order (.f32 / .f64).
+//   hybrid <circuit.txt> <out> <num_prefix> <num_root> <prefix> <parts>
+//          <bitstrings>
+//       QSimHRunner<IO, BasicGateFuser, HybridSimulator>::Run on the text
+//       circuit (CircuitQsimParser, double), parts as "0,1,1,...", the
+//       bitstrings a raw uint64 file; writes the amplitudes as complex
+//       doubles (each result starts from 0).
 //   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
 //       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
 //       with one std::mt19937(seed); writes bits per round (.bits) and the
@@ -66,14 +72,17 @@
 #include "circuit_qsim_parser.h"
 #include "io_file.h"
 #include "formux.h"
+#include "fuser_basic.h"
 #include "fuser_mqubit.h"
 #include "gate.h"
 #include "gate_appl.h"
 #include "gates_qsim.h"
+#include "hybrid.h"
 #include "io.h"
 #include "operation.h"
 #include "qtrajectory.h"
 #include "run_qsim.h"
+#include "run_qsimh.h"
 #include "simmux.h"
 #include "simulator_basic.h"
 #include "statespace_basic.h"
@@ -437,11 +446,51 @@ static int CmdUnitary(int argc, char** argv) {
   return 0;
 }
 
+struct HybridFactory {
+  using Simulator = SimulatorBasic<For, double>;
+  using StateSpace = Simulator::StateSpace;
+  using fp_type = double;
+  StateSpace CreateStateSpace() const { return StateSpace(1); }
+  Simulator CreateSimulator() const { return Simulator(1); }
+};
+
+static int CmdHybrid(int argc, char** argv) {
+  if (argc < 9) return 2;
+  Circuit<Operation<double>> circuit;
+  if (!CircuitQsimParser<IOFile>::FromFile(~0u, argv[2], circuit)) return 1;
+  std::vector<unsigned> parts;
+  {
+    std::stringstream ss(argv[7]);
+    std::string tok;
+    while (std::getline(ss, tok, ',')) parts.push_back(std::stoul(tok));
+  }
+  std::vector<uint64_t> bitstrings;
+  {
+    std::ifstream in(argv[8], std::ios::binary);
+    uint64_t b;
+    while (in.read(reinterpret_cast<char*>(&b), sizeof(b))) bitstrings.push_back(b);
+  }
+  using HS = HybridSimulator<IO, For>;
+  using Runner = QSimHRunner<IO, BasicGateFuser<IO>, HS>;
+  Runner::Parameter param;
+  param.num_prefix_gatexs = std::stoul(argv[4]);
+  param.num_root_gatexs = std::stoul(argv[5]);
+  param.prefix = std::stoull(argv[6]);
+  param.num_threads = 1;
+  param.verbosity = 0;
+  std::vector<std::complex<double>> results(bitstrings.size(), 0);
+  if (!Runner::Run(param, HybridFactory(), circuit, parts, bitstrings, results))
+    return 1;
+  WriteRaw(argv[3], results.data(), sizeof(std::complex<double>) * results.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   if (std::string(argv[1]) == "unitary") return CmdUnitary(argc, argv);
   std::string cmd = argv[1];
   if (cmd == "text") return CmdText(argc, argv);
+  if (cmd == "hybrid") return CmdHybrid(argc, argv);
   if (cmd == "fuse") return CmdFuse(argc, argv);
   if (cmd == "mt") return CmdMt(argc, argv);
   if (cmd == "run") return CmdRun(argc, argv);

@@ -140,6 +140,9 @@ SIGNATURES = {
     "qsg_unitary_apply_controlled_gate": (i32, [vp, vp, u32, P_u32, u32, P_u32,
                                                 u32, u64, P_f32]),
     "qsg_unitary_run_plan": (i32, [vp, vp, vp, u32]),
+    "qsg_hybrid_split": (i32, [vp, P_u32, u32, vp]),
+    "qsg_hybrid_run": (i32, [vp, vp, P_u32, u32, vp, P_u64, u64, P_f64, vp]),
+    "qsg_circuit_get_schmidt": (i32, [vp, u64, P_u32, P_f64]),
     "qsg_traj_run_packed": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                   vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                   P_u64, vp]),
@@ -169,6 +172,20 @@ class FuseOptions(C.Structure):
     _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
                 ("tensor_path", C.c_int), ("tc_min_k", C.c_uint),
                 ("cost_model", C.c_void_p)]
+
+
+class HybridOptions(C.Structure):
+    _fields_ = [("prefix", C.c_uint64), ("num_prefix_gatexs", C.c_uint),
+                ("num_root_gatexs", C.c_uint), ("max_fused_size", C.c_uint),
+                ("tensor_path", C.c_int), ("max_batch_bits", C.c_uint)]
+
+
+class HybridInfo(C.Structure):
+    _fields_ = [("num_qubits0", C.c_uint), ("num_qubits1", C.c_uint),
+                ("num_ops0", C.c_uint), ("num_ops1", C.c_uint),
+                ("num_gatexs", C.c_uint), ("prefix_bits", C.c_uint),
+                ("root_bits", C.c_uint), ("suffix_bits", C.c_uint),
+                ("batch_bits", C.c_uint), ("paths_run", C.c_uint64)]
 
 
 class TrajOptions(C.Structure):

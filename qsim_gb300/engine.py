@@ -138,6 +138,19 @@ class Circuit:
     def ops(self):
         return [self.op(i) for i in range(len(self))]
 
+    def schmidt(self, i: int):
+        """Operator Schmidt terms of op i (two-qubit named gates): a list of
+        (A, B), A the 2x2 factor on the op's first qubit; [] otherwise."""
+        t = C.c_uint()
+        check(N.lib.qsg_circuit_get_schmidt(self.h, i, C.byref(t), None))
+        buf = np.zeros(16 * max(1, t.value), dtype=np.float64)
+        check(N.lib.qsg_circuit_get_schmidt(self.h, i, C.byref(t),
+                                            buf.ctypes.data_as(N.P_f64)))
+        c = buf.view(np.complex128)
+        return [(c[8 * j:8 * j + 4].reshape(2, 2).copy(),
+                 c[8 * j + 4:8 * j + 8].reshape(2, 2).copy())
+                for j in range(t.value)]
+
     def __del__(self):
         try:
             N.lib.qsg_circuit_destroy(self.h)
@@ -265,6 +278,19 @@ class Plan:
 
     def ops(self):
         return [self.op(i) for i in range(len(self))]
+
+    def schmidt(self, i: int):
+        """Operator Schmidt terms of op i (two-qubit named gates): a list of
+        (A, B), A the 2x2 factor on the op's first qubit; [] otherwise."""
+        t = C.c_uint()
+        check(N.lib.qsg_circuit_get_schmidt(self.h, i, C.byref(t), None))
+        buf = np.zeros(16 * max(1, t.value), dtype=np.float64)
+        check(N.lib.qsg_circuit_get_schmidt(self.h, i, C.byref(t),
+                                            buf.ctypes.data_as(N.P_f64)))
+        c = buf.view(np.complex128)
+        return [(c[8 * j:8 * j + 4].reshape(2, 2).copy(),
+                 c[8 * j + 4:8 * j + 8].reshape(2, 2).copy())
+                for j in range(t.value)]
 
     def run(self, ctx, state, seed: int = 1, max_meas: int = 1024):
         self._ctx = ctx   # the plan's device buffers belong to this context

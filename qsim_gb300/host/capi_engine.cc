@@ -220,6 +220,21 @@ int qsg_circuit_get_op(const qsg_circuit* c, uint64_t i, int* kind,
   return QSG_OK;
 }
 
+int qsg_circuit_get_schmidt(const qsg_circuit* c, uint64_t i,
+                            unsigned* num_terms, double* terms) {
+  if (!c || !num_terms || i >= c->c.ops.size())
+    return invalid("op index out of range");
+  const Op& op = c->c.ops[i];
+  *num_terms = unsigned(op.schmidt.size() / 8);
+  if (terms) {
+    for (size_t j = 0; j < op.schmidt.size(); ++j) {
+      terms[2 * j] = op.schmidt[j].real();
+      terms[2 * j + 1] = op.schmidt[j].imag();
+    }
+  }
+  return QSG_OK;
+}
+
 int qsg_pauli_sum(unsigned n, unsigned count, unsigned max_weight,
                   uint64_t seed, unsigned* weights, unsigned* qubits,
                   char* letters, double* coeffs) {

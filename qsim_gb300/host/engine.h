@@ -30,6 +30,10 @@ struct Op {
   std::vector<unsigned> cqs;
   uint64_t cvals = 0;
   std::vector<cplx> m;
+  // Two-qubit named gates: operator Schmidt terms, U = sum_t A_t (x) B_t,
+  // 8 values per term: A_t on qs[0] then B_t on qs[1] (2x2 row-major).
+  // Empty for other gates.  Used by the hybrid simulator (hybrid.cc).
+  std::vector<cplx> schmidt;
 };
 
 struct Circuit {
@@ -47,6 +51,11 @@ bool named_gate(const std::string& name, unsigned time,
                 const std::vector<unsigned>& qubits,
                 const std::vector<double>& params, Op* out);
 std::vector<cplx> u3_matrix(double theta, double phi, double lambda);
+// Operator Schmidt terms of a two-qubit named gate with the qubits in the
+// given order (8 values per term, first the factor on qubits[0]); empty for
+// names without a decomposition.
+std::vector<cplx> schmidt_terms(const std::string& name,
+                                const std::vector<double>& params);
 // Kronecker product of Pauli letters; letter j acts on sorted qubit j.
 std::vector<cplx> pauli_string_matrix(const std::string& letters);
 

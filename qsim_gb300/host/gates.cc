@@ -163,7 +163,84 @@ bool named_gate(const std::string& name, unsigned time,
     return false;
   }
   *out = make_gate(time, q, std::move(m));
+  if (q.size() == 2) {
+    out->schmidt = schmidt_terms(name, p);
+    if (q[0] > q[1]) {
+      // make_gate sorted the qubits: the factors trade places.
+      for (size_t t = 0; t + 8 <= out->schmidt.size(); t += 8)
+        std::swap_ranges(out->schmidt.begin() + t, out->schmidt.begin() + t + 4,
+                         out->schmidt.begin() + t + 4);
+    }
+  }
   return true;
+}
+
+// Operator Schmidt terms of the two-qubit gates (lib/gates_qsim.h:382-651
+// lists the same decompositions).  A path of the hybrid simulator picks one
+// term per gate on the cut, so partial sums over fixed path bits equal the
+// reference's only with these terms, which is why they are the same.
+//   id2        I (x) I
+//   cz, cp     |0><0| (x) I + |1><1| (x) diag(1, e^{-i phi})   (cz: phi = pi)
+//   cnot       |0><0| (x) I + |1><1| (x) X                     (control first)
+//   sw         (I I + X X + Y Y + Z Z) / 2
+//   is         (I I + Z Z) / 2 + i (X X + Y Y) / 2
+//   fs         diagonal part D = A (x) A + E (x) E (rank 2) plus
+//              -i sin(theta) (X X + Y Y) / 2 (rank 2)
+std::vector<cplx> schmidt_terms(const std::string& name,
+                                const std::vector<double>& p) {
+  const double is2 = std::sqrt(0.5);
+  const cplx P0[4] = {1, 0, 0, 0}, P1[4] = {0, 0, 0, 1};
+  const cplx Id[4] = {1, 0, 0, 1}, X[4] = {0, 1, 1, 0};
+  const cplx Y[4] = {0, -I, I, 0}, Z[4] = {1, 0, 0, -1.0};
+  std::vector<cplx> t;
+  auto term = [&](const cplx* a, cplx ca, const cplx* b, cplx cb) {
+    for (int j = 0; j < 4; ++j) t.push_back(ca * a[j]);
+    for (int j = 0; j < 4; ++j) t.push_back(cb * b[j]);
+  };
+  if (name == "id2") {
+    term(Id, 1.0, Id, 1.0);
+  } else if (name == "cz" || name == "cp") {
+    const cplx ph = name == "cz" ? cplx(-1.0) : std::exp(-I * p.at(0));
+    const cplx D[4] = {1, 0, 0, ph};
+    term(P0, 1.0, Id, 1.0);
+    term(P1, 1.0, D, 1.0);
+  } else if (name == "cnot" || name == "cx") {
+    term(P0, 1.0, Id, 1.0);
+    term(P1, 1.0, X, 1.0);
+  } else if (name == "sw") {
+    term(Id, is2, Id, is2);
+    term(X, is2, X, is2);
+    term(Y, is2, Y, is2);
+    term(Z, is2, Z, is2);
+  } else if (name == "is") {
+    const cplx c(0.5, 0.5);  // c^2 = i/2
+    term(Id, is2, Id, is2);
+    term(X, c, X, c);
+    term(Y, c, Y, c);
+    term(Z, is2, Z, is2);
+  } else if (name == "fs") {
+    const double theta = p.at(0);
+    double phi = p.at(1);
+    if (phi < 0) phi += 2 * kPi;
+    const double ct = std::cos(theta), st = std::sin(theta);
+    // D = diag(1, ct, ct, e^{-i phi}) = A (x) A + E (x) E with
+    // A = z0 / sqrt2 diag(w, 1/w), E = z1 / sqrt2 diag(w, -1/w),
+    // w = e^{i phi / 4}, z0^2 = e^{-i phi / 2} + ct, z1^2 = e^{-i phi / 2} - ct
+    // (principal roots).
+    const cplx w = std::exp(I * (0.25 * phi));
+    const cplx h2 = std::exp(-I * (0.5 * phi));
+    const cplx z0 = std::sqrt(h2 + ct) * is2, z1 = std::sqrt(h2 - ct) * is2;
+    const cplx A[4] = {z0 * w, 0, 0, z0 / w}, E[4] = {z1 * w, 0, 0, -z1 / w};
+    // -i st (X X + Y Y) / 2 = (f X) (x) (g X) + (f Y) (x) (g Y) with
+    // f = sqrt|st| (1 - i) / 2 and g = f sign(st).
+    const cplx f = std::sqrt(std::abs(st)) * cplx(0.5, -0.5);
+    const cplx g = st < 0 ? -f : f;
+    term(A, 1.0, A, 1.0);
+    term(X, f, X, g);
+    term(Y, f, Y, g);
+    term(E, 1.0, E, 1.0);
+  }
+  return t;
 }
 
 }  // namespace host

@@ -24,6 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+# The reference checkout whose test files hold known answers.
+REF_ROOT = os.environ.get("QSIM_REF", "/root/reference")
 
 PAULI = {
     "I": np.eye(2, dtype=np.complex128),
@@ -448,6 +450,144 @@ def unitary_cases():
     unitary_case("unitary7", 7, small_gate_list(rng, 7, 30, 4, 0.2))
 
 
+def random_hybrid_text(rng, n, layers, parts, max_cut):
+    """One- and two-qubit named gates only (the hybrid simulator's gate set),
+    two-qubit gates on random pairs in random order, at most `max_cut` of
+    them across the cut (each cut gate adds up to two path bits), angles
+    exact in float."""
+    lines = [str(n)]
+    cut = 0
+    for t in range(layers):
+        perm = rng.permutation(n).tolist()
+        used = set()
+        for i, q in enumerate(perm):
+            if q in used:
+                continue
+            used.add(q)
+            free = [p for p in perm[i + 1:] if p not in used]
+            same = [p for p in free if parts[p] == parts[q]]
+            other = [p for p in free if parts[p] != parts[q]]
+            r = rng.random()
+            ang = lambda: f"{int(rng.integers(-400, 400)) / 64}"
+            two = r >= 0.45 and (same or (other and cut < max_cut))
+            if not two:
+                if r < 0.3:
+                    g = GATES_1Q[int(rng.integers(len(GATES_1Q)))]
+                    lines.append(f"{t} {g} {q}")
+                else:
+                    g, npar = GATES_1Q_P[int(rng.integers(len(GATES_1Q_P)))]
+                    lines.append(f"{t} {g} {q} " + " ".join(ang() for _ in range(npar)))
+                continue
+            pool = other if (other and cut < max_cut and rng.random() < 0.5) or not same else same
+            p2 = pool[int(rng.integers(len(pool)))]
+            used.add(p2)
+            if parts[p2] != parts[q]:
+                cut += 1
+            a, b = (q, p2) if rng.random() < 0.5 else (p2, q)
+            if rng.random() < 0.6:
+                g = GATES_2Q[int(rng.integers(len(GATES_2Q)))]
+                lines.append(f"{t} {g} {a} {b}")
+            else:
+                g, npar = GATES_2Q_P[int(rng.integers(len(GATES_2Q_P)))]
+                # fs angles with sin(theta) >= 0 (the reference's fs
+                # decomposition takes sqrt(sin(theta))).
+                ps = [f"{int(rng.integers(0, 200)) / 64}"] if g == "fs" else []
+                ps += [ang() for _ in range(npar - len(ps))]
+                lines.append(f"{t} {g} {a} {b} " + " ".join(ps))
+    return "\n".join(lines) + "\n"
+
+
+def hybrid_run(text, parts, np_, nr, prefix, bitstrings):
+    with tempfile.TemporaryDirectory() as td:
+        cp = os.path.join(td, "c.txt")
+        bp = os.path.join(td, "b.u64")
+        op = os.path.join(td, "out")
+        with open(cp, "w") as f:
+            f.write(text)
+        np.asarray(bitstrings, np.uint64).tofile(bp)
+        subprocess.run([DRIVER, "hybrid", cp, op, str(np_), str(nr), str(prefix),
+                        ",".join(str(int(x)) for x in parts), bp], check=True)
+        return np.fromfile(op, np.complex128)
+
+
+def hybrid_known_case():
+    """The reference's own hybrid known-answer tests
+    (tests/hybrid_testfixture.h: circuits, parts, runs and EXPECT_NEAR
+    values), read from the reference's test file, checked against the
+    reference driver here and stored as a fixture."""
+    import re
+    src = open(os.path.join(REF_ROOT, "tests", "hybrid_testfixture.h")).read()
+    bodies = src.split("void TestHybrid")[1:]
+    cases = []
+    for body in bodies:
+        text = re.search(r'R"\((.*?)\)"', body, re.S).group(1)
+        text = text.lstrip("\n")
+        parts = [int(x) for x in re.search(
+            r"std::vector<unsigned> parts = \{([^}]*)\};", body).group(1).split(",")]
+        nres = int(re.search(r"results\((\d+), 0\)", body).group(1))
+        counts = [int(re.search(r"EXPECT_EQ\(hd\.%s(?:\.size\(\))?, (\d+)\);" % k,
+                                body).group(1))
+                  for k in ("ops0", "ops1", "gatexs", "num_qubits0", "num_qubits1")]
+        runs, cur = [], {}
+        for line in body.splitlines():
+            m = re.search(r"param\.(prefix|num_prefix_gatexs|num_root_gatexs) = (\d+);", line)
+            if m:
+                cur[m.group(1)] = int(m.group(2))
+            if "HybridSimulator(1).Run(" in line:
+                runs.append(dict(cur, want=np.zeros(nres, np.complex128),
+                                 seen=np.zeros((nres, 2), bool)))
+            m = re.search(r"EXPECT_NEAR\(std::(real|imag)\(results\[(\d+)\]\), "
+                          r"([-0-9.e]+), ", line)
+            if m and runs:
+                i, v = int(m.group(2)), float(m.group(3))
+                if m.group(1) == "real":
+                    runs[-1]["want"][i] += v
+                    runs[-1]["seen"][i, 0] = True
+                else:
+                    runs[-1]["want"][i] += 1j * v
+                    runs[-1]["seen"][i, 1] = True
+        for r in runs:
+            k = int(r["seen"].all(axis=1).sum())   # results with expectations
+            got = hybrid_run(text, parts, r["num_prefix_gatexs"],
+                             r["num_root_gatexs"], r["prefix"], range(k))
+            assert np.abs(got - r["want"][:k]).max() < 1e-6, (got, r["want"])
+            cases.append(dict(text=text, parts=parts, counts=counts,
+                              prefix=r["prefix"],
+                              np=r["num_prefix_gatexs"], nr=r["num_root_gatexs"],
+                              want=r["want"][:k]))
+    out = {}
+    for i, c in enumerate(cases):
+        for key, v in c.items():
+            out[f"{key}{i}"] = np.array(v)
+    np.savez_compressed(os.path.join(HERE, "hybrid_known.npz"),
+                        count=np.int32(len(cases)), **out)
+    print("hybrid_known written:", len(cases), "runs")
+
+
+def hybrid_random_cases():
+    """Seeded circuits of 6..10 qubits: parts contiguous or interleaved,
+    prefix / root / suffix splits including a nonzero prefix; amplitudes of
+    every bitstring (n <= 8) or 256 random ones, from the reference."""
+    rng = np.random.default_rng(4242)
+    specs = [("hybrid6", 6, 10, [0, 0, 0, 1, 1, 1], [(0, 0, 0), (0, 2, 0), (2, 1, 1)]),
+             ("hybrid8", 8, 12, [0, 1, 0, 1, 1, 0, 0, 1], [(0, 0, 0), (1, 2, 0), (3, 0, 2)]),
+             ("hybrid10", 10, 14, [0] * 5 + [1] * 5, [(0, 0, 0), (0, 3, 0), (2, 2, 2)])]
+    for name, n, layers, parts, runs in specs:
+        text = random_hybrid_text(rng, n, layers, parts, 7)
+        if n <= 8:
+            bits = np.arange(1 << n, dtype=np.uint64)
+        else:
+            bits = rng.choice(1 << n, 256, replace=False).astype(np.uint64)
+        res = []
+        for np_, nr, prefix in runs:
+            res.append(hybrid_run(text, parts, np_, nr, prefix, bits))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), n=np.int32(n),
+                            text=np.array(text), parts=np.array(parts, np.uint32),
+                            runs=np.array(runs, np.uint64), bits=bits,
+                            amps=np.array(res))
+        print(name, "written")
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
@@ -457,7 +597,10 @@ def main():
     if sys.argv[1:] == ["unitary"]:
         unitary_cases()
         return
-        sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
+    if sys.argv[1:] == ["hybrid"]:
+        hybrid_known_case()
+        hybrid_random_cases()
+        return
     mt_case()
     text_case("text_gates9", 9, 30, 5)
     fuse_counts_case()
@@ -482,6 +625,8 @@ def main():
              measure=(17, 6, [0, 5, 13]))
     traj_cases()
     unitary_cases()
+    hybrid_known_case()
+    hybrid_random_cases()
 
 
 if __name__ == "__main__":
