@@ -51,6 +51,28 @@ def test_reference_apply_gate_compiles_with_gb300_unitary(tmp_path):
                  extra=("-I" + os.path.join(REF, "lib"),))
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lib")),
+                    reason="qsim checkout (reference headers) not present")
+def test_reference_circuits_compile_with_gb300_hybrid_runner(tmp_path):
+    """qsim's Circuit<Operation<float>> and text parser drive
+    QSimHRunnerGB300 with the Parameter fields of apps/qsimh_base.cc."""
+    exe = str(tmp_path / "dropin_hybrid")
+    compile_prog("dropin_hybrid.cc", exe, extra=("-I" + os.path.join(REF, "lib"),))
+    # The adapter's circuit conversion (no GPU) against the reference's own
+    # SplitLattice counts and gate matrices, on every hybrid fixture.
+    cases = [(load_golden(c), None) for c in ("hybrid6", "hybrid8", "hybrid10")]
+    kd = load_golden("hybrid_known")
+    cases += [(None, (str(kd[f"text{i}"]), kd[f"parts{i}"].tolist()))
+              for i in (0, 4)]
+    for d, known in cases:
+        text, parts = (str(d["text"]), d["parts"].tolist()) if d is not None else known
+        cp = tmp_path / "c.txt"
+        cp.write_text(text)
+        r = subprocess.run([exe, "--check", str(cp), "".join(str(p) for p in parts)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout)
+
+
 @pytest.mark.gpu
 def test_adapter_program_matches_reference(tmp_path, oracle):
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
