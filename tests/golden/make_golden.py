@@ -588,6 +588,192 @@ def hybrid_random_cases():
         print(name, "written")
 
 
+# ---- qsim_cuda-compatible module (pybind_interface) ----------------------
+# Circuits are described as data (JSON) and built through the module API, so
+# the same description drives the reference's module (built from its
+# sources by `make -C oracle pybind`) here and qsim_gb300.qsim_cuda in the
+# tests.
+
+_EXP = ("exponent", "global_shift")
+PARAM_KINDS = {
+    "kXPowGate": _EXP, "kYPowGate": _EXP, "kZPowGate": _EXP, "kHPowGate": _EXP,
+    "kCZPowGate": _EXP, "kCXPowGate": _EXP, "krx": ("phi",), "kry": ("phi",),
+    "krz": ("phi",), "kPhasedXPowGate": ("phase_exponent",) + _EXP,
+    "kPhasedXZGate": ("x_exponent", "z_exponent", "axis_phase_exponent"),
+    "kXXPowGate": _EXP, "kYYPowGate": _EXP, "kZZPowGate": _EXP,
+    "kSwapPowGate": _EXP, "kISwapPowGate": _EXP, "kriswap": ("phi",),
+    "kPhasedISwapPowGate": ("phase_exponent", "exponent"), "kgivens": ("phi",),
+    "kFSimGate": ("theta", "phi"), "kCCZPowGate": _EXP, "kCCXPowGate": _EXP,
+}
+KIND_QUBITS = {
+    "kI1": 1, "kI2": 2, "kXPowGate": 1, "kYPowGate": 1, "kZPowGate": 1,
+    "kHPowGate": 1, "kCZPowGate": 2, "kCXPowGate": 2, "krx": 1, "kry": 1,
+    "krz": 1, "kH": 1, "kS": 1, "kCZ": 2, "kCX": 2, "kT": 1, "kX": 1, "kY": 1,
+    "kZ": 1, "kPhasedXPowGate": 1, "kPhasedXZGate": 1, "kXXPowGate": 2,
+    "kYYPowGate": 2, "kZZPowGate": 2, "kXX": 2, "kYY": 2, "kZZ": 2,
+    "kSwapPowGate": 2, "kISwapPowGate": 2, "kriswap": 2, "kSWAP": 2,
+    "kISWAP": 2, "kPhasedISwapPowGate": 2, "kgivens": 2, "kFSimGate": 2,
+    "kCCZPowGate": 3, "kCCXPowGate": 3, "kCSwapGate": 3, "kCCZ": 3, "kCCX": 3,
+}
+
+
+def build_module_circuit(mod, n, desc):
+    c = mod.Circuit()
+    c.num_qubits = n
+    for d in desc:
+        if d["t"] == "gate":
+            mod.add_gate(getattr(mod, d["kind"]), d["time"], d["qubits"], d["params"], c)
+        elif d["t"] == "diag":
+            mod.add_diagonal_gate(d["time"], d["qubits"], d["angles"], c)
+        elif d["t"] == "matrix":
+            mod.add_matrix_gate(d["time"], d["qubits"], d["matrix"], c)
+        elif d["t"] == "ctrl":
+            mod.control_last_gate(d["qubits"], d["values"], c)
+        elif d["t"] == "meas":
+            mod.add_measurement(d["time"], d["qubits"], c)
+    return c
+
+
+def build_module_opsums(mod, spec):
+    out = []
+    for strings, count in spec:
+        ops = []
+        for weight, terms in strings:
+            s = mod.OpString()
+            s.weight = complex(*weight)
+            for kind, qs in terms:
+                mod.add_gate_to_opstring(getattr(mod, kind), qs, s)
+            ops.append(s)
+        out.append((ops, count))
+    return out
+
+
+def random_module_gate(rng, n, time, kinds=None):
+    kinds = kinds or list(KIND_QUBITS)
+    kind = kinds[int(rng.integers(len(kinds)))]
+    qs = rng.permutation(n)[:KIND_QUBITS[kind]].tolist()
+    ps = {p: float(np.float32(rng.uniform(-1.5, 1.5))) for p in PARAM_KINDS.get(kind, ())}
+    return dict(t="gate", kind=kind, time=time, qubits=qs, params=ps)
+
+
+def random_module_circuit(rng, n, layers, measure_at=()):
+    """Every op at its own time step (the reference's fuser needs the gates
+    of each qubit in time order)."""
+    desc = [dict(t="gate", kind="kH", time=0, qubits=[q], params={}) for q in range(n)]
+    t = 1
+    for layer in range(layers):
+        for _ in range(max(1, n // 2)):
+            desc.append(random_module_gate(rng, n, t))
+            t += 1
+            r = rng.random()
+            if r < 0.1 and KIND_QUBITS[desc[-1]["kind"]] < n - 1:
+                free = [q for q in range(n) if q not in desc[-1]["qubits"]]
+                cq = rng.permutation(free)[:1 + int(rng.integers(2))].tolist()
+                desc.append(dict(t="ctrl", qubits=cq,
+                                 values=rng.integers(0, 2, len(cq)).tolist()))
+            elif r < 0.2:
+                k = 2 + int(rng.integers(2))
+                qs = rng.permutation(n)[:k].tolist()
+                na = int(rng.integers(1, (1 << k) + 1))
+                desc.append(dict(t="diag", time=t, qubits=qs,
+                                 angles=rng.uniform(-3, 3, na).tolist()))
+                t += 1
+            elif r < 0.3:
+                k = 1 + int(rng.integers(3))
+                qs = rng.permutation(n)[:k].tolist()
+                m = interleave(random_unitary(rng, k)).astype(np.float32)
+                desc.append(dict(t="matrix", time=t, qubits=qs, matrix=m.tolist()))
+                t += 1
+        if layer in measure_at:
+            desc.append(dict(t="meas", time=t, qubits=rng.permutation(n)[:3].tolist()))
+            t += 1
+    return desc
+
+
+def random_pauli_opsums(rng, n, count, wmax, big=None):
+    spec = []
+    for _ in range(count):
+        strings = []
+        for _ in range(1 + int(rng.integers(3))):
+            w = 1 + int(rng.integers(wmax))
+            qs = rng.permutation(n)[:w].tolist()
+            terms = [[["kX", "kY", "kZ"][int(rng.integers(3))], [q]] for q in qs]
+            strings.append([[float(rng.uniform(-1, 1)), float(rng.uniform(-1, 1))], terms])
+        cnt = len({q for _, ts in strings for _, qq in ts for q in qq})
+        spec.append([strings, cnt])
+    if big:
+        qs = rng.permutation(n)[:big].tolist()
+        terms = [[["kX", "kY", "kZ"][int(rng.integers(3))], [q]] for q in qs]
+        spec.append([[[[0.5, 0.25], terms]], big])
+    spec.append([[[[0.75, 0.0], []]], 0])          # identity: EV = weight
+    return spec
+
+
+def pybind_cases():
+    import json
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+    import qsim_basic as ref  # the reference's module, built from its sources
+
+    def opts(c, **kw):
+        return dict(dict(c=c, f=2, s=1, t=1, v=0, z=0), **kw)
+
+    rng = np.random.default_rng(9090)
+    out = {}
+    # One circuit per gate kind: a generic 4-qubit state, then the gate.
+    kinds = []
+    for kind in KIND_QUBITS:
+        desc = [dict(t="gate", kind="kH", time=0, qubits=[q], params={}) for q in range(4)]
+        desc += [dict(t="gate", kind="krx", time=1, qubits=[q],
+                      params={"phi": 0.3 + 0.4 * q}) for q in range(4)]
+        desc += [dict(t="gate", kind="kCZ", time=2, qubits=[0, 1], params={}),
+                 dict(t="gate", kind="kCZ", time=2, qubits=[2, 3], params={})]
+        desc.append(random_module_gate(rng, 4, 3, [kind]))
+        fs = np.array(ref.qsim_simulate_fullstate(opts(build_module_circuit(ref, 4, desc)), 0))
+        kinds.append(dict(desc=desc, fs=fs.tolist()))
+    out["gate_kinds"] = json.dumps(kinds)
+    # A 10-qubit circuit of every builder.
+    n = 10
+    desc = random_module_circuit(rng, n, 12)
+    c = build_module_circuit(ref, n, desc)
+    vec = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    vec = (vec / np.linalg.norm(vec)).astype(np.complex64).view(np.float32)
+    bits = rng.choice(1 << n, 16, replace=False)
+    btxt = "\n".join("".join(str((int(b) >> q) & 1) for q in range(n)) for b in bits)
+    ops_spec = random_pauli_opsums(rng, n, 6, 4, big=8)
+    nops = sum(1 for d in desc if d["t"] != "ctrl")   # control_last_gate adds none
+    moments = [[nops // 2, random_pauli_opsums(rng, n, 2, 3)],
+               [nops, random_pauli_opsums(rng, n, 2, 3)]]
+    mix = dict(n=n, desc=desc, bits=[int(b) for b in bits], btxt=btxt,
+               vec=vec.tolist(), opsums=ops_spec, moments=moments)
+    mix["fs0"] = np.array(ref.qsim_simulate_fullstate(opts(c), 0)).tolist()
+    mix["fs_vec"] = np.array(ref.qsim_simulate_fullstate(opts(c), vec)).tolist()
+    mix["fs_basis"] = np.array(ref.qsim_simulate_fullstate(opts(c), 37)).tolist()
+    mix["amps"] = [[a.real, a.imag] for a in ref.qsim_simulate(opts(c, i=btxt))]
+    mix["samples"] = [int(x) for x in ref.qsim_sample_final(opts(c, s=5), 500)]
+    evs = ref.qsim_simulate_expectation_values(opts(c), build_module_opsums(ref, ops_spec), 0)
+    mix["evs"] = [[e.real, e.imag] for e in evs]
+    mevs = ref.qsim_simulate_moment_expectation_values(
+        opts(c), [(end, build_module_opsums(ref, sp)) for end, sp in moments], 0)
+    mix["mevs"] = [[[e.real, e.imag] for e in row] for row in mevs]
+    assert mix["amps"] and mix["samples"] and mix["evs"] and mix["mevs"]
+    out["mixed"] = json.dumps(mix)
+    # Measurements inside the circuit: qsim_sample's bits.
+    n = 6
+    desc = random_module_circuit(rng, n, 6, measure_at=(2, 5))
+    c = build_module_circuit(ref, n, desc)
+    meas = dict(n=n, desc=desc, seeds={})
+    for seed in (1, 2, 3):
+        meas["seeds"][str(seed)] = [int(b) for b in ref.qsim_sample(opts(c, s=seed))]
+        assert meas["seeds"][str(seed)]
+    out["measure"] = json.dumps(meas)
+    out["names"] = json.dumps(sorted(x for x in dir(ref) if not x.startswith("_")))
+    out["kind_values"] = json.dumps({x: int(getattr(ref, x)) for x in dir(ref)
+                                     if x.startswith("k")})
+    np.savez_compressed(os.path.join(HERE, "pybind_module.npz"),
+                        **{k: np.array(v) for k, v in out.items()})
+    print("pybind_module written")
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
@@ -596,6 +782,9 @@ def main():
         return
     if sys.argv[1:] == ["unitary"]:
         unitary_cases()
+        return
+    if sys.argv[1:] == ["pybind"]:
+        pybind_cases()
         return
     if sys.argv[1:] == ["hybrid"]:
         hybrid_known_case()
@@ -627,6 +816,7 @@ def main():
     unitary_cases()
     hybrid_known_case()
     hybrid_random_cases()
+    pybind_cases()
 
 
 if __name__ == "__main__":
