@@ -432,6 +432,11 @@ int qsg_traj_info(const qsg_traj* t, unsigned* num_qubits, uint64_t* num_ops,
  * receives num_ops entries (may be NULL). */
 int qsg_traj_run(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
                  uint64_t* stats);
+/* QuantumTrajectorySimulator::RunOnce (lib/qtrajectory.h) on the state as
+ * given (the caller prepares it), as the reference's Python module runs
+ * noisy circuits from an input state. */
+int qsg_traj_run_from(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
+                      uint64_t* stats);
 /* RunBatch over items (runners[item_runner[i]], item_rep[i]) on concurrent
  * streams of `device` (one host thread, stream, state buffer and workspace
  * each).  stats (may be NULL): the items' entries concatenated in item

@@ -126,6 +126,7 @@ SIGNATURES = {
     "qsg_traj_destroy": (i32, [vp]),
     "qsg_traj_info": (i32, [vp, P_u32, P_u64, P_u64]),
     "qsg_traj_run": (i32, [vp, vp, vp, u64, P_u64]),
+    "qsg_traj_run_from": (i32, [vp, vp, vp, u64, P_u64]),
     "qsg_traj_run_batch": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                  vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                  P_u64]),

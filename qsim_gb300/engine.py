@@ -437,6 +437,13 @@ class Trajectories:
                                  stats.ctypes.data_as(N.P_u64)))
         return stats
 
+    def run_from(self, ctx, state, rep: int) -> np.ndarray:
+        """RunOnce on `state` as given (not reset to |0..0>)."""
+        stats = np.zeros(max(1, self.info()["num_ops"]), dtype=np.uint64)
+        check(N.lib.qsg_traj_run_from(ctx.h, self.h, state.get(), rep,
+                                      stats.ctypes.data_as(N.P_u64)))
+        return stats
+
     @staticmethod
     def samples(stats: np.ndarray) -> np.ndarray:
         """The reference's stat.samples: entries other than NO_STAT."""

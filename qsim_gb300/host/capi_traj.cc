@@ -227,6 +227,17 @@ int qsg_traj_run(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
   return rc ? rc : rc2;
 }
 
+int qsg_traj_run_from(qsg_ctx* ctx, qsg_traj* t, float* state, uint64_t rep,
+                      uint64_t* stats) {
+  if (!ctx || !t || !state) return invalid("null argument");
+  TrajWorkspace ws;
+  int rc = ws.init(ctx, 4096);
+  if (rc) return rc;
+  rc = t->r->enqueue(ws, state, rep, stats, /*from_state=*/true);
+  int rc2 = ws.resolve();
+  return rc ? rc : rc2;
+}
+
 int qsg_traj_run_batch(int device, qsg_traj* const* runners,
                        uint64_t num_runners, const uint32_t* item_runner,
                        const uint64_t* item_rep, uint64_t num_items,

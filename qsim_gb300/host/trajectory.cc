@@ -690,8 +690,11 @@ struct StreamSink {
   unsigned n;
   unsigned tc_min_k;  // recomputed blocks of >= tc_min_k qubits on tcgen05
                       // (0: never)
+  bool keep_state = false;  // start from the state given, not |0..0>
 
-  int set_zero() { return qsg_set_state_zero(ws.ctx, state, n); }
+  int set_zero() {
+    return keep_state ? QSG_OK : qsg_set_state_zero(ws.ctx, state, n);
+  }
   int gate(const std::vector<unsigned>& qs, const Op* ctl, const float* m32,
            ptrdiff_t, const void* tc_operands) {
     if (tc_operands)
@@ -815,11 +818,11 @@ struct ProgramSink {
 }  // namespace
 
 int TrajectoryRunner::enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
-                              uint64_t* stats) const {
+                              uint64_t* stats, bool from_state) const {
   const int rc = upload(ws.ctx);
   if (rc) return rc;
   StreamSink sink{ws, state, nc_.num_qubits,
-                  has_tc_ ? std::max(opt_.tc_min_k, 1u) : 0u};
+                  has_tc_ ? std::max(opt_.tc_min_k, 1u) : 0u, from_state};
   return walk(rep, stats, sink);
 }
 

@@ -137,11 +137,12 @@ class TrajectoryRunner {
   const Plan& base_plan() const { return base_; }
 
   // Enqueues one trajectory (repetition `rep`) on ws.ctx's stream:
-  // |0..0>, the noisy circuit, the final normalisation.  `stats` (num_ops()
-  // entries) is filled for host-side choices now and for device-side ones by
-  // ws.resolve().  Measurements synchronise the stream.
+  // |0..0> (or, with from_state, the state as given), the noisy circuit,
+  // the final normalisation.  `stats` (num_ops() entries) is filled for
+  // host-side choices now and for device-side ones by ws.resolve().
+  // Measurements synchronise the stream.
   int enqueue(TrajWorkspace& ws, float* state, uint64_t rep,
-              uint64_t* stats) const;
+              uint64_t* stats, bool from_state = false) const;
 
   // Device table of the channels sampled on the device (uploaded on first
   // use for the given context's device).

@@ -12,8 +12,10 @@ builders (``add_gate``, ``add_diagonal_gate``, ``add_matrix_gate``,
 ``"f"`` max fused size, ``"s"`` seed, ``"t"``, ``"v"``, ``"z"``):
 ``qsim_simulate``, ``qsim_simulate_fullstate``, ``qsim_sample``,
 ``qsim_sample_final``, ``qsim_simulate_expectation_values`` and
-``qsim_simulate_moment_expectation_values``.  Noisy-circuit (qtrajectory)
-and qsimh entry points of the reference module are not part of this module.
+``qsim_simulate_moment_expectation_values``, and for noisy circuits
+(``add_channel``) the ``qtrajectory_*`` counterparts on the engine's
+trajectory runner.  ``qsimh_simulate`` is not part of this module (the
+hybrid simulator is ``qsim_gb300.hybrid``).
 
 Gate matrices follow Cirq's definitions (eigen-decomposed power gates
 U(t, s) = sum_k exp(i pi t (theta_k + s)) P_k), in the reference's layout:
@@ -343,6 +345,22 @@ def control_last_gate(qubits, values, circuit: Circuit) -> None:
     op.update(kind=1, cqs=[int(q) for q in qubits], cvals=cv)
 
 
+def add_channel(time, qubits, prob_matrix_unitary_triples,
+                circuit: Circuit) -> None:
+    """A noisy-circuit channel (pybind_main.cpp add_channel): Kraus
+    operators given as (lower-bound probability, matrix in Cirq's qubit
+    order, is unitary)."""
+    kops = []
+    cqs = None
+    for prob, mat, unitary in prob_matrix_unitary_triples:
+        g = _matrix_gate(time, qubits, mat)
+        qs, m = _sorted(g["qs"], g["m"])
+        cqs = qs
+        kops.append((bool(unitary), float(prob), m))
+    circuit.ops.append(dict(kind=3, time=int(time), qs=cqs or [], kops=kops,
+                            m=None, cqs=[], cvals=0))
+
+
 def add_gate_to_opstring(gate_kind, qubits, opstring: OpString) -> None:
     opstring.ops.append(_gate(gate_kind, 0, qubits, {}))
 
@@ -387,6 +405,24 @@ def _engine_circuit(num_qubits, ops):
         else:
             c.add_gate(o["time"], o["qs"], o["m"])
     return c
+
+
+def _noisy_circuit(num_qubits, ops):
+    """The engine's noisy circuit: runs of gates appended as circuits, each
+    channel as a general Kraus channel."""
+    from . import engine as E
+    nc = E.NoisyCircuit(num_qubits)
+    run = []
+    for o in list(ops) + [None]:
+        if o is not None and o["kind"] != 3:
+            run.append(o)
+            continue
+        if run:
+            nc.append(_engine_circuit(num_qubits, run))
+            run = []
+        if o is not None:
+            nc.add_kraus_channel(o["time"], o["qs"], o["kops"])
+    return nc
 
 
 def _max_fused(options):
@@ -459,6 +495,22 @@ class _Run:
             bits = plan.run(self.ctx, self.state, seed=self.seed)
         self.seed += 1
         return bits
+
+    def run_noisy(self, ops, from_state=True, collect_mea_stat=False):
+        """QuantumTrajectorySimulator::RunOnce with repetition = seed on the
+        current state (from_state) or from |0..0>; returns its stats."""
+        from . import engine as E
+        stats = np.zeros(0, dtype=np.uint64)
+        if ops:
+            traj = E.Trajectories(_noisy_circuit(self.n, ops),
+                                  max_fused_size=self.f, collect_kop_stat=False,
+                                  collect_mea_stat=collect_mea_stat)
+            if from_state:
+                stats = traj.run_from(self.ctx, self.state, self.seed)
+            else:
+                stats = traj.run(self.ctx, self.state, self.seed)
+        self.seed += 1
+        return stats
 
     def expectation_values(self, opsums_and_qubit_counts):
         out = []
@@ -554,3 +606,77 @@ def qsim_simulate_moment_expectation_values(options, opsums_and_qubit_counts,
         out.append(r.expectation_values(counts))
         begin = int(end)
     return out
+
+
+# -------------------------------------------------- noisy circuits -------
+
+
+def qtrajectory_simulate(options) -> List[complex]:
+    """Amplitudes of the bitstrings options["i"] after one trajectory
+    (repetition s) of the noisy circuit from |0...0>."""
+    r = _Run(options)
+    bits = _bitstrings(options["i"], r.n)
+    r.run_noisy(r.circuit.ops, from_state=False)
+    amps = r.ss.to_numpy(r.state)
+    return [complex(amps[b]) for b in bits]
+
+
+def qtrajectory_simulate_fullstate(options, input_state=0) -> np.ndarray:
+    """Final state of one trajectory (repetition s) from the input state."""
+    r = _Run(options)
+    r.init(input_state)
+    r.run_noisy(r.circuit.ops)
+    amps = np.ascontiguousarray(r.ss.to_numpy(r.state), dtype=np.complex64)
+    return amps.view(np.float32).copy()
+
+
+def qtrajectory_sample_final(options, num_samples: int) -> List[int]:
+    """Samples of the final state of one trajectory (seed s + 1)."""
+    r = _Run(options)
+    r.init(0)
+    r.run_noisy(r.circuit.ops)
+    return [int(x) for x in r.ss.Sample(r.state, int(num_samples), r.seed)]
+
+
+def qtrajectory_sample(options) -> List[int]:
+    """Measurement results of one trajectory (repetition s), one bit per
+    measured qubit in the gates' qubit order, concatenated."""
+    from . import engine as E
+    r = _Run(options)
+    stats = r.run_noisy(r.circuit.ops, from_state=False, collect_mea_stat=True)
+    vals = E.Trajectories.samples(stats)
+    out = []
+    meas = [o for o in r.circuit.ops if o["kind"] == 2]
+    for o, v in zip(meas, vals):
+        out.extend(int((int(v) >> q) & 1) for q in o["qs"])
+    return out
+
+
+def qtrajectory_simulate_expectation_values(options, opsums_and_qubit_counts,
+                                            input_state=0) -> List[complex]:
+    """Expectation values averaged over options["r"] trajectories
+    (repetitions s, s + 1, ...), each from the input state."""
+    r = _Run(options)
+    reps = int(options["r"])
+    acc = np.zeros(len(opsums_and_qubit_counts), dtype=np.complex128)
+    for _ in range(reps):
+        r.init(input_state)
+        r.run_noisy(r.circuit.ops)
+        acc += np.array(r.expectation_values(opsums_and_qubit_counts))
+    return [complex(x) for x in acc / reps]
+
+
+def qtrajectory_simulate_moment_expectation_values(
+        options, opsums_and_qubit_counts, input_state=0):
+    """Moment expectation values averaged over options["r"] trajectories."""
+    r = _Run(options)
+    reps = int(options["r"])
+    acc = [np.zeros(len(c), dtype=np.complex128) for _, c in opsums_and_qubit_counts]
+    for _ in range(reps):
+        r.init(input_state)
+        begin = 0
+        for i, (end, counts) in enumerate(opsums_and_qubit_counts):
+            r.run_noisy(r.circuit.ops[begin:int(end)])
+            acc[i] += np.array(r.expectation_values(counts))
+            begin = int(end)
+    return [[complex(x) for x in a / reps] for a in acc]

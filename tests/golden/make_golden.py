@@ -631,6 +631,9 @@ def build_module_circuit(mod, n, desc):
             mod.control_last_gate(d["qubits"], d["values"], c)
         elif d["t"] == "meas":
             mod.add_measurement(d["time"], d["qubits"], c)
+        elif d["t"] == "chan":
+            mod.add_channel(d["time"], d["qubits"],
+                            [(p, m, u) for p, m, u in d["kops"]], c)
     return c
 
 
@@ -709,6 +712,96 @@ def random_pauli_opsums(rng, n, count, wmax, big=None):
     return spec
 
 
+def _flat(m):
+    return interleave(np.asarray(m, np.complex128)).astype(np.float32).tolist()
+
+
+def random_noisy_module_circuit(rng, n, layers, measure=False):
+    """Every op at its own time step; after each gate a channel on one of
+    its qubits: a Pauli mixture (unitary), amplitude damping (non-unitary,
+    lower bounds 1 - gamma and 0) or, for two-qubit gates, a mixture of the
+    identity and CZ."""
+    px = np.array([[0, 1], [1, 0]])
+    py = np.array([[0, -1j], [1j, 0]])
+    pz = np.diag([1, -1])
+    desc = [dict(t="gate", kind="kH", time=0, qubits=[q], params={}) for q in range(n)]
+    t = 1
+    for layer in range(layers):
+        for _ in range(max(1, n // 2)):
+            g = random_module_gate(rng, n, t, [k for k in KIND_QUBITS
+                                               if KIND_QUBITS[k] <= 2])
+            desc.append(g)
+            t += 1
+            q = g["qubits"][0]
+            r = rng.random()
+            if r < 0.4:
+                p = float(np.float32(0.02 + 0.1 * rng.random()))
+                kops = [[1 - 3 * p, _flat(np.eye(2)), True]]
+                kops += [[p, _flat(m), True] for m in (px, py, pz)]
+            elif r < 0.8:
+                gam = float(np.float32(0.05 + 0.2 * rng.random()))
+                kops = [[1 - gam, _flat(np.diag([1, np.sqrt(1 - gam)])), False],
+                        [0.0, _flat(np.array([[0, np.sqrt(gam)], [0, 0]])), False]]
+            else:
+                if len(g["qubits"]) < 2:
+                    continue
+                cz = np.diag([1, 1, 1, -1])
+                p = float(np.float32(0.1 + 0.2 * rng.random()))
+                desc.append(dict(t="chan", time=t, qubits=g["qubits"],
+                                 kops=[[1 - p, _flat(np.eye(4)), True],
+                                       [p, _flat(cz), True]]))
+                t += 1
+                continue
+            desc.append(dict(t="chan", time=t, qubits=[q], kops=kops))
+            t += 1
+        if measure and layer in (1, layers - 1):
+            desc.append(dict(t="meas", time=t, qubits=rng.permutation(n)[:3].tolist()))
+            t += 1
+    return desc
+
+
+def noisy_module_case(ref, rng, opts):
+    n = 6
+    desc = random_noisy_module_circuit(rng, n, 5)
+    c = build_module_circuit(ref, n, desc)
+    vec = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    vec = (vec / np.linalg.norm(vec)).astype(np.complex64).view(np.float32)
+    out = dict(n=n, desc=desc, vec=vec.tolist(), fs={}, fs_vec={}, amps={},
+               samples={})
+    bits = rng.choice(1 << n, 8, replace=False)
+    btxt = "\n".join("".join(str((int(b) >> q) & 1) for q in range(n)) for b in bits)
+    out["btxt"] = btxt
+    for seed in (1, 2, 3, 4, 5, 6):
+        out["fs"][str(seed)] = np.array(
+            ref.qtrajectory_simulate_fullstate(opts(c, s=seed, r=1), 0)).tolist()
+        out["fs_vec"][str(seed)] = np.array(
+            ref.qtrajectory_simulate_fullstate(opts(c, s=seed, r=1), vec)).tolist()
+        out["amps"][str(seed)] = [[a.real, a.imag] for a in
+                                  ref.qtrajectory_simulate(opts(c, s=seed, i=btxt))]
+        out["samples"][str(seed)] = [int(x) for x in
+                                     ref.qtrajectory_sample_final(opts(c, s=seed, r=1), 200)]
+    spec = random_pauli_opsums(rng, n, 4, 3)
+    out["opsums"] = spec
+    evs = ref.qtrajectory_simulate_expectation_values(
+        opts(c, r=8), build_module_opsums(ref, spec), 0)
+    out["evs"] = [[e.real, e.imag] for e in evs]
+    nops = sum(1 for d in desc if d["t"] != "ctrl")
+    moments = [[nops // 2, random_pauli_opsums(rng, n, 2, 2)],
+               [nops, random_pauli_opsums(rng, n, 2, 2)]]
+    out["moments"] = moments
+    mevs = ref.qtrajectory_simulate_moment_expectation_values(
+        opts(c, r=4), [(end, build_module_opsums(ref, sp)) for end, sp in moments], 0)
+    out["mevs"] = [[[e.real, e.imag] for e in row] for row in mevs]
+    mdesc = random_noisy_module_circuit(rng, n, 4, measure=True)
+    mc = build_module_circuit(ref, n, mdesc)
+    out["mdesc"] = mdesc
+    out["mbits"] = {str(seed): [int(b) for b in ref.qtrajectory_sample(opts(mc, s=seed))]
+                    for seed in (1, 2, 3, 4)}
+    assert all(out["mbits"].values()) and out["evs"] and out["mevs"]
+    assert all(out["samples"].values()) and all(out["fs"].values())
+    return out
+
+
 def pybind_cases():
     import json
     sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
@@ -766,6 +859,9 @@ def pybind_cases():
         meas["seeds"][str(seed)] = [int(b) for b in ref.qsim_sample(opts(c, s=seed))]
         assert meas["seeds"][str(seed)]
     out["measure"] = json.dumps(meas)
+    # Noisy circuits: gates, Pauli-mixture and amplitude-damping channels on
+    # one qubit, a two-qubit unitary mixture, measurements.
+    out["noisy"] = json.dumps(noisy_module_case(ref, rng, opts))
     out["names"] = json.dumps(sorted(x for x in dir(ref) if not x.startswith("_")))
     out["kind_values"] = json.dumps({x: int(getattr(ref, x)) for x in dir(ref)
                                      if x.startswith("k")})

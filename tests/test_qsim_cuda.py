@@ -9,7 +9,10 @@ outputs for them: one 4-qubit circuit per Cirq gate kind (final state), a
 diagonal and matrix gates) with its final states from |0>, a basis state and
 a state vector, amplitudes of bitstrings, 500 samples, expectation values of
 Pauli sums (one on 8 qubits, one the identity) and moment expectation
-values, and a circuit with measurements (qsim_sample bits for 3 seeds).
+values, a circuit with measurements (qsim_sample bits for 3 seeds), and a
+noisy circuit (Pauli-mixture, amplitude-damping and two-qubit channels)
+with one trajectory's state, amplitudes and samples per seed, expectation
+values over 8 and 4 repetitions, and measurement bits per seed.
 
 CPU: the module exports every name of the reference module's simulator and
 builder interface with the same enum values; the gate matrices, applied by
@@ -24,13 +27,9 @@ import pytest
 
 from conftest import load_golden, rel_l2
 
-# Entry points of the reference module not built here (noisy circuits and
-# qsimh through the options dict).
-NOT_BUILT = {"add_channel", "qsimh_simulate", "qtrajectory_sample",
-             "qtrajectory_sample_final", "qtrajectory_simulate",
-             "qtrajectory_simulate_expectation_values",
-             "qtrajectory_simulate_fullstate",
-             "qtrajectory_simulate_moment_expectation_values"}
+# The reference module's qsimh entry point is not built here (the hybrid
+# simulator is qsim_gb300.hybrid).
+NOT_BUILT = {"qsimh_simulate"}
 
 
 @pytest.fixture(scope="module")
@@ -59,6 +58,8 @@ def build(Q, n, desc):
             Q.control_last_gate(d["qubits"], d["values"], c)
         elif d["t"] == "meas":
             Q.add_measurement(d["time"], d["qubits"], c)
+        elif d["t"] == "chan":
+            Q.add_channel(d["time"], d["qubits"], [tuple(k) for k in d["kops"]], c)
     return c
 
 
@@ -171,3 +172,36 @@ def test_gpu_measurement_bits(fx, Q):
     c = build(Q, m["n"], m["desc"])
     for seed, want in m["seeds"].items():
         assert Q.qsim_sample(options(c, s=int(seed))) == want
+
+
+@pytest.mark.gpu
+def test_gpu_noisy_circuit_entry_points(fx, Q):
+    """The reference's trajectories for the same seeds: the same Kraus
+    choices, so the same states (FP32 bar), amplitudes, samples, averaged
+    expectation values and measurement bits."""
+    m = fx["noisy"]
+    n = m["n"]
+    c = build(Q, n, m["desc"])
+    vec = np.asarray(m["vec"], np.float32)
+    for seed in m["fs"]:
+        o = options(c, s=int(seed), r=1)
+        assert rel_l2(cplx(Q.qtrajectory_simulate_fullstate(o, 0)),
+                      cplx(m["fs"][seed])) < 1e-5, seed
+        assert rel_l2(cplx(Q.qtrajectory_simulate_fullstate(o, vec)),
+                      cplx(m["fs_vec"][seed])) < 1e-5, seed
+        amps = np.array(Q.qtrajectory_simulate(options(c, s=int(seed), i=m["btxt"])))
+        want = np.array([complex(*a) for a in m["amps"][seed]])
+        assert np.abs(amps - want).max() < 2e-6
+        smp = np.array(Q.qtrajectory_sample_final(o, 200))
+        assert np.mean(smp == np.array(m["samples"][seed])) >= 0.99
+    evs = np.array(Q.qtrajectory_simulate_expectation_values(
+        options(c, r=8), opsums(Q, m["opsums"]), 0))
+    want = np.array([complex(*e) for e in m["evs"]])
+    assert np.abs(evs - want).max() < 2e-6
+    mevs = Q.qtrajectory_simulate_moment_expectation_values(
+        options(c, r=4), [(end, opsums(Q, sp)) for end, sp in m["moments"]], 0)
+    for row, wrow in zip(mevs, m["mevs"]):
+        assert np.abs(np.array(row) - np.array([complex(*e) for e in wrow])).max() < 2e-6
+    mc = build(Q, n, m["mdesc"])
+    for seed, want in m["mbits"].items():
+        assert Q.qtrajectory_sample(options(mc, s=int(seed), r=1)) == want
