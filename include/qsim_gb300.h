@@ -568,6 +568,12 @@ int qsg_hybrid_run(qsg_ctx* ctx, const qsg_circuit* c, const unsigned* parts,
  * matrix; *num_terms = 0 for other ops.  terms may be NULL. */
 int qsg_circuit_get_schmidt(const qsg_circuit* c, uint64_t i,
                             unsigned* num_terms, double* terms);
+/* Sets the operator Schmidt terms of two-qubit op i (same layout; the
+ * terms must sum to the op's matrix), for gates other than the named ones,
+ * e.g. the Cirq gate set of lib/gates_cirq.h, whose decompositions the
+ * reference defines per gate.  At most 4 terms. */
+int qsg_circuit_set_schmidt(qsg_circuit* c, uint64_t i, unsigned num_terms,
+                            const double* terms);
 
 /* ---- timing ------------------------------------------------------------ */
 /* CUDA-event timing on the context stream: qsg_timer_start records an event,

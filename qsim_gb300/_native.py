@@ -144,6 +144,7 @@ SIGNATURES = {
     "qsg_hybrid_split": (i32, [vp, P_u32, u32, vp]),
     "qsg_hybrid_run": (i32, [vp, vp, P_u32, u32, vp, P_u64, u64, P_f64, vp]),
     "qsg_circuit_get_schmidt": (i32, [vp, u64, P_u32, P_f64]),
+    "qsg_circuit_set_schmidt": (i32, [vp, u64, u32, P_f64]),
     "qsg_traj_run_packed": (i32, [i32, C.POINTER(vp), u64, P_u32, P_u64, u64,
                                   vp, P_u64, C.POINTER(vp), P_f32, P_f64,
                                   P_u64, vp]),

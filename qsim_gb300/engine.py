@@ -138,6 +138,17 @@ class Circuit:
     def ops(self):
         return [self.op(i) for i in range(len(self))]
 
+    def set_schmidt(self, i: int, terms):
+        """Schmidt terms of two-qubit op i: a list of (A, B) 2x2 factors, A
+        on the op's first (lower) qubit, summing to the op's matrix."""
+        buf = np.zeros(16 * max(1, len(terms)), dtype=np.float64)
+        c = buf.view(np.complex128)
+        for j, (a, b) in enumerate(terms):
+            c[8 * j:8 * j + 4] = np.asarray(a, np.complex128).ravel()
+            c[8 * j + 4:8 * j + 8] = np.asarray(b, np.complex128).ravel()
+        check(N.lib.qsg_circuit_set_schmidt(self.h, i, len(terms),
+                                            buf.ctypes.data_as(N.P_f64)))
+
     def schmidt(self, i: int):
         """Operator Schmidt terms of op i (two-qubit named gates): a list of
         (A, B), A the 2x2 factor on the op's first qubit; [] otherwise."""
@@ -278,6 +289,17 @@ class Plan:
 
     def ops(self):
         return [self.op(i) for i in range(len(self))]
+
+    def set_schmidt(self, i: int, terms):
+        """Schmidt terms of two-qubit op i: a list of (A, B) 2x2 factors, A
+        on the op's first (lower) qubit, summing to the op's matrix."""
+        buf = np.zeros(16 * max(1, len(terms)), dtype=np.float64)
+        c = buf.view(np.complex128)
+        for j, (a, b) in enumerate(terms):
+            c[8 * j:8 * j + 4] = np.asarray(a, np.complex128).ravel()
+            c[8 * j + 4:8 * j + 8] = np.asarray(b, np.complex128).ravel()
+        check(N.lib.qsg_circuit_set_schmidt(self.h, i, len(terms),
+                                            buf.ctypes.data_as(N.P_f64)))
 
     def schmidt(self, i: int):
         """Operator Schmidt terms of op i (two-qubit named gates): a list of

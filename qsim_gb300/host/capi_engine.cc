@@ -235,6 +235,37 @@ int qsg_circuit_get_schmidt(const qsg_circuit* c, uint64_t i,
   return QSG_OK;
 }
 
+int qsg_circuit_set_schmidt(qsg_circuit* c, uint64_t i, unsigned num_terms,
+                            const double* terms) {
+  if (!c || i >= c->c.ops.size() || (num_terms && !terms))
+    return invalid("op index out of range");
+  Op& op = c->c.ops[i];
+  if (op.kind != OpKind::kGate || op.qs.size() != 2 || num_terms > 4)
+    return invalid("Schmidt terms need a two-qubit gate and at most 4 terms");
+  // The terms must rebuild the gate: sum_t A_t (x) B_t, bit 0 <-> qs[0].
+  double err = 0, scale = 0;
+  for (unsigned r = 0; r < 4; ++r) {
+    for (unsigned col = 0; col < 4; ++col) {
+      cplx v = 0;
+      for (unsigned t = 0; t < num_terms; ++t) {
+        const double* a = terms + 16 * t;
+        const double* b = a + 8;
+        const unsigned ia = 2 * ((r & 1) * 2 + (col & 1));
+        const unsigned ib = 2 * ((r >> 1) * 2 + (col >> 1));
+        v += cplx(a[ia], a[ia + 1]) * cplx(b[ib], b[ib + 1]);
+      }
+      err = std::max(err, std::abs(v - op.m[r * 4 + col]));
+      scale = std::max(scale, std::abs(op.m[r * 4 + col]));
+    }
+  }
+  if (err > 1e-6 * std::max(1.0, scale))
+    return invalid("Schmidt terms do not rebuild the gate");
+  op.schmidt.assign(size_t(8) * num_terms, 0.0);
+  for (size_t j = 0; j < op.schmidt.size(); ++j)
+    op.schmidt[j] = cplx(terms[2 * j], terms[2 * j + 1]);
+  return QSG_OK;
+}
+
 int qsg_pauli_sum(unsigned n, unsigned count, unsigned max_weight,
                   uint64_t seed, unsigned* weights, unsigned* qubits,
                   char* letters, double* coeffs) {

@@ -14,8 +14,9 @@ builders (``add_gate``, ``add_diagonal_gate``, ``add_matrix_gate``,
 ``qsim_sample_final``, ``qsim_simulate_expectation_values`` and
 ``qsim_simulate_moment_expectation_values``, and for noisy circuits
 (``add_channel``) the ``qtrajectory_*`` counterparts on the engine's
-trajectory runner.  ``qsimh_simulate`` is not part of this module (the
-hybrid simulator is ``qsim_gb300.hybrid``).
+trajectory runner, and ``qsimh_simulate`` on the hybrid simulator
+(``qsim_gb300.hybrid``) with the reference's Schmidt terms of the Cirq
+two-qubit gates.
 
 Gate matrices follow Cirq's definitions (eigen-decomposed power gates
 U(t, s) = sum_k exp(i pi t (theta_k + s)) P_k), in the reference's layout:
@@ -294,7 +295,7 @@ def _gate(kind, time, qubits, params):
         raise ValueError(f"{k.name} acts on {want} qubits")
     ps = {str(a): float(v) for a, v in params.items()}
     return dict(kind=0, time=int(time), qs=qs, m=gate_matrix(k, len(qs), ps),
-                cqs=[], cvals=0)
+                cqs=[], cvals=0, gate=k, params=ps)
 
 
 def _matrix_gate(time, qubits, matrix):
@@ -680,3 +681,96 @@ def qtrajectory_simulate_moment_expectation_values(
             acc[i] += np.array(r.expectation_values(counts))
             begin = int(end)
     return [[complex(x) for x in a / reps] for a in acc]
+
+
+# ------------------------------------------------------------------ qsimh --
+
+_H = 0.5
+_IS2 = math.sqrt(0.5)
+_C = 0.5 + 0.5j
+# First Schmidt factor (on the gate's first listed qubit) of the Cirq
+# two-qubit gates, as lib/gates_cirq.h's SchmidtDecomp functions choose
+# them: a path of the hybrid simulator picks one term per gate on the cut,
+# so partial sums over fixed prefix bits equal the reference's only with the
+# same terms.  The second factors follow from the gate matrix (projection
+# onto these mutually orthogonal first factors).
+_FIRST = {
+    GateKind.kI2: [_I],
+    GateKind.kCZPowGate: [_P0, _P1], GateKind.kCZ: [_P0, _P1],
+    GateKind.kCXPowGate: [_P0, _P1], GateKind.kCX: [_P0, _P1],
+    GateKind.kXXPowGate: [_I, _X], GateKind.kYYPowGate: [_I, _Y],
+    GateKind.kZZPowGate: [_I, _Z],
+    GateKind.kXX: [_X], GateKind.kYY: [_Y], GateKind.kZZ: [_Z],
+    GateKind.kSwapPowGate: [_H * _I, _H * _X, _H * _Y, _H * _Z],
+    GateKind.kISwapPowGate: [_H * _I, _H * _X, _H * _Y, _H * _Z],
+    GateKind.kriswap: [_H * _I, _H * _X, _H * _Y, _H * _Z],
+    GateKind.kPhasedISwapPowGate: [_H * _I, _H * _X, _H * _Y, _H * _Z],
+    GateKind.kgivens: [_H * _I, _H * _X, _H * _Y, _H * _Z],
+    GateKind.kSWAP: [_IS2 * _I, _IS2 * _X, _IS2 * _Y, _IS2 * _Z],
+    GateKind.kISWAP: [_IS2 * _I, _C * _X, _C * _Y, _IS2 * _Z],
+}
+
+
+def _schmidt_terms(kind, m):
+    """[(A_k, B_k)] with A_k on the first listed qubit (bit 0 of m)."""
+    terms = []
+    u = m.reshape(2, 2, 2, 2)          # [b, a, b', a'] for index a + 2 b
+    for a in _FIRST[kind]:
+        b = np.einsum("xy,bxcy->bc", a.conj(), u) / np.sum(np.abs(a) ** 2)
+        terms.append((a, b))
+    return terms
+
+
+def _hybrid_circuit(c: Circuit):
+    """The engine circuit of a qsimh run: gates only; two-qubit Cirq gates
+    carry the reference's Schmidt terms (fSim as the engine's named fs
+    gate, whose terms are the same)."""
+    from . import engine as E
+    ec = E.Circuit(c.num_qubits)
+    i = 0
+    for o in c.ops:
+        if o["kind"] != 0:
+            raise ValueError("measurement, controlled or other non-matrix "
+                             "gates are not supported by qsimh.")
+        k = o.get("gate")
+        if len(o["qs"]) == 2 and k == GateKind.kFSimGate:
+            ec.add_named(o["time"], "fs", o["qs"],
+                         (o["params"]["theta"], o["params"]["phi"]))
+        else:
+            ec.add_gate(o["time"], o["qs"], o["m"])
+            if len(o["qs"]) == 2 and k in _FIRST:
+                terms = _schmidt_terms(k, o["m"])
+                if o["qs"][0] > o["qs"][1]:      # engine: A on the lower qubit
+                    terms = [(b, a) for a, b in terms]
+                ec.set_schmidt(i, terms)
+        i += 1
+    return ec
+
+
+def qsimh_simulate(options) -> List[complex]:
+    """Amplitudes of the bitstrings options["i"] by the hybrid simulator
+    (pybind_main.cpp qsimh_simulate): options["k"] lists the qubits of part
+    1, "w" the prefix, "p" and "r" the numbers of prefix and root gates on
+    the cut.  Errors are printed and give an empty list, as the reference's
+    module does."""
+    import sys
+    from . import hybrid
+    from ._native import QsgError
+    c: Circuit = options["c"]
+    n = c.num_qubits
+    try:
+        bits = _bitstrings(options["i"], n)
+        parts = [0] * n
+        for q in options["k"]:
+            if int(q) >= n:
+                raise ValueError("Invalid arguments are provided for arg k.")
+            parts[int(q)] = 1
+        amps, _ = hybrid.run(_ctx(), _hybrid_circuit(c), parts, bits,
+                             prefix=int(options["w"]),
+                             num_prefix_gatexs=int(options["p"]),
+                             num_root_gatexs=int(options["r"]),
+                             max_fused_size=_max_fused(options))
+    except (QsgError, ValueError) as e:
+        print(e, file=sys.stderr)
+        return []
+    return [complex(np.complex64(a)) for a in amps]

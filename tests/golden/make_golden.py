@@ -802,6 +802,46 @@ def noisy_module_case(ref, rng, opts):
     return out
 
 
+# Cirq two-qubit gates with a Schmidt decomposition in the reference
+# (lib/gates_cirq.h GetSchmidtDecomp), the ones qsimh accepts on the cut.
+SCHMIDT_KINDS = ["kI2", "kCZPowGate", "kCXPowGate", "kCZ", "kCX", "kXXPowGate",
+                 "kYYPowGate", "kZZPowGate", "kXX", "kYY", "kZZ", "kSwapPowGate",
+                 "kISwapPowGate", "kriswap", "kSWAP", "kISWAP",
+                 "kPhasedISwapPowGate", "kgivens", "kFSimGate"]
+
+
+def hybrid_module_case(ref, rng, opts):
+    n = 8
+    parts = [0, 0, 0, 0, 1, 1, 1, 1]
+    ones = [k for k, v in KIND_QUBITS.items() if v == 1]
+    desc = [dict(t="gate", kind="kH", time=0, qubits=[q], params={}) for q in range(n)]
+    t, cut = 1, 0
+    for _ in range(10):
+        for _ in range(4):
+            if rng.random() < 0.4:
+                g = random_module_gate(rng, n, t, ones)
+            else:
+                g = random_module_gate(rng, n, t, SCHMIDT_KINDS)
+                a, b = g["qubits"]
+                if parts[a] != parts[b]:
+                    if cut >= 6:
+                        continue
+                    cut += 1
+                if g["kind"] == "kFSimGate":
+                    g["params"]["theta"] = float(np.float32(rng.uniform(0, 3)))
+            desc.append(g)
+            t += 1
+    c = build_module_circuit(ref, n, desc)
+    bits = rng.choice(1 << n, 32, replace=False)
+    btxt = "\n".join("".join(str((int(b) >> q) & 1) for q in range(n)) for b in bits)
+    runs = []
+    for p, r, w in ((0, 0, 0), (0, 2, 0), (2, 1, 1), (3, 0, 2), (1, 1, 3)):
+        amps = ref.qsimh_simulate(opts(c, i=btxt, k=[4, 5, 6, 7], w=w, p=p, r=r))
+        assert amps, (p, r, w)
+        runs.append(dict(p=p, r=r, w=w, amps=[[a.real, a.imag] for a in amps]))
+    return dict(n=n, desc=desc, btxt=btxt, k=[4, 5, 6, 7], cut=cut, runs=runs)
+
+
 def pybind_cases():
     import json
     sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
@@ -862,6 +902,7 @@ def pybind_cases():
     # Noisy circuits: gates, Pauli-mixture and amplitude-damping channels on
     # one qubit, a two-qubit unitary mixture, measurements.
     out["noisy"] = json.dumps(noisy_module_case(ref, rng, opts))
+    out["hybrid"] = json.dumps(hybrid_module_case(ref, rng, opts))
     out["names"] = json.dumps(sorted(x for x in dir(ref) if not x.startswith("_")))
     out["kind_values"] = json.dumps({x: int(getattr(ref, x)) for x in dir(ref)
                                      if x.startswith("k")})

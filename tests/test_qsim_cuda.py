@@ -12,7 +12,9 @@ Pauli sums (one on 8 qubits, one the identity) and moment expectation
 values, a circuit with measurements (qsim_sample bits for 3 seeds), and a
 noisy circuit (Pauli-mixture, amplitude-damping and two-qubit channels)
 with one trajectory's state, amplitudes and samples per seed, expectation
-values over 8 and 4 repetitions, and measurement bits per seed.
+values over 8 and 4 repetitions, and measurement bits per seed, and an
+8-qubit circuit of Cirq gates cut into halves (6 gates on the cut) with
+qsimh_simulate's amplitudes for five prefix/root splits.
 
 CPU: the module exports every name of the reference module's simulator and
 builder interface with the same enum values; the gate matrices, applied by
@@ -27,9 +29,8 @@ import pytest
 
 from conftest import load_golden, rel_l2
 
-# The reference module's qsimh entry point is not built here (the hybrid
-# simulator is qsim_gb300.hybrid).
-NOT_BUILT = {"qsimh_simulate"}
+# Every entry point of the reference module is built.
+NOT_BUILT = set()
 
 
 @pytest.fixture(scope="module")
@@ -124,6 +125,28 @@ def test_mixed_circuit_on_the_oracle(fx, Q, oracle):
     assert rel_l2(oracle_state(Q, oracle, c), cplx(m["fs0"])) < 1e-6
 
 
+def test_qsimh_terms_on_the_oracle(fx, Q):
+    """The Schmidt terms given to the engine for the Cirq gates on the cut,
+    summed over paths by the FP64 hybrid oracle: the reference module's
+    qsimh amplitudes, also for partial sums over fixed prefixes."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "oracle"))
+    import hybrid_oracle as HO
+    h = fx["hybrid"]
+    n = h["n"]
+    ec = Q._hybrid_circuit(build(Q, n, h["desc"]))
+    ops = ec.ops()
+    for i, o in enumerate(ops):
+        o["schmidt"] = ec.schmidt(i) if len(o["qs"]) == 2 else []
+    parts = [1 if q in h["k"] else 0 for q in range(n)]
+    bits = Q._bitstrings(h["btxt"], n)
+    for r in h["runs"]:
+        got = HO.hybrid_amplitudes(n, ops, parts, bits, r["w"], r["p"], r["r"])
+        want = np.array([complex(*a) for a in r["amps"]])
+        assert np.abs(got - want).max() < 2e-6, (r["p"], r["r"], r["w"])
+
+
 def test_bitstring_parsing(Q):
     assert Q._bitstrings("011\n100\n", 3) == [0b110, 0b001]
     with pytest.raises(ValueError):
@@ -205,3 +228,14 @@ def test_gpu_noisy_circuit_entry_points(fx, Q):
     mc = build(Q, n, m["mdesc"])
     for seed, want in m["mbits"].items():
         assert Q.qtrajectory_sample(options(mc, s=int(seed), r=1)) == want
+
+
+@pytest.mark.gpu
+def test_gpu_qsimh(fx, Q):
+    h = fx["hybrid"]
+    c = build(Q, h["n"], h["desc"])
+    for r in h["runs"]:
+        got = np.array(Q.qsimh_simulate(options(c, i=h["btxt"], k=h["k"], w=r["w"],
+                                                p=r["p"], r=r["r"])))
+        want = np.array([complex(*a) for a in r["amps"]])
+        assert np.abs(got - want).max() < 2e-6, (r["p"], r["r"], r["w"])
