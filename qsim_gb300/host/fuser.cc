@@ -16,6 +16,7 @@
 // (cost of the block) per block, i.e. the most time saved.
 
 #include <algorithm>
+#include <thread>
 #include <cstring>
 
 #include "engine.h"
@@ -399,19 +400,29 @@ constexpr unsigned kStartWindows[] = {2, 3, 4, 6, 8};
 Plan fuse(const Circuit& c, const FuseOptions& opt) {
   const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
   if (!opt.cost) {
-    Plan best = fuse_greedy(c, opt, f, false);
+    if (!opt.tensor_path) return fuse_greedy(c, opt, f, false);
     // Tensor-core plans cost about the same per block, so their run time is
-    // their block count: keep the greedy result with the fewest blocks.
-    if (opt.tensor_path) {
-      for (unsigned w : kStartWindows) {
-        if (w == opt.seeds) continue;
+    // their block count: keep the greedy result with the fewest blocks (the
+    // first of equal ones, in window order).  The runs are independent and
+    // run on host threads of their own.
+    std::vector<unsigned> windows{opt.seeds};
+    for (unsigned w : kStartWindows)
+      if (w != opt.seeds) windows.push_back(w);
+    std::vector<Plan> plans(windows.size());
+    std::vector<std::thread> pool;
+    for (size_t i = 1; i < windows.size(); ++i) {
+      pool.emplace_back([&, i] {
         FuseOptions o = opt;
-        o.seeds = w;
-        Plan p = fuse_greedy(c, o, f, false);
-        if (p.ops.size() < best.ops.size()) best = std::move(p);
-      }
+        o.seeds = windows[i];
+        plans[i] = fuse_greedy(c, o, f, false);
+      });
     }
-    return best;
+    plans[0] = fuse_greedy(c, opt, f, false);
+    for (auto& t : pool) t.join();
+    size_t best = 0;
+    for (size_t i = 1; i < plans.size(); ++i)
+      if (plans[i].ops.size() < plans[best].ops.size()) best = i;
+    return std::move(plans[best]);
   }
   // Learned planner: candidate plans for every block-size limit up to f,
   // grown by gate count and by predicted time per gate (for limits >= 5

@@ -34,6 +34,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -256,11 +257,18 @@ struct DevBuf {
   }
 };
 
-int run_plan(qsg_ctx* ctx, const Circuit& c, const FuseOptions& fo,
-             float* state) {
+int run_plan(qsg_ctx* ctx, Plan plan, float* state) {
   PlanRuntime rt;
-  rt.plan = fuse(c, fo);
+  rt.plan = std::move(plan);
   return rt.run(ctx, state, 0, nullptr);
+}
+
+// Fuses the two parts' circuits, part 1 on a host thread of its own.
+void fuse_parts(const Circuit& c0, const Circuit& c1, const FuseOptions& fo,
+                Plan* out) {
+  std::thread t([&] { out[1] = fuse(c1, fo); });
+  out[0] = fuse(c0, fo);
+  t.join();
 }
 
 }  // namespace
@@ -412,10 +420,14 @@ int qsg_hybrid_run(qsg_ctx* ctx, const qsg_circuit* c, const unsigned* parts,
     c2[p] = first_cut_at_least(sp, p, PR);
   }
   // Prefix: once per part.
-  for (int p = 0; p < 2 && !rc; ++p) {
-    rc = qsg_set_state_zero(ctx, st_p[p].p, sp.n[p]);
-    if (!rc)
-      rc = run_plan(ctx, portion(sp, p, 0, c1[p], sp.n[p], sel), fo, st_p[p].p);
+  {
+    Plan pl[2];
+    fuse_parts(portion(sp, 0, 0, c1[0], sp.n[0], sel),
+               portion(sp, 1, 0, c1[1], sp.n[1], sel), fo, pl);
+    for (int p = 0; p < 2 && !rc; ++p) {
+      rc = qsg_set_state_zero(ctx, st_p[p].p, sp.n[p]);
+      if (!rc) rc = run_plan(ctx, std::move(pl[p]), st_p[p].p);
+    }
   }
   // Suffix plans of batched gates; host-looped gates fixed per s_host.
   for (size_t i = PR; i < S_dev_end; ++i) sel.k[i] = -1;
@@ -424,35 +436,40 @@ int qsg_hybrid_run(qsg_ctx* ctx, const qsg_circuit* c, const unsigned* parts,
   // Suffix plans (one per host-looped suffix path), kept with their device
   // matrices across root paths.
   std::vector<std::unique_ptr<PlanRuntime>> suffix_rts[2];
-  auto suffix_plan = [&](int p, uint64_t sh, PlanRuntime** out) -> bool {
-    if (suffix_rts[p].empty()) suffix_rts[p].resize(hmax);
-    auto& rt = suffix_rts[p][sh];
-    if (!rt) {
+  for (auto& v : suffix_rts) v.resize(hmax);
+  auto suffix_plans = [&](uint64_t sh, PlanRuntime** out) -> bool {
+    if (!suffix_rts[0][sh]) {
       if (!select(sp, S_dev_end, G, sh, &sel, nullptr)) return false;
-      rt = std::make_unique<PlanRuntime>();
-      rt->plan = fuse(portion(sp, p, c2[p], sp.ops[p].size(),
-                              sp.n[p] + dev_bits, sel),
-                      fo);
+      Plan pl[2];
+      fuse_parts(portion(sp, 0, c2[0], sp.ops[0].size(), sp.n[0] + dev_bits, sel),
+                 portion(sp, 1, c2[1], sp.ops[1].size(), sp.n[1] + dev_bits, sel),
+                 fo, pl);
+      for (int p = 0; p < 2; ++p) {
+        suffix_rts[p][sh] = std::make_unique<PlanRuntime>();
+        suffix_rts[p][sh]->plan = std::move(pl[p]);
+      }
     }
-    *out = rt.get();
+    out[0] = suffix_rts[0][sh].get();
+    out[1] = suffix_rts[1][sh].get();
     return true;
   };
   uint64_t paths = 0;
   for (uint64_t r = 0; r < rmax && !rc; ++r) {
     if (!select(sp, P, PR, r, &sel, nullptr)) continue;
+    Plan pl[2];
+    fuse_parts(portion(sp, 0, c1[0], c2[0], sp.n[0], sel),
+               portion(sp, 1, c1[1], c2[1], sp.n[1], sel), fo, pl);
     for (int p = 0; p < 2 && !rc; ++p) {
       rc = qsg_copy_d2d(ctx, st_r[p].p, st_p[p].p, sp.n[p]);
-      if (!rc)
-        rc = run_plan(ctx, portion(sp, p, c1[p], c2[p], sp.n[p], sel), fo,
-                      st_r[p].p);
+      if (!rc) rc = run_plan(ctx, std::move(pl[p]), st_r[p].p);
     }
     for (uint64_t sh = 0; sh < hmax && !rc; ++sh) {
-      PlanRuntime* pl[2];
-      if (!suffix_plan(0, sh, &pl[0]) || !suffix_plan(1, sh, &pl[1])) continue;
+      PlanRuntime* srt[2];
+      if (!suffix_plans(sh, srt)) continue;
       for (int p = 0; p < 2 && !rc; ++p) {
         rc = qsg_copy_d2d(ctx, big[p].p, st_r[p].p, sp.n[p]);
         if (!rc) rc = hybrid_broadcast(ctx, big[p].p, sp.n[p], dev_bits);
-        if (!rc) rc = pl[p]->run(ctx, big[p].p, 0, nullptr);
+        if (!rc) rc = srt[p]->run(ctx, big[p].p, 0, nullptr);
       }
       if (!rc)
         rc = hybrid_collect(ctx, big[0].p, sp.n[0], big[1].p, sp.n[1],
