@@ -653,6 +653,32 @@ def hybrid_cpu_sample(c, parts, num_prefix, paths, max_paths=16):
                       f"FP32 port), x {paths} paths"}
 
 
+def hybrid_case(tensor: bool):
+    """One small qsimh job for ncu captures: the 24-qubit 4x6 grid depth-14
+    circuit cut into column halves (12 + 12 qubits, 12 fSim gates on the
+    cut), 5 gates fixed by the prefix, the other 7 (14 path bits = 16384
+    paths, batch states of 2^26 amplitudes, 512 MiB per part) summed for 1000
+    amplitudes; a warm-up job, then the job the capture looks at."""
+    import numpy as np
+    from qsim_gb300 import api, engine as E, hybrid
+    c = E.Circuit.grid(4, 6, 0, 14, 1)
+    n = c.num_qubits
+    parts = [0 if (q % 6) < 3 else 1 for q in range(n)]
+    bits = np.random.default_rng(11).integers(0, 1 << n, 1000, dtype=np.uint64)
+    ctx = api.Context(0)
+    kw = dict(num_prefix_gatexs=5, max_fused_size=6 if tensor else 4,
+              tensor_path=tensor)
+    hybrid.run(ctx, c, parts, bits, **kw)
+    ctx.sync()
+    before = ctx.launches()
+    t0 = time.perf_counter()
+    _, info = hybrid.run(ctx, c, parts, bits, **kw)
+    ctx.sync()
+    print(json.dumps({"hybrid_case": info, "s_per_job": time.perf_counter() - t0,
+                      "launches_before": before,
+                      "launches": ctx.launches() - before}), flush=True)
+
+
 UNITARY_GRID = dict(rows=2, cols=7, extra=0, cycles=14, seed=1)
 
 
@@ -961,11 +987,16 @@ def main():
                     choices=["auto", "packed", "streams"])
     ap.add_argument("--traj-split", type=int, default=-1,
                     help="largest qubit count run in the packed kernel")
+    ap.add_argument("--hybrid-case", default=None, choices=["plain", "tc"],
+                    help="one small qsimh job (for ncu captures), then exit")
     ap.add_argument("--traj-ctas-per-sm", type=int, default=0)
     ap.add_argument("--traj-tile-kib", type=int, default=0)
     args = ap.parse_args()
     if args.kernel_case:
         kernel_case(args.kernel_case, args.qubits, args.reps)
+        return
+    if args.hybrid_case:
+        hybrid_case(args.hybrid_case == "tc")
         return
     if args.traj_only:
         print(json.dumps({"trajectories": bench_trajectories(
