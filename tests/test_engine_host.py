@@ -132,6 +132,20 @@ def test_planner_pass_counts_vs_reference_fuser(E):
             assert mine <= 1.1 * ref[f - 2] + 1, (name, f, mine, ref[f - 2])
 
 
+def test_multi_start_fusion_is_deterministic_and_fewest(E):
+    """Tensor-core plans try several seed windows on parallel host threads
+    and keep the fewest blocks (the first of equal ones): the same plan on
+    every call, never more blocks than any single window."""
+    c = E.Circuit.grid(5, 6, 0, 20, 1)
+    plans = [E.Plan(c, max_fused_size=6, tensor_path=True) for _ in range(3)]
+    sig = [[(o["qs"], o["members"]) for o in p.ops()] for p in plans]
+    assert sig[0] == sig[1] == sig[2]
+    assert len(plans[0]) == 36
+    for w in (2, 3, 4, 6, 8, 12):
+        single = E.Plan(c, max_fused_size=6, seeds=w)
+        assert len(plans[0]) <= len(single)
+
+
 def test_grid_generator_invariants(E):
     rows, cols, cycles = 4, 5, 14
     c = E.Circuit.grid(rows, cols, 0, cycles, 11)
