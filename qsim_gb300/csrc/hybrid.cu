@@ -45,7 +45,23 @@ __global__ void __launch_bounds__(kThreads)
        w < m; w += warps) {
     const uint64_t i0 = idx[2 * w], i1 = idx[2 * w + 1];
     double re = 0, im = 0;
-    for (uint64_t b = lane; b < blocks; b += 32) {
+    uint64_t b = lane;
+    // Four blocks per lane and step, loads first: the gathers are scattered
+    // 8-byte reads, so more of them in flight hide more latency.
+    for (; b + 96 < blocks; b += 128) {
+      float2 a[4], c[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        a[j] = s0[i0 + ((b + 32 * j) << n0)];
+        c[j] = s1[i1 + ((b + 32 * j) << n1)];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        re += double(a[j].x * c[j].x - a[j].y * c[j].y);
+        im += double(a[j].x * c[j].y + a[j].y * c[j].x);
+      }
+    }
+    for (; b < blocks; b += 32) {
       const float2 a = s0[i0 + (b << n0)];
       const float2 c = s1[i1 + (b << n1)];
       re += double(a.x * c.x - a.y * c.y);
