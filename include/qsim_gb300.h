@@ -110,21 +110,24 @@ int qsg_real_inner_product(qsg_ctx* ctx, const float* s1, const float* s2,
 /* Norm (:239-241): sum |s[i]|^2 in FP64. */
 int qsg_norm(qsg_ctx* ctx, const float* state, unsigned n, double* out);
 /* Norm that allocates nothing; no counterpart in the reference.  For callers
- * that must not allocate memory once they are running: for example code
- * that runs while a CUDA stream is being captured into a graph, a real-time
- * loop with a fixed memory budget, or a host that installs its own device
- * allocator and forbids allocation behind its back.  qsg_norm may grow the
- * context's scratch (cudaMalloc) and pinned result slot (cudaMallocHost) on
- * its first use; this variant keeps its partial sums in a fixed 64 KiB
- * device array inside the library and returns the result through a plain
- * device-to-host copy, so it never allocates.  Same result as qsg_norm (same
- * kernels and partition).  Limits: the reduction may need at most 4096
- * partial sums (8 per SM; any GPU with up to 512 SMs) and larger requests
- * fail with QSG_ERR_INVALID.  The first call on a device looks up the
- * array's device address, so make that call before any stream capture.
- * There is one array per device: calls that overlap in time on the same
- * device (from several threads or streams) race on it and must be
- * serialised by the caller. */
+ * that cannot allocate memory once they are running: a host application that
+ * has already reserved nearly all device memory for its own pool (so a
+ * cudaMalloc would fail or evict its data), a real-time loop with a fixed
+ * memory budget, or a program that installs its own device allocator and
+ * forbids allocation behind its back.  qsg_norm may grow the context's
+ * scratch (cudaMalloc) and pinned result slot (cudaMallocHost) on its first
+ * use; this variant keeps its partial sums in a fixed 64 KiB device array
+ * inside the library and returns the result through a plain device-to-host
+ * copy followed by a synchronisation of the context stream, so it never
+ * allocates.  Same result as qsg_norm (same kernels and partition).  Limits:
+ * the reduction may need at most 4096 partial sums (8 per SM; any GPU with
+ * up to 512 SMs) and larger requests fail with QSG_ERR_INVALID.  The first
+ * call on a device looks up the array's device address (with that device
+ * made current), so make that call before any stream capture.  The call
+ * makes the context's device current for its duration and restores the
+ * caller's device afterwards.  There is one array per device: calls that
+ * overlap in time on the same device (from several threads or streams) race
+ * on it and must be serialised by the caller. */
 int qsg_norm_noalloc(qsg_ctx* ctx, const float* state, unsigned n,
                      double* out);
 /* PartialNorms (:331-355).  The state is cut into qsg_num_chunks(n) equal
@@ -583,6 +586,14 @@ int qsg_timer_start(qsg_ctx* ctx);
 int qsg_timer_stop(qsg_ctx* ctx, float* ms);
 /* Number of kernels this library launched on the context so far. */
 uint64_t qsg_ctx_launch_count(qsg_ctx* ctx);
+/* Bytes the context currently holds in its on-demand reduction scratch
+ * (device, cudaMalloc) and in its pinned result slot (host, cudaMallocHost);
+ * both start at 0 and grow on first use.  No counterpart in the reference
+ * (its StateSpaceCUDA allocates its scratch in the constructor,
+ * lib/statespace_cuda.h:54-66); a diagnostic for callers with a memory
+ * budget. */
+int qsg_ctx_scratch_bytes(qsg_ctx* ctx, size_t* device_bytes,
+                          size_t* pinned_bytes);
 
 #ifdef __cplusplus
 }  /* extern "C" */

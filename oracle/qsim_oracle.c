@@ -177,6 +177,122 @@ void orc_apply_gate_f32(float* s, unsigned n, const unsigned* qs, unsigned k,
   }
 }
 
+/* ---- lane-batched gate application ------------------------------------
+ * The reference's SIMD simulators (lib/simulator_avx512.h,
+ * lib/simulator_neon.h, lib/simulator_sse.h: ApplyGateH / ApplyGateL) hold
+ * the same amplitude of several consecutive groups in one vector register
+ * and multiply the gate matrix into 2^k such registers at once.  This is the
+ * portable restatement of that scheme: LANES consecutive groups at a time,
+ * the group amplitudes held as LANES-wide real and imaginary rows, and the
+ * matrix-vector product written as loops over the lanes that the C
+ * compiler vectorises (NEON on Arm, SSE/AVX on x86).  When the lowest
+ * target qubit is >= log2(LANES) the LANES groups are LANES consecutive
+ * amplitudes of every member (the reference's H case); otherwise their
+ * indices are gathered (the reference permutes inside registers, its L
+ * case).  The per-row sum runs over the columns in order, as in orc_apply_gate_f64.
+ * FP64: the oracle's fast path for large states.  FP32: the timed CPU
+ * baseline ("port").  Multi-threaded over group chunks like the
+ * reference's ParallelFor (lib/parfor.h:44-100). */
+#define ORC_LANES 16
+#define ORC_LANE_BITS 4 /* log2(ORC_LANES) */
+
+#define ORC_DEFINE_LANE_APPLY(T, NAME)                                        \
+  static inline __attribute__((always_inline)) void NAME##_body(             \
+      T* s, unsigned n, const unsigned* qs, const unsigned k, const T* m) {  \
+    const unsigned D = 1u << k;                                              \
+    uint64_t xss[64];                                                        \
+    member_offsets(qs, k, xss);                                              \
+    const uint64_t groups = UINT64_C(1) << (n - k);                          \
+    const int contiguous = (k == 0) || qs[0] >= ORC_LANE_BITS;               \
+    _Pragma("omp parallel for schedule(static)")                             \
+    for (int64_t g0 = 0; g0 < (int64_t)groups; g0 += ORC_LANES) {            \
+      uint64_t base[ORC_LANES];                                              \
+      T vr[64][ORC_LANES], vi[64][ORC_LANES];                                \
+      for (unsigned l = 0; l < ORC_LANES; ++l)                               \
+        base[l] = group_base((uint64_t)g0 + l, qs, k);                       \
+      if (contiguous) {                                                      \
+        for (unsigned c = 0; c < D; ++c) {                                   \
+          const T* p = s + 2 * (base[0] + xss[c]);                           \
+          for (unsigned l = 0; l < ORC_LANES; ++l) {                         \
+            vr[c][l] = p[2 * l];                                             \
+            vi[c][l] = p[2 * l + 1];                                         \
+          }                                                                  \
+        }                                                                    \
+      } else {                                                               \
+        for (unsigned c = 0; c < D; ++c)                                     \
+          for (unsigned l = 0; l < ORC_LANES; ++l) {                         \
+            vr[c][l] = s[2 * (base[l] + xss[c])];                            \
+            vi[c][l] = s[2 * (base[l] + xss[c]) + 1];                        \
+          }                                                                  \
+      }                                                                      \
+      for (unsigned r = 0; r < D; ++r) {                                     \
+        T ar[ORC_LANES], ai[ORC_LANES];                                      \
+        for (unsigned l = 0; l < ORC_LANES; ++l) ar[l] = ai[l] = 0;          \
+        for (unsigned c = 0; c < D; ++c) {                                   \
+          const T mr = m[2 * (r * D + c)], mi = m[2 * (r * D + c) + 1];      \
+          for (unsigned l = 0; l < ORC_LANES; ++l) {                         \
+            ar[l] += mr * vr[c][l] - mi * vi[c][l];                          \
+            ai[l] += mr * vi[c][l] + mi * vr[c][l];                          \
+          }                                                                  \
+        }                                                                    \
+        if (contiguous) {                                                    \
+          T* p = s + 2 * (base[0] + xss[r]);                                 \
+          for (unsigned l = 0; l < ORC_LANES; ++l) {                         \
+            p[2 * l] = ar[l];                                                \
+            p[2 * l + 1] = ai[l];                                            \
+          }                                                                  \
+        } else {                                                             \
+          for (unsigned l = 0; l < ORC_LANES; ++l) {                         \
+            s[2 * (base[l] + xss[r])] = ar[l];                               \
+            s[2 * (base[l] + xss[r]) + 1] = ai[l];                           \
+          }                                                                  \
+        }                                                                    \
+      }                                                                      \
+    }                                                                        \
+  }
+
+ORC_DEFINE_LANE_APPLY(double, lanes_f64)
+ORC_DEFINE_LANE_APPLY(float, lanes_f32)
+
+/* Dispatch on k so that every loop bound above is a compile-time constant.
+ * States with fewer than ORC_LANES groups take the one-group loops. */
+void orc_apply_gate_lanes_f64(double* s, unsigned n, const unsigned* qs,
+                              unsigned k, const double* m) {
+  if (k > 6 || n < k + ORC_LANE_BITS) {
+    orc_apply_gate_f64(s, n, qs, k, m);
+    return;
+  }
+  switch (k) {
+    case 0: lanes_f64_body(s, n, qs, 0, m); break;
+    case 1: lanes_f64_body(s, n, qs, 1, m); break;
+    case 2: lanes_f64_body(s, n, qs, 2, m); break;
+    case 3: lanes_f64_body(s, n, qs, 3, m); break;
+    case 4: lanes_f64_body(s, n, qs, 4, m); break;
+    case 5: lanes_f64_body(s, n, qs, 5, m); break;
+    default: lanes_f64_body(s, n, qs, 6, m); break;
+  }
+}
+
+void orc_apply_gate_f32(float* s, unsigned n, const unsigned* qs, unsigned k,
+                        const float* m);
+
+void orc_port_apply_gate_f32(float* s, unsigned n, const unsigned* qs,
+                             unsigned k, const float* m) {
+  if (k > 6 || n < k + ORC_LANE_BITS) {
+    orc_apply_gate_f32(s, n, qs, k, m);
+    return;
+  }
+  switch (k) {
+    case 0: lanes_f32_body(s, n, qs, 0, m); break;
+    case 1: lanes_f32_body(s, n, qs, 1, m); break;
+    case 2: lanes_f32_body(s, n, qs, 2, m); break;
+    case 3: lanes_f32_body(s, n, qs, 3, m); break;
+    case 4: lanes_f32_body(s, n, qs, 4, m); break;
+    case 5: lanes_f32_body(s, n, qs, 5, m); break;
+    default: lanes_f32_body(s, n, qs, 6, m); break;
+  }
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -52,6 +52,17 @@
 //       circuit (CircuitQsimParser, double), parts as "0,1,1,...", the
 //       bitstrings a raw uint64 file; writes the amplitudes as complex
 //       doubles (each result starts from 0).
+//   plan <gates> <max_fused_size> <out>
+//       MultiQubitGateFuser's fused gates for the gate list (matrix gates
+//       only), as QSimRunner applies them: per fused gate a uint32 k, k
+//       uint32 qubits (ascending) and the 2*4^k floats of its matrix
+//       (CalculateFusedMatrix, lib/fuser.h:149-179).
+//   bench <gates> <max_fused_size> <reps> <threads>
+//       QSimRunner<IO, MultiQubitGateFuser, host SIMD simulator>::Run on
+//       the gate list from |0...0> in float with ParallelFor(threads),
+//       `reps` times; prints one line per run: the wall seconds of Run
+//       (fusion + every fused gate, the state synchronised), then the
+//       seconds of FuseGates alone.
 //   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
 //       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
 //       with one std::mt19937(seed); writes bits per round (.bits) and the
@@ -485,6 +496,73 @@ static int CmdHybrid(int argc, char** argv) {
   return 0;
 }
 
+struct Factory32T {
+  using Simulator = qsim::Simulator<For>;
+  using StateSpace = Simulator::StateSpace;
+  unsigned threads = 1;
+  StateSpace CreateStateSpace() const { return StateSpace(threads); }
+  Simulator CreateSimulator() const { return Simulator(threads); }
+};
+
+static int CmdPlan(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  unsigned fsize = std::atoi(argv[3]);
+  Circuit<Operation<float>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<float>(g));
+  auto fused = MultiQubitGateFuser<IO>::FuseGates(
+      MultiQubitGateFuser<IO>::Parameter{fsize, 0}, n, circuit.ops);
+  FILE* f = std::fopen(argv[4], "wb");
+  if (!f) return 1;
+  for (const auto& op : fused) {
+    const auto* pg = OpGetAlternative<FusedGate<float>>(op);
+    if (!pg) continue;
+    const uint32_t k = pg->qubits.size();
+    std::fwrite(&k, 4, 1, f);
+    for (unsigned q : pg->qubits) {
+      const uint32_t q32 = q;
+      std::fwrite(&q32, 4, 1, f);
+    }
+    std::fwrite(pg->matrix.data(), sizeof(float), pg->matrix.size(), f);
+  }
+  std::fclose(f);
+  return 0;
+}
+
+static int CmdBench(int argc, char** argv) {
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  unsigned fsize = std::atoi(argv[3]);
+  unsigned reps = std::atoi(argv[4]);
+  Circuit<Operation<float>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<float>(g));
+  Factory32T factory;
+  factory.threads = std::atoi(argv[5]);
+  using Runner = QSimRunner<IO, MultiQubitGateFuser<IO>, Factory32T>;
+  Runner::Parameter param;
+  param.max_fused_size = fsize;
+  param.seed = 1;
+  param.verbosity = 0;
+  auto ss = factory.CreateStateSpace();
+  auto s = ss.Create(n);
+  if (ss.IsNull(s)) return 1;
+  for (unsigned r = 0; r < reps; ++r) {
+    ss.SetStateZero(s);
+    const double t0 = GetTime();
+    if (!Runner::Run(param, factory, circuit, s)) return 1;
+    ss.DeviceSync();
+    const double t1 = GetTime();
+    auto fused = MultiQubitGateFuser<IO>::FuseGates(
+        MultiQubitGateFuser<IO>::Parameter{fsize, 0}, n, circuit.ops);
+    const double t2 = GetTime();
+    std::printf("%.6f %.6f %zu\n", t1 - t0, t2 - t1, fused.size());
+    std::fflush(stdout);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   if (std::string(argv[1]) == "unitary") return CmdUnitary(argc, argv);
@@ -496,5 +574,7 @@ int main(int argc, char** argv) {
   if (cmd == "run") return CmdRun(argc, argv);
   if (cmd == "measure") return CmdMeasure(argc, argv);
   if (cmd == "traj") return CmdTraj(argc, argv);
+  if (cmd == "plan") return CmdPlan(argc, argv);
+  if (cmd == "bench") return CmdBench(argc, argv);
   return 2;
 }

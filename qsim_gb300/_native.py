@@ -34,6 +34,8 @@ SIGNATURES = {
     "qsg_ctx_num_sms": (i32, [vp, C.POINTER(C.c_int)]),
     "qsg_ctx_stream": (vp, [vp]),
     "qsg_ctx_launch_count": (u64, [vp]),
+    "qsg_ctx_scratch_bytes": (i32, [vp, C.POINTER(C.c_size_t),
+                                    C.POINTER(C.c_size_t)]),
     "qsg_min_size": (u64, [u32]),
     "qsg_state_create": (i32, [vp, u32, C.POINTER(vp)]),
     "qsg_state_free": (i32, [vp, vp]),

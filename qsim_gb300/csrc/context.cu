@@ -194,6 +194,14 @@ void* qsg_ctx_stream(qsg_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
 
 uint64_t qsg_ctx_launch_count(qsg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int qsg_ctx_scratch_bytes(qsg_ctx* ctx, size_t* device_bytes,
+                          size_t* pinned_bytes) {
+  QSG_CHECK_ARG(ctx && device_bytes && pinned_bytes, "null argument");
+  *device_bytes = ctx->scratch_size;
+  *pinned_bytes = ctx->hscratch_size;
+  return QSG_OK;
+}
+
 uint64_t qsg_min_size(unsigned num_qubits) { return min_size(num_qubits); }
 
 int qsg_state_create(qsg_ctx* ctx, unsigned n, float** out) {

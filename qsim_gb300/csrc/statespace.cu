@@ -760,7 +760,7 @@ static std::mutex g_norm_noalloc_mu;
 static double2* g_norm_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 // Device address of the array for `device`, looked up once per device with
-// that device current.
+// that device current (qsg_norm_noalloc makes it current first).
 static int norm_noalloc_scratch(int device, double2** out) {
   std::lock_guard<std::mutex> lock(g_norm_noalloc_mu);
   if (device < 0 || device >= kNoAllocMaxDevices) {
@@ -768,12 +768,9 @@ static int norm_noalloc_scratch(int device, double2** out) {
     return QSG_ERR_INVALID;
   }
   if (g_norm_noalloc_ptr[device] == nullptr) {
-    int cur = -1;
-    QSG_CUDA(cudaGetDevice(&cur));
-    if (cur != device) QSG_CUDA(cudaSetDevice(device));
+    // The caller has made `device` current.
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_norm_noalloc_scratch);
-    if (cur != device) cudaSetDevice(cur);
     if (e != cudaSuccess)
       return cuda_status(e, "cudaGetSymbolAddress(norm scratch)");
     g_norm_noalloc_ptr[device] = static_cast<double2*>(p);
@@ -792,6 +789,18 @@ int qsg_norm_noalloc(qsg_ctx* ctx, const float* state, unsigned n,
   QSG_CHECK_ARG(grid <= kNormNoAllocPartials,
                 "qsg_norm_noalloc: %u partial sums needed, the fixed scratch "
                 "holds %u", grid, kNormNoAllocPartials);
+  // The context's device is current for the whole call (the symbol lookup,
+  // the launches on ctx->stream and the copy); the caller's device comes
+  // back on every return path.
+  int caller_device = -1;
+  QSG_CUDA(cudaGetDevice(&caller_device));
+  if (caller_device != ctx->device) QSG_CUDA(cudaSetDevice(ctx->device));
+  struct Restore {
+    int dev, ctx_dev;
+    ~Restore() {
+      if (dev != ctx_dev) cudaSetDevice(dev);
+    }
+  } restore{caller_device, ctx->device};
   double2* scratch = nullptr;
   int rc = norm_noalloc_scratch(ctx->device, &scratch);
   if (rc) return rc;

@@ -16,7 +16,7 @@
 // (cost of the block) per block, i.e. the most time saved.
 
 #include <algorithm>
-#include <thread>
+#include <future>
 #include <cstring>
 
 #include "engine.h"
@@ -408,17 +408,20 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
     std::vector<unsigned> windows{opt.seeds};
     for (unsigned w : kStartWindows)
       if (w != opt.seeds) windows.push_back(w);
+    // std::async futures carry a worker's exception (bad_alloc, say) to
+    // get() on this thread, and their destructors wait for the worker, so
+    // an exception here never leaves a joinable thread behind.
     std::vector<Plan> plans(windows.size());
-    std::vector<std::thread> pool;
+    std::vector<std::future<Plan>> pool;
     for (size_t i = 1; i < windows.size(); ++i) {
-      pool.emplace_back([&, i] {
+      pool.push_back(std::async(std::launch::async, [&, i] {
         FuseOptions o = opt;
         o.seeds = windows[i];
-        plans[i] = fuse_greedy(c, o, f, false);
-      });
+        return fuse_greedy(c, o, f, false);
+      }));
     }
     plans[0] = fuse_greedy(c, opt, f, false);
-    for (auto& t : pool) t.join();
+    for (size_t i = 1; i < windows.size(); ++i) plans[i] = pool[i - 1].get();
     size_t best = 0;
     for (size_t i = 1; i < plans.size(); ++i)
       if (plans[i].ops.size() < plans[best].ops.size()) best = i;

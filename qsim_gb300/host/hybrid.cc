@@ -34,7 +34,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
-#include <thread>
+#include <future>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -263,12 +263,13 @@ int run_plan(qsg_ctx* ctx, Plan plan, float* state) {
   return rt.run(ctx, state, 0, nullptr);
 }
 
-// Fuses the two parts' circuits, part 1 on a host thread of its own.
+// Fuses the two parts' circuits, part 1 on a host thread of its own (a
+// future, so an exception on either thread reaches the caller).
 void fuse_parts(const Circuit& c0, const Circuit& c1, const FuseOptions& fo,
                 Plan* out) {
-  std::thread t([&] { out[1] = fuse(c1, fo); });
+  auto part1 = std::async(std::launch::async, [&] { return fuse(c1, fo); });
   out[0] = fuse(c0, fo);
-  t.join();
+  out[1] = part1.get();
 }
 
 }  // namespace

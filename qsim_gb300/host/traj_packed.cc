@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <new>
 #include <thread>
 
 #include <cuda_runtime.h>
@@ -130,8 +131,17 @@ int run_trajectory_batch_packed(int device, std::vector<BatchItem>& items,
           for (size_t j = t; j < packed.size(); j += nthreads) {
             const BatchItem& it = items[packed[j]];
             Program& p = progs[j];
-            p.rc = it.runner->build_program(it.rep, it.stats, &p.ops, &p.extra,
-                                            &p.extra_refs, &p.log_refs);
+            // An exception may not leave a host thread (std::terminate):
+            // it becomes this program's status.
+            try {
+              p.rc = it.runner->build_program(it.rep, it.stats, &p.ops,
+                                              &p.extra, &p.extra_refs,
+                                              &p.log_refs);
+            } catch (const std::bad_alloc&) {
+              p.rc = QSG_ERR_OOM;
+            } catch (...) {
+              p.rc = QSG_ERR_INVALID;
+            }
           }
         });
       }

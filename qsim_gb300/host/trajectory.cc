@@ -8,6 +8,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <random>
 #include <thread>
 
@@ -928,6 +929,9 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
         Worker& w = *wp;
         cudaSetDevice(device);
         cudaStream_t s = static_cast<cudaStream_t>(ctx_stream(w.ctx));
+        // An exception may not leave a host thread (std::terminate): it
+        // ends this worker with a status instead.
+        try {
         for (;;) {
           if (first_err.load() != QSG_OK) break;
           size_t item = size_t(-1);
@@ -962,6 +966,11 @@ int run_trajectory_batch(int device, std::vector<BatchItem>& items,
             w.rc = r;
             break;
           }
+        }
+        } catch (const std::bad_alloc&) {
+          w.rc = QSG_ERR_OOM;
+        } catch (...) {
+          w.rc = QSG_ERR_INVALID;
         }
         int r = w.ws.resolve();
         if (w.rc == QSG_OK) w.rc = r;

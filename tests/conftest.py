@@ -59,6 +59,8 @@ class Oracle:
             ("orc_expectation_value_f64", None,
              [dp, C.c_uint, up, C.c_uint, dp, dp]),
             ("orc_apply_gate_f32", None, [fp, C.c_uint, up, C.c_uint, fp]),
+            ("orc_apply_gate_lanes_f64", None, [dp, C.c_uint, up, C.c_uint, dp]),
+            ("orc_port_apply_gate_f32", None, [fp, C.c_uint, up, C.c_uint, fp]),
             ("orc_norm_f64", C.c_double, [dp, C.c_uint]),
             ("orc_inner_product_f64", None, [dp, dp, C.c_uint, dp]),
             ("orc_mt_seed", None, [C.c_void_p, C.c_uint32]),
@@ -145,6 +147,55 @@ class Oracle:
                 self.apply_controlled_gate(u, 2 * n, o["qs"], o["cqs"],
                                            o["cvals"], o["m"])
         return u.reshape(d, d)
+
+    def apply_gate_lanes(self, s, n, qs, m):
+        """orc_apply_gate_f64 restated lane-batched (same sums, vectorised):
+        the fast path for large states."""
+        m = np.ascontiguousarray(np.asarray(m, np.complex128)).view(np.float64)
+        self.L.orc_apply_gate_lanes_f64(self._dp(s), n, self._u32(qs), len(qs),
+                                        self._dp(m))
+
+    def run_ops_fp64_fused(self, n, ops):
+        """FP64 final state from |0...0> with every one-qubit gate folded
+        into the next two-qubit gate on its qubit, the matrix products in
+        FP64: QSimRunner with the reference's BasicGateFuser
+        (lib/fuser_basic.h: one-qubit gates fused into their neighbouring
+        two-qubit gates) on SimulatorBasic<For, double>
+        (lib/simulator_basic.h:31).  Controlled gates and gates on more
+        qubits are applied as they are, after the one-qubit gates pending on
+        their qubits.  A 30-qubit grid circuit of depth 20 takes ~270 passes
+        instead of ~840."""
+        s = self.zero_state(n)
+        pending = {}
+
+        def flush(qs):
+            for q in qs:
+                m = pending.pop(q, None)
+                if m is not None:
+                    self.apply_gate_lanes(s, n, [q], m)
+
+        for o in ops:
+            if o["kind"] == 0 and len(o["qs"]) == 1:
+                q = o["qs"][0]
+                m = np.asarray(o["m"], np.complex128)
+                pending[q] = m @ pending[q] if q in pending else m
+            elif o["kind"] == 0 and len(o["qs"]) == 2:
+                a, b = o["qs"]
+                pa = pending.pop(a, np.eye(2))
+                pb = pending.pop(b, np.eye(2))
+                m = np.asarray(o["m"], np.complex128) @ np.kron(pb, pa)
+                self.apply_gate_lanes(s, n, [a, b], m)
+            elif o["kind"] == 0:
+                flush(o["qs"])
+                self.apply_gate_lanes(s, n, o["qs"], o["m"])
+            elif o["kind"] == 1:
+                flush(list(o["qs"]) + list(o["cqs"]))
+                self.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"],
+                                           o["m"])
+            else:
+                flush(o.get("qs", ()))
+        flush(sorted(pending))
+        return s
 
     def run_ops(self, n, ops):
         s = self.zero_state(n)

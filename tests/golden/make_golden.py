@@ -25,7 +25,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 # The reference checkout whose test files hold known answers.
-REF_ROOT = os.environ.get("QSIM_REF", "/root/reference")
+REF_ROOT = os.environ.get("QSIM_REF",
+                          os.path.join(os.path.dirname(ROOT), "reference"))
 
 PAULI = {
     "I": np.eye(2, dtype=np.complex128),
@@ -286,6 +287,47 @@ def config1_case():
             s32=np.fromfile(out + ".s32", np.uint64),
             s64=np.fromfile(out + ".s64", np.uint64), meta=meta)
     print("config1_grid4x5d14 written")
+
+
+def read_ref_plan(path):
+    """Fused gates written by `ref_driver plan`: per gate k, k qubits and
+    the 2*4^k floats of its matrix."""
+    import struct
+    raw = open(path, "rb").read()
+    pos, ks, qs, ms = 0, [], [], []
+    while pos < len(raw):
+        k = struct.unpack_from("<I", raw, pos)[0]
+        pos += 4
+        qs.extend(struct.unpack_from(f"<{k}I", raw, pos))
+        pos += 4 * k
+        cnt = 2 * 4 ** k
+        ms.append(np.frombuffer(raw, np.float32, cnt, pos).copy())
+        pos += 4 * cnt
+        ks.append(k)
+    return (np.array(ks, np.int32), np.array(qs, np.int32),
+            np.concatenate(ms).astype(np.float32))
+
+
+def ref_plan_case():
+    """The reference's own fused plan (MultiQubitGateFuser, max_fused_size
+    4, matrices from CalculateFusedMatrix) of the 30-qubit 5x6 grid depth-20
+    circuit (seed 1): the gate passes the CPU baseline times, with no part
+    of this repository's engine in the loop."""
+    sys.path.insert(0, ROOT)
+    from qsim_gb300 import engine as E
+    c = E.Circuit.grid(5, 6, 0, 20, 1)
+    n = c.num_qubits
+    ops = [dict(kind="g", time=o["time"], qs=o["qs"], m=o["m"]) for o in c.ops()]
+    with tempfile.TemporaryDirectory() as td:
+        gl = os.path.join(td, "g.txt")
+        write_gate_list(gl, n, ops)
+        out = os.path.join(td, "plan.bin")
+        subprocess.run([DRIVER, "plan", gl, "4", out], check=True)
+        ks, qs, ms = read_ref_plan(out)
+    np.savez_compressed(os.path.join(HERE, "ref_plan_grid5x6d20_f4.npz"),
+                        n=np.int32(n), max_fused_size=np.int32(4), k=ks,
+                        qubits=qs, matrices=ms)
+    print(f"ref_plan_grid5x6d20_f4 written ({len(ks)} fused gates)")
 
 
 def mt_case():
@@ -923,6 +965,9 @@ def main():
     if sys.argv[1:] == ["pybind"]:
         pybind_cases()
         return
+    if sys.argv[1:] == ["refplan"]:
+        ref_plan_case()
+        return
     if sys.argv[1:] == ["hybrid"]:
         hybrid_known_case()
         hybrid_random_cases()
@@ -954,6 +999,7 @@ def main():
     hybrid_known_case()
     hybrid_random_cases()
     pybind_cases()
+    ref_plan_case()
 
 
 if __name__ == "__main__":

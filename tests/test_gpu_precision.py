@@ -14,7 +14,9 @@ Workloads (seeded synthetic circuits with the configurations' shapes):
 
 By default the grid is 4x6 (24 qubits) and the layered circuit has 20
 qubits; QSG_FULL_SIZE=1 runs the full sizes (5x6 grid = 30 qubits, FP64
-oracle 16 GiB on the host; layered circuit on 28 qubits).  Each test prints
+oracle 16 GiB on the host; layered circuit on 28 qubits).  The 30-qubit grid
+circuit's plain, tensor-core and learned forms are checked at full size in
+every run (test_headline_circuit_30q_against_fp64).  Each test prints
 one JSON line with the measured errors (pytest -s shows it)."""
 import json
 import os
@@ -37,14 +39,15 @@ def eng():
 
 
 def oracle_state(oracle, c):
-    n = c.num_qubits
-    s = oracle.zero_state(n)
-    for o in c.ops():
-        if o["kind"] == 0:
-            oracle.apply_gate(s, n, o["qs"], o["m"])
-        elif o["kind"] == 1:
-            oracle.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
-    return s
+    return oracle.run_ops_fp64_fused(c.num_qubits, c.ops())
+
+
+def state_c64(ss, st):
+    """The device state as a complex64 host array (no FP64 copy: 8 GiB at
+    30 qubits)."""
+    buf = np.empty(ss.MinSize(st.num_qubits()), dtype=np.float32)
+    ss.Copy(st, buf)
+    return buf[: 2 << st.num_qubits()].view(np.complex64)
 
 
 def errors(got, want):
@@ -82,9 +85,42 @@ def test_grid_circuit_forms_against_fp64(eng, oracle):
     for name, plan in forms.items():
         ss.SetStateZero(st)
         plan.run(ctx, st)
-        rel, fid = errors(ss.to_numpy(st), want)
+        rel, fid = errors(state_c64(ss, st), want)
         out["forms"][name] = {"rel_l2": rel, "fidelity": fid,
                               "passes": len(plan)}
+    print(json.dumps(out))
+    for name, r in out["forms"].items():
+        assert r["rel_l2"] <= 1e-5, name
+        assert r["fidelity"] >= 1 - 1e-6, name
+
+
+def test_headline_circuit_30q_against_fp64(eng, oracle):
+    """The 30-qubit 5x6 grid depth-20 circuit (seed 1) at its full size in
+    every default run: the plain CUDA-core f = 4 plan, the split-FP16
+    tensor-core f = 6 plan (the form the headline time is measured on) and
+    the learned planner's plan, each against the FP64 oracle (one-qubit
+    gates folded into two-qubit gates in FP64, 16 GiB on the host).  Bar:
+    relative L2 <= 1e-5 and fidelity >= 1 - 1e-6."""
+    q, E, ctx, ss, sim = eng
+    from qsim_gb300 import learned as L
+    c = E.Circuit.grid(5, 6, 0, 20, 1)
+    n = c.num_qubits
+    want = oracle.run_ops_fp64_fused(n, c.ops())
+    forms = {
+        "plain_f4": E.Plan(c, max_fused_size=4),
+        "tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5),
+        "learned_tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True,
+                                tc_min_k=2, cost_model=L.CostMLP.load()),
+    }
+    st = ss.Create(n)
+    out = {"workload": "grid5x6 (30 qubits) depth 20, seed 1", "forms": {}}
+    for name, plan in forms.items():
+        ss.SetStateZero(st)
+        plan.run(ctx, st)
+        rel, fid = errors(state_c64(ss, st), want)
+        out["forms"][name] = {"rel_l2": rel, "fidelity": fid,
+                              "passes": len(plan)}
+    del st
     print(json.dumps(out))
     for name, r in out["forms"].items():
         assert r["rel_l2"] <= 1e-5, name
@@ -100,7 +136,7 @@ def test_layered_controlled_expectations_against_fp64(eng, oracle):
     st = ss.Create(n)
     ss.SetStateZero(st)
     E.Plan(c, max_fused_size=4).run(ctx, st)
-    rel, fid = errors(ss.to_numpy(st), want)
+    rel, fid = errors(state_c64(ss, st), want)
     worst, tot, tot_ref = 0.0, 0.0, 0.0
     for qs, letters, coeff in E.pauli_sum(n, 64, 6, 5):
         m = pauli_matrix(letters)

@@ -1,7 +1,15 @@
-"""qsg_norm_noalloc, the allocation-free Norm: called through the C ABI and
-compared with qsg_norm (the existing entry point) and with an FP64 numpy
-norm, on two calls in a row.  The file name sorts last so that it also runs
-after every other test; it needs nothing from them and passes alone."""
+"""qsg_norm_noalloc, the Norm that allocates nothing, for callers that
+cannot allocate device or pinned host memory once they run (an application
+that has reserved nearly all device memory for its own pool, a fixed memory
+budget, an allocator that forbids allocation behind its back).
+
+Each case calls it first on a fresh context and checks that the context's
+on-demand scratch (device and pinned) is still empty afterwards; only then is
+qsg_norm, the existing entry point, called on the same state as the
+reference, and the allocation-free call is repeated (two calls in a row share
+the library's fixed array).  The file name sorts last so that a run that
+stops at the first failure has already run every other test; the cases need
+nothing from other tests and pass alone in a fresh process."""
 import ctypes as C
 
 import numpy as np
@@ -16,6 +24,12 @@ REL_TOL_SAME = 1e-12
 REL_TOL_FP64 = 1e-6
 
 
+def scratch_bytes(ctx):
+    dev, pinned = C.c_size_t(), C.c_size_t()
+    N.check(N.lib.qsg_ctx_scratch_bytes(ctx.h, C.byref(dev), C.byref(pinned)))
+    return dev.value, pinned.value
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 5, 13, 22])
 def test_norm_noalloc_matches_norm(n):
@@ -27,11 +41,17 @@ def test_norm_noalloc_matches_norm(n):
     amps = (rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)) * 0.37
     ss.from_numpy(amps, st)
     want64 = float(np.sum(np.abs(amps.astype(np.complex64).astype(np.complex128)) ** 2))
+    assert scratch_bytes(ctx) == (0, 0)
+    first = C.c_double(-1.0)
+    N.check(N.lib.qsg_norm_noalloc(ctx.h, st.get(), n, C.byref(first)))
+    # Nothing was allocated on the context by the allocation-free call.
+    assert scratch_bytes(ctx) == (0, 0)
     ref = C.c_double()
     N.check(N.lib.qsg_norm(ctx.h, st.get(), n, C.byref(ref)))
-    for _ in range(2):
-        out = C.c_double(-1.0)
-        N.check(N.lib.qsg_norm_noalloc(ctx.h, st.get(), n, C.byref(out)))
+    assert scratch_bytes(ctx) != (0, 0)   # the ordinary Norm did allocate
+    second = C.c_double(-1.0)
+    N.check(N.lib.qsg_norm_noalloc(ctx.h, st.get(), n, C.byref(second)))
+    for out in (first, second):
         assert abs(out.value - ref.value) <= REL_TOL_SAME * ref.value
         assert abs(out.value - want64) <= REL_TOL_FP64 * want64
 
@@ -45,3 +65,4 @@ def test_norm_noalloc_rejects_bad_arguments():
     assert N.lib.qsg_norm_noalloc(ctx.h, st.get(), 41, C.byref(out)) == 1
     assert b"qubits" in N.lib.qsg_last_error()
     assert N.lib.qsg_norm_noalloc(ctx.h, None, 3, C.byref(out)) == 1
+    assert scratch_bytes(ctx) == (0, 0)
