@@ -77,8 +77,20 @@ int qsg_copy_h2d(qsg_ctx* ctx, float* dest, const float* host_src, unsigned n);
 int qsg_copy_h2d_partial(qsg_ctx* ctx, float* dest, const float* host_src,
                          uint64_t size, unsigned n);
 
-/* Page-locked host buffers for fast host<->device copies of whole states. */
+/* Page-locked host buffers for fast host<->device copies of whole states.
+ * No counterpart in the reference (its copies use pageable host memory,
+ * lib/vectorspace_cuda.h:116-160).  qsg_host_alloc uses cudaMallocHost.
+ * qsg_host_alloc_near places the pages on the host NUMA node nearest to
+ * `device` (cudaDevAttrHostNumaId; preferred, not strict, so a full node
+ * falls back to another one) and pins them with cudaHostRegister: on hosts
+ * with several CPU sockets a pinned buffer on the far socket halves or
+ * worse the device<->host copy rate.  Where the device reports no host NUMA
+ * node it is qsg_host_alloc.  qsg_host_free releases either kind. */
 int qsg_host_alloc(size_t bytes, void** out);
+int qsg_host_alloc_near(int device, size_t bytes, void** out);
+/* The host NUMA node nearest to `device` (cudaDevAttrHostNumaId), -1 where
+ * the device reports none. */
+int qsg_host_numa_node(int device, int* out);
 int qsg_host_free(void* p);
 
 /* ---- state space (lib/statespace_cuda.h) ------------------------------- */
@@ -191,6 +203,18 @@ int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
 /* Reads and clears the tensor-core kernels' error flag: 1 if a bounded
  * device-side wait gave up (the kernel then skipped its remaining tiles). */
 int qsg_tc_error(qsg_ctx* ctx, int* out);
+/* Failure-detection test of the tensor-core kernel's bounded waits; no
+ * counterpart in the reference (its CUDA errors exit the process,
+ * lib/util_cuda.h:31-39).  Launches the kernel with the identity on qubits
+ * 0..5 of an n-qubit state (12 <= n <= 24) and a wait budget of
+ * `wait_cycles` SM clocks (1000 .. ~2 s), its MMA thread first waiting on a
+ * barrier that no thread arrives at: that wait runs out before any MMA is
+ * issued, every role takes the error exit (tensor memory freed, copies in
+ * flight awaited) and the state is left unchanged.  Returns QSG_ERR_TIMEOUT
+ * when the kernel reported the expired wait (the expected result), and
+ * clears the flag, so later launches on the context run normally. */
+int qsg_tc_stall_test(qsg_ctx* ctx, float* state, unsigned n,
+                      long long wait_cycles);
 /* SIMDRegisterSize (:265-267). */
 unsigned qsg_simd_register_size(void);
 

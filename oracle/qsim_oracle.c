@@ -293,6 +293,44 @@ void orc_port_apply_gate_f32(float* s, unsigned n, const unsigned* qs,
   }
 }
 
+/* ---- FP32-state reductions of the CPU port ----------------------------
+ * StateSpace::Norm (lib/statespace_basic.h:144-160: FP32 products, double
+ * sums), Multiply (:125-142) and the one-qubit diagonal ExpectationValue that
+ * QuantumTrajectorySimulator needs for <psi|K^dagger K|psi>
+ * (lib/qtrajectory.h:331-380), multi-threaded like the reference's
+ * ParallelFor reductions. */
+double orc_port_norm_f32(const float* s, unsigned n) {
+  const int64_t N = (int64_t)1 << n;
+  double acc = 0;
+#pragma omp parallel for schedule(static) reduction(+ : acc)
+  for (int64_t i = 0; i < N; ++i)
+    acc += (double)(s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1]);
+  return acc;
+}
+
+void orc_port_scale_f32(float* s, unsigned n, float a) {
+  const int64_t N = (int64_t)2 << n;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) s[i] *= a;
+}
+
+/* sum_i |s_i|^2 d[bit q of i] */
+double orc_port_diag1_ev_f32(const float* s, unsigned n, unsigned q,
+                             double d0, double d1) {
+  const int64_t N = (int64_t)1 << n;
+  double a0 = 0, a1 = 0;
+#pragma omp parallel for schedule(static) reduction(+ : a0, a1)
+  for (int64_t i = 0; i < N; ++i) {
+    const double p =
+        (double)(s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1]);
+    if ((i >> q) & 1)
+      a1 += p;
+    else
+      a0 += p;
+  }
+  return d0 * a0 + d1 * a1;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

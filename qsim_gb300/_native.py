@@ -40,6 +40,8 @@ SIGNATURES = {
     "qsg_state_create": (i32, [vp, u32, C.POINTER(vp)]),
     "qsg_state_free": (i32, [vp, vp]),
     "qsg_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
+    "qsg_host_alloc_near": (i32, [i32, C.c_size_t, C.POINTER(vp)]),
+    "qsg_host_numa_node": (i32, [i32, C.POINTER(C.c_int)]),
     "qsg_host_free": (i32, [vp]),
     "qsg_copy_d2d": (i32, [vp, vp, vp, u32]),
     "qsg_copy_d2h": (i32, [vp, vp, vp, u32]),
@@ -72,6 +74,7 @@ SIGNATURES = {
     "qsg_expectation_value": (i32, [vp, vp, u32, P_u32, u32, P_f32, P_f64]),
     "qsg_apply_gate_tc": (i32, [vp, vp, u32, P_u32, u32, P_f32]),
     "qsg_tc_error": (i32, [vp, C.POINTER(C.c_int)]),
+    "qsg_tc_stall_test": (i32, [vp, vp, u32, C.c_longlong]),
     "qsg_simd_register_size": (u32, []),
     "qsg_rng_create": (vp, [u32]),
     "qsg_rng_destroy": (None, [vp]),

@@ -134,19 +134,21 @@ def runners_for(make_runners, qubits, cfg):
     return out
 
 
-def run(runners, items, cfg, num_streams: int = 8, out_states=None):
+def run(runners, items, cfg, num_streams: int = 8, out_states=None,
+        device: int = 0):
     """Runs `items` [(runner index, rep)] with configuration `cfg` (split 0:
-    stream path only); returns (per-item stats, latency_ms, wall seconds,
-    launches, info)."""
+    stream path only) on GPU `device`; returns (per-item stats, latency_ms,
+    wall seconds, launches, info)."""
     if cfg["split"] == 0:
         per, lat, wall, launches = E.run_trajectory_batch(
-            runners, items, num_streams=num_streams, out_states=out_states,
-            return_launches=True)
+            runners, items, num_streams=num_streams, device=device,
+            out_states=out_states, return_launches=True)
         return per, lat, wall, launches, None
     return E.run_trajectory_batch_packed(
         runners, items, ctas_per_sm=cfg["ctas_per_sm"],
         max_qubits=cfg["split"], tile_kib=cfg["tile_kib"],
-        num_streams=num_streams, overlap=True, out_states=out_states)
+        num_streams=num_streams, device=device, overlap=True,
+        out_states=out_states)
 
 
 def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
@@ -174,8 +176,10 @@ def tune_trajectories(make_runners, qubits, reps: int, tag: str = "",
         runners = runners_for(make_runners, qubits, cfg)
         items = [(i, 10**6 + r) for i in range(len(runners))
                  for r in range(sample_reps)]
-        run(runners, items[:len(runners)], cfg, num_streams)  # warm-up
-        _, _, wall, _, _ = run(runners, items, cfg, num_streams)
+        run(runners, items[:len(runners)], cfg, num_streams,
+            device=device)  # warm-up
+        _, _, wall, _, _ = run(runners, items, cfg, num_streams,
+                               device=device)
         table.append((cfg, len(items) / wall))
     best = max(table, key=lambda x: x[1])[0]
     if use_cache:

@@ -176,11 +176,11 @@ __device__ __forceinline__ void batch_gate_pass(float4* st, BatchShared& sm,
                 "tile budget");
   double er = 0, ei = 0;
   if constexpr (K >= 3) {
-    tile_pass<K, PAIR, 0, true, BatchStages<K, PAIR, BUDGET>::value>(
+    tile_pass<K, PAIR, 0, 1, BatchStages<K, PAIR, BUDGET>::value>(
         st, sm.geom.g, NoMat{}, sm.smat, tiles, 0, 1, er, ei);
   } else {
     const RegMat<K> m(mat);
-    tile_pass<K, PAIR, 0, false, BatchStages<K, PAIR, BUDGET>::value>(
+    tile_pass<K, PAIR, 0, 0, BatchStages<K, PAIR, BUDGET>::value>(
         st, sm.geom.g, m, nullptr, tiles, 0, 1, er, ei);
   }
 }

@@ -4,6 +4,12 @@
 
 #include <cstdarg>
 #include <cstring>
+#include <map>
+#include <mutex>
+
+#include <sys/mman.h>
+#include <sys/syscall.h>
+#include <unistd.h>
 
 #include "common.cuh"
 #include "internal.h"
@@ -242,8 +248,99 @@ int qsg_host_alloc(size_t bytes, void** out) {
   return QSG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Buffers of qsg_host_alloc_near that were mapped and registered here
+// (address -> length); everything else came from cudaMallocHost.
+std::mutex g_near_mu;
+std::map<void*, size_t> g_near_bufs;
+
+// Anonymous mapping with a preferred-node memory policy, pinned by
+// cudaHostRegister (which faults every page in, on that node).
+int host_alloc_on_node(int node, size_t bytes, void** out) {
+#ifdef SYS_mbind
+  constexpr int kMpolPreferred = 1;
+  constexpr int kMaskWords = 16;   // nodes 0..1023
+  if (node < 0 || node >= 64 * kMaskWords) return QSG_ERR_UNSUPPORTED;
+  void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE,
+                 MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED) return QSG_ERR_OOM;
+  unsigned long mask[kMaskWords] = {};
+  mask[node / 64] = 1ul << (node % 64);
+  // maxnode counts one bit more than the mask holds (the kernel drops the
+  // last one), as libnuma passes it.
+  if (syscall(SYS_mbind, p, bytes, kMpolPreferred, mask,
+              (unsigned long)(64 * kMaskWords + 1), 0u) != 0) {
+    munmap(p, bytes);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    munmap(p, bytes);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_near_mu);
+    g_near_bufs[p] = bytes;
+  }
+  *out = p;
+  return QSG_OK;
+#else
+  (void)node; (void)bytes; (void)out;
+  return QSG_ERR_UNSUPPORTED;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsg_host_numa_node(int device, int* out) {
+  QSG_CHECK_ARG(out, "qsg_host_numa_node: null out");
+  *out = -1;
+  if (cudaDeviceGetAttribute(out, cudaDevAttrHostNumaId, device) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    *out = -1;
+  }
+  return QSG_OK;
+}
+
+int qsg_host_alloc_near(int device, size_t bytes, void** out) {
+  QSG_CHECK_ARG(out, "qsg_host_alloc_near: null out");
+  *out = nullptr;
+  int node = -1;
+  if (cudaDeviceGetAttribute(&node, cudaDevAttrHostNumaId, device) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    node = -1;
+  }
+  if (node >= 0 && bytes > 0 &&
+      host_alloc_on_node(node, bytes, out) == QSG_OK)
+    return QSG_OK;
+  return qsg_host_alloc(bytes, out);
+}
+
 int qsg_host_free(void* p) {
-  if (p) QSG_CUDA(cudaFreeHost(p));
+  if (!p) return QSG_OK;
+  size_t bytes = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_near_mu);
+    auto it = g_near_bufs.find(p);
+    if (it != g_near_bufs.end()) {
+      bytes = it->second;
+      g_near_bufs.erase(it);
+    }
+  }
+  if (bytes) {
+    QSG_CUDA(cudaHostUnregister(p));
+    munmap(p, bytes);
+    return QSG_OK;
+  }
+  QSG_CUDA(cudaFreeHost(p));
   return QSG_OK;
 }
 

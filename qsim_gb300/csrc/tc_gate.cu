@@ -96,7 +96,7 @@ constexpr uint32_t kOffTabSplitO = kOffTabSplitE + 16;  // 4 x u32 op offset
 constexpr uint32_t kOffTabGrpE = kOffTabSplitO + 16;    // 64 x u32 group e
 constexpr uint32_t kOffTabRd = kOffTabGrpE + 256;       // 8 x u32 stage read
 constexpr uint32_t kOffTabWr = kOffTabRd + 32;          // 8 x u32 raw write
-constexpr uint32_t kNumBars = 4 * kNB + 1;
+constexpr uint32_t kNumBars = 4 * kNB + 2;  // + gate ready, + never arrived
 constexpr uint32_t kOffBar = kOffTabWr + 32;            // mbarriers
 constexpr uint32_t kOffFlag = kOffBar + 8 * kNumBars;   // failure flag
 constexpr uint32_t kOffNorm = kOffFlag + 16;             // 16 x f64 + carry
@@ -139,6 +139,13 @@ struct TcArgs {
   const double* prev;
   uint32_t prev_count;
   double* out;
+  // Clock budget of every bounded wait (kWaitCycles in normal launches).
+  long long wait_cycles;
+  // Failure-detection test hook (0 in normal launches): the MMA thread
+  // first waits on a barrier that no thread ever arrives at, so its bounded
+  // wait runs out before any MMA is issued and every role takes the error
+  // exit (the state is left as it was).
+  int stall;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -371,11 +378,12 @@ __device__ __forceinline__ void bar_sync(int id, int count) {
 // Bounded wait on an mbarrier phase; false if the clock budget ran out or
 // another role already failed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          volatile int* flag) {
+                                          volatile int* flag,
+                                          long long budget) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
     if (*flag) return false;
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > budget) {
       *flag = 1;
       return false;
     }
@@ -401,6 +409,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* acc_full = bars + 2 * kNB;  // [kNB] MMA commit -> epilogue
   uint64_t* acc_free = bars + 3 * kNB;  // [kNB] epilogue -> MMA
   uint64_t* gate_ready = bars + 4 * kNB;  // epilogue (gate in TMEM) -> MMA
+  uint64_t* never = bars + 4 * kNB + 1;   // no thread arrives (test hook)
   volatile int* flag = reinterpret_cast<volatile int*>(smem + kOffFlag);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kOffTmem);
   const uint32_t sbase = smem_u32(smem);
@@ -498,7 +507,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // Operand buffer s is free once the epilogue read tile i-kNB out of it
       // (the ((i-kNB)/kNB)-th completion of op_free[s]).
       bool bad = false;
-      if (i >= kNB) bad = !mbar_wait(&op_free[s], ((i - kNB) / kNB) & 1, flag);
+      if (i >= kNB) bad = !mbar_wait(&op_free[s], ((i - kNB) / kNB) & 1, flag,
+                                     a.wait_cycles);
       if (bar_or(1, kProdThreads, bad)) break;
       // Split the raw tile into FP16 hi / lo operand rows (K-major): four
       // members (8 K-elements, one 16-byte core-matrix row) per item.
@@ -611,7 +621,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     int i = 0;
     for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
       const int s = i % kNB;
-      const bool bad = !mbar_wait(&acc_full[s], (i / kNB) & 1, flag);
+      const bool bad =
+          !mbar_wait(&acc_full[s], (i / kNB) & 1, flag, a.wait_cycles);
       if (bar_or(2, kEpiThreads, bad)) break;
       tc_fence_after();
       uint32_t v[32];
@@ -667,16 +678,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (lane == 0) {
     // ======================== MMA issuer =================================
     int i = 0;
-    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+    // Test hook: a wait that nothing ends; it gives up after the budget and
+    // sets the flag, and the loop below then issues nothing.
+    const bool stalled = a.stall && !mbar_wait(never, 0, flag, a.wait_cycles);
+    for (uint64_t t = t0; !stalled && t < g.num_tiles; t += step, ++i) {
       const int s = i % kNB;
-      if (!mbar_wait(&op_full[s], (i / kNB) & 1, flag)) break;
+      if (!mbar_wait(&op_full[s], (i / kNB) & 1, flag, a.wait_cycles)) break;
       // The gate must be in tensor memory before the first MMA, and
       // accumulator s is free once the epilogue drained tile i-kNB (the
       // ((i-kNB)/kNB)-th completion of acc_free[s]).
       if (i == 0) {
-        if (!mbar_wait(gate_ready, 0, flag)) break;
+        if (!mbar_wait(gate_ready, 0, flag, a.wait_cycles)) break;
       } else if (i >= kNB) {
-        if (!mbar_wait(&acc_free[s], ((i - kNB) / kNB) & 1, flag)) break;
+        if (!mbar_wait(&acc_free[s], ((i - kNB) / kNB) & 1, flag,
+                       a.wait_cycles))
+          break;
       }
       tc_fence_after();
       const uint32_t obuf = kOffOp + s * kOpBytes;
@@ -712,9 +728,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       // The MMAs of an abandoned tile get one more bounded wait before
       // their tensor memory is released.
       const long long c0 = clock64();
-      while (clock64() - c0 < kWaitCycles / 4) {
+      while (clock64() - c0 < a.wait_cycles / 4) {
       }
     }
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(
                      tmem),
@@ -901,6 +918,10 @@ void tcring_release(qsg_ctx* ctx) {
 }
 
 static int* g_tc_err = nullptr;
+// Wait budget and test stall of the next launches; changed only for the
+// duration of qsg_tc_stall_test on the calling thread.
+static thread_local long long g_tc_wait_cycles = tc::kWaitCycles;
+static thread_local int g_tc_stall = 0;
 
 // One-time set-up (error flag, shared-memory opt-in); must precede any
 // graph capture that contains tensor-core launches.
@@ -964,6 +985,8 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
   a.prev = prev;
   a.prev_count = prev ? prev_count : 0;
   a.out = out;
+  a.wait_cycles = g_tc_wait_cycles;
+  a.stall = g_tc_stall;
   const uint64_t grid = std::min<uint64_t>(a.g.num_tiles, ctx->num_sms);
   tc_gate_kernel<<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
       reinterpret_cast<float2*>(state), a);
@@ -1011,6 +1034,37 @@ int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
 int qsg_tc_error(qsg_ctx* ctx, int* out) {
   QSG_CHECK_ARG(ctx && out, "qsg_tc_error: null argument");
   return tc_check_error(ctx, out);
+}
+
+int qsg_tc_stall_test(qsg_ctx* ctx, float* state, unsigned n,
+                      long long wait_cycles) {
+  QSG_CHECK_ARG(ctx && state, "qsg_tc_stall_test: null argument");
+  QSG_CHECK_ARG(wait_cycles >= 1000 && wait_cycles <= tc::kWaitCycles,
+                "qsg_tc_stall_test: wait budget %lld out of [1000, %lld]",
+                wait_cycles, tc::kWaitCycles);
+  QSG_CHECK_ARG(n >= unsigned(tc::kTileBits) && n <= 24,
+                "qsg_tc_stall_test: %u qubits (12..24)", n);
+  // The identity on qubits 0..5: had an MMA run, the state would not change.
+  std::vector<float> eye(2 * 64 * 64, 0.f);
+  for (int i = 0; i < 64; ++i) eye[2 * (i * 64 + i)] = 1.f;
+  const unsigned qs[6] = {0, 1, 2, 3, 4, 5};
+  int before = 0;
+  int rc = tc_check_error(ctx, &before);   // clears an older flag
+  if (rc) return rc;
+  g_tc_wait_cycles = wait_cycles;
+  g_tc_stall = 1;
+  rc = apply_gate_tc_host(ctx, state, n, qs, 6, eye.data());
+  g_tc_wait_cycles = tc::kWaitCycles;
+  g_tc_stall = 0;
+  if (rc) return rc;
+  int err = 0;
+  rc = tc_check_error(ctx, &err);
+  if (rc) return rc;
+  if (err) {
+    set_error("tensor-core kernel: a bounded wait gave up (test stall)");
+    return QSG_ERR_TIMEOUT;
+  }
+  return QSG_OK;
 }
 
 }  // extern "C"

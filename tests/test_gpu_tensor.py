@@ -148,3 +148,33 @@ def test_tc_deep_plan_keeps_norm_and_accuracy(eng, oracle):
     plan.replay(ctx)
     ctx.sync()
     assert rel_l2(ss.to_numpy(st), want) < 1e-5
+
+
+@pytest.mark.parametrize("n", [12, 16])
+def test_tc_bounded_wait_runs_out_and_context_recovers(eng, oracle, n):
+    """Failure detection without a GPU fault: the kernel's MMA thread waits
+    on a barrier that nothing arrives at, with a ~1 ms clock budget; the
+    wait runs out before any MMA is issued, every role leaves through the
+    error exit and the host reads QSG_ERR_TIMEOUT.  The state is unchanged,
+    the flag is cleared, and the next tensor-core gate on the same context
+    matches the oracle."""
+    import ctypes as C
+    q, E, N, ctx, ss, sim = eng
+    rng = np.random.default_rng(7 + n)
+    s0 = random_state(rng, n)
+    st = ss.Create(n)
+    ss.from_numpy(s0, st)
+    rc = N.lib.qsg_tc_stall_test(ctx.h, st.get(), n, C.c_longlong(2_000_000))
+    assert rc == 6, N.lib.qsg_last_error()          # QSG_ERR_TIMEOUT
+    assert b"bounded wait" in N.lib.qsg_last_error()
+    assert np.array_equal(ss.to_numpy(st), s0.astype(np.complex64))
+    assert tc_error(N, ctx) == 0
+    m = random_unitary(rng, 6)
+    qs = sorted(rng.choice(n, 6, replace=False).tolist())
+    apply_tc(N, ctx, st, n, qs, m)
+    ref = s0.copy()
+    oracle.apply_gate(ref, n, qs, m)
+    assert tc_error(N, ctx) == 0
+    assert rel_l2(ss.to_numpy(st), ref) <= 1e-5
+    # Out-of-range budgets are argument errors, not launches.
+    assert N.lib.qsg_tc_stall_test(ctx.h, st.get(), n, C.c_longlong(10)) == 1

@@ -225,3 +225,37 @@ def test_gpu_batched_workload_noise_vs_oracle(ctx, ss, oracle):
             agree += 1
             assert rel_l2(ss.to_numpy(st), s_ref) < STATE_TOL
     assert agree >= 5
+
+
+@pytest.mark.parametrize("case", ["traj_depol8", "traj_ad8", "traj_chain12"])
+def test_cpu_port_matches_reference(case, oracle):
+    """The timed FP32 CPU port of RunIteration (oracle/traj_port.py, the
+    trajectories' CPU baseline) makes the reference's Kraus choices and
+    reaches its final states."""
+    import traj_port
+    d = load_golden(case)
+    n = int(d["n"])
+    ops = traj_oracle.ops_from_fixture(d, unpack_ops)
+    is_chan = np.array(["channel" in op for op in ops])
+    ref32 = ref_samples(d, "32")
+    port = traj_port.TrajectoryPort(oracle.L, n)
+    agree = 0
+    for i, rep in enumerate(range(int(d["r0"]), int(d["r1"]))):
+        choices = port.run(ops, rep)
+        want = [int(x) for x, c in zip(ref32[i], is_chan) if c]
+        if choices == want:
+            agree += 1
+            got = port.state().astype(np.complex128)
+            assert rel_l2(got, d["f64"][i].astype(np.complex128)) < 1e-5
+    assert agree >= MIN_AGREE[case] * len(ref32), (case, agree, len(ref32))
+
+
+def test_cpu_port_noisy_ops_follow_make_noisy():
+    """traj_port.noisy_ops inserts channels by the engine's MakeNoisy rule:
+    the same channel count as the engine's noisy circuit."""
+    import traj_port
+    c = E.Circuit.chain(9, 6, 3)
+    nc = E.NoisyCircuit.make(c, 1e-3, 5e-3, 2)
+    ops = traj_port.noisy_ops(c.ops(), 9, 1e-3, 5e-3, 2)
+    assert sum("channel" in o for o in ops) == nc.info()["num_channels"]
+    assert sum("channel" not in o for o in ops) == len(c.ops())
