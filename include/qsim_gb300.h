@@ -80,12 +80,12 @@ int qsg_copy_h2d_partial(qsg_ctx* ctx, float* dest, const float* host_src,
 /* Page-locked host buffers for fast host<->device copies of whole states.
  * No counterpart in the reference (its copies use pageable host memory,
  * lib/vectorspace_cuda.h:116-160).  qsg_host_alloc uses cudaMallocHost.
- * qsg_host_alloc_near places the pages on the host NUMA node nearest to
- * `device` (cudaDevAttrHostNumaId; preferred, not strict, so a full node
- * falls back to another one) and pins them with cudaHostRegister: on hosts
- * with several CPU sockets a pinned buffer on the far socket halves or
- * worse the device<->host copy rate.  Where the device reports no host NUMA
- * node it is qsg_host_alloc.  qsg_host_free releases either kind. */
+ * qsg_host_alloc_near allocates it with the calling thread's memory policy
+ * set, for the call, to prefer the host NUMA node nearest to `device`
+ * (cudaDevAttrHostNumaId; preferred, not strict, so a full node falls back
+ * to another one): on hosts with several CPU sockets a pinned buffer on the
+ * far socket slows device<->host copies.  Where the device reports no host
+ * NUMA node it is qsg_host_alloc.  qsg_host_free releases either. */
 int qsg_host_alloc(size_t bytes, void** out);
 int qsg_host_alloc_near(int device, size_t bytes, void** out);
 /* The host NUMA node nearest to `device` (cudaDevAttrHostNumaId), -1 where
@@ -163,6 +163,16 @@ int qsg_find_measured_bits(qsg_ctx* ctx, const float* state, unsigned n,
 int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
                       uint64_t num_samples, const double* sorted_u,
                       uint64_t* out_bitstrings);
+/* Sample with absolute thresholds: `sorted_r` holds num_samples values on
+ * the scale of the running sum of |s|^2 (the reference's rs of
+ * GenerateRandomValues<DistrRealType>(num_samples, seed, norm), converted to
+ * double), sorted ascending; per j the first index k whose inclusive running
+ * sum exceeds r_j (2^n - 1 if none).  Serves Sample<DistrRealType> for
+ * DistrRealType other than double (lib/statespace_cuda.h:243-312), whose
+ * draws the caller makes with its own std::uniform_real_distribution. */
+int qsg_sample_thresholds(qsg_ctx* ctx, const float* state, unsigned n,
+                          uint64_t num_samples, const double* sorted_r,
+                          uint64_t* out_bitstrings);
 /* Sample with the reference's RNG convention: std::mt19937(seed) +
  * uniform_real_distribution<double>(0, norm), sorted (lib/util.h:67-85). */
 int qsg_sample(qsg_ctx* ctx, const float* state, unsigned n,

@@ -17,6 +17,7 @@
 #ifndef QSIM_GB300_STATESPACE_GB300_H_
 #define QSIM_GB300_STATESPACE_GB300_H_
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -24,6 +25,7 @@
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -249,16 +251,30 @@ class StateSpaceGB300 {
   }
 
   // lib/statespace_cuda.h:243-312: the same uniforms as the reference
-  // (std::mt19937(seed), uniform_real_distribution<DistrRealType>, sorted),
-  // CDF search on the device.
+  // (std::mt19937(seed), uniform_real_distribution<DistrRealType>(0, norm),
+  // sorted), CDF search on the device.  For double the library draws them
+  // (the same libstdc++ algorithm); for any other DistrRealType they are
+  // drawn here with the caller's std::uniform_real_distribution, in that
+  // type, as the reference's GenerateRandomValues (lib/util.h:67-85) does.
   template <typename DistrRealType = double>
   std::vector<uint64_t> Sample(const State& s, uint64_t num_samples,
                                unsigned seed) const {
     std::vector<uint64_t> out(num_samples);
-    if (num_samples > 0) {
+    if (num_samples == 0) return out;
+    if (std::is_same<DistrRealType, double>::value) {
       check(qsg_sample(ctx_->get(), s.get(), s.num_qubits(), num_samples,
                        seed, out.data()));
+      return out;
     }
+    const DistrRealType norm = DistrRealType(Norm(s));
+    std::mt19937 rgen(seed);
+    std::uniform_real_distribution<DistrRealType> distr(0.0, norm);
+    std::vector<DistrRealType> rs(num_samples);
+    for (auto& r : rs) r = distr(rgen);
+    std::sort(rs.begin(), rs.end());
+    std::vector<double> r64(rs.begin(), rs.end());
+    check(qsg_sample_thresholds(ctx_->get(), s.get(), s.num_qubits(),
+                                num_samples, r64.data(), out.data()));
     return out;
   }
 

@@ -418,6 +418,11 @@ static int cmp_double(const void* a, const void* b) {
   return (x > y) - (x < y);
 }
 
+static int cmp_float(const void* a, const void* b) {
+  float x = *(const float*)a, y = *(const float*)b;
+  return (x > y) - (x < y);
+}
+
 /* lib/util.h:67-85 GenerateRandomValues: m draws of
  * uniform_real_distribution<double>(0, max) from mt19937(seed), sorted. */
 void orc_generate_random_values(uint64_t m, uint32_t seed, double max_value,
@@ -426,6 +431,36 @@ void orc_generate_random_values(uint64_t m, uint32_t seed, double max_value,
   orc_mt_seed(&g, seed);
   for (uint64_t i = 0; i < m; ++i) out[i] = orc_uniform(&g, max_value);
   qsort(out, m, sizeof(double), cmp_double);
+}
+
+/* GenerateRandomValues<float> (lib/util.h:67-85): m draws of libstdc++'s
+ * uniform_real_distribution<float>(0, max) from mt19937(seed), i.e.
+ * generate_canonical<float, 24> from one 32-bit draw, (float(g) / 2^32)
+ * clamped below 1, times max in float; sorted. */
+void orc_generate_random_values_f32(uint64_t m, uint32_t seed, float max_value,
+                                    float* out) {
+  orc_mt19937 g;
+  orc_mt_seed(&g, seed);
+  for (uint64_t i = 0; i < m; ++i) {
+    float c = (float)orc_mt_next(&g) / 4294967296.0f;
+    if (c >= 1.0f) c = nextafterf(1.0f, 0.0f);
+    out[i] = c * (max_value - 0.0f) + 0.0f;
+  }
+  qsort(out, m, sizeof(float), cmp_float);
+}
+
+/* Sample against given sorted thresholds (FP64 CDF scan, as
+ * orc_sample_f64 after its draws). */
+void orc_sample_thresholds_f64(const double* s, unsigned n, uint64_t m,
+                               const double* rs, uint64_t* out) {
+  const uint64_t N = UINT64_C(1) << n;
+  uint64_t j = 0;
+  double csum = 0;
+  for (uint64_t k = 0; k < N && j < m; ++k) {
+    csum += s[2 * k] * s[2 * k] + s[2 * k + 1] * s[2 * k + 1];
+    while (j < m && rs[j] < csum) out[j++] = k;
+  }
+  for (; j < m; ++j) out[j] = N - 1;
 }
 
 /* lib/statespace_basic.h:187-226 Sample: FP64 CDF scan. */

@@ -16,7 +16,9 @@
 // Commands:
 //   mt <seed> <count> <out>
 //       raw std::mt19937 outputs (uint32) then `count` draws of
-//       uniform_real_distribution<double>(0,1) from a fresh mt19937(seed).
+//       uniform_real_distribution<double>(0,1) from a fresh mt19937(seed)
+//       (.u01), and `count` draws of uniform_real_distribution<float>(0,
+//       0.73) from another fresh mt19937(seed) (.f073).
 //   run <gates> <out-prefix> <max_fused_size> <num_samples> <sample_seed>
 //       [<ev-file>]
 //       .f64  : final state of SimulatorBasic<For,double>, ops unfused
@@ -213,9 +215,14 @@ static int CmdMt(int argc, char** argv) {
   std::uniform_real_distribution<double> d(0.0, 1.0);
   std::vector<double> u(count);
   for (auto& x : u) x = d(g2);
+  std::mt19937 g3(seed);
+  std::uniform_real_distribution<float> df(0.0f, 0.73f);
+  std::vector<float> uf(count);
+  for (auto& x : uf) x = df(g3);
   std::string out = argv[4];
   WriteRaw(out + ".raw", raw.data(), raw.size() * 4);
   WriteRaw(out + ".u01", u.data(), u.size() * 8);
+  WriteRaw(out + ".f073", uf.data(), uf.size() * 4);
   return 0;
 }
 

@@ -66,6 +66,7 @@ SIGNATURES = {
     "qsg_find_measured_bits": (i32, [vp, vp, u32, u64, f64, u64, P_u64]),
     "qsg_sample_sorted": (i32, [vp, vp, u32, u64, P_f64, P_u64]),
     "qsg_sample": (i32, [vp, vp, u32, u64, u32, P_u64]),
+    "qsg_sample_thresholds": (i32, [vp, vp, u32, u64, P_f64, P_u64]),
     "qsg_collapse": (i32, [vp, vp, u32, u64, u64]),
     "qsg_measure": (i32, [vp, vp, u32, u64, f64, i32, P_u64]),
     "qsg_apply_gate": (i32, [vp, vp, u32, P_u32, u32, P_f32]),

@@ -4,10 +4,6 @@
 
 #include <cstdarg>
 #include <cstring>
-#include <map>
-#include <mutex>
-
-#include <sys/mman.h>
 #include <sys/syscall.h>
 #include <unistd.h>
 
@@ -252,41 +248,35 @@ int qsg_host_alloc(size_t bytes, void** out) {
 
 namespace {
 
-// Buffers of qsg_host_alloc_near that were mapped and registered here
-// (address -> length); everything else came from cudaMallocHost.
-std::mutex g_near_mu;
-std::map<void*, size_t> g_near_bufs;
-
-// Anonymous mapping with a preferred-node memory policy, pinned by
-// cudaHostRegister (which faults every page in, on that node).
+// cudaMallocHost with this thread's memory policy set to "preferred node"
+// for the call (the pages are allocated and pinned inside it), then the
+// previous policy restored.  Preferred, not bound: a full node falls back to
+// another one instead of failing.
 int host_alloc_on_node(int node, size_t bytes, void** out) {
-#ifdef SYS_mbind
+#if defined(SYS_get_mempolicy) && defined(SYS_set_mempolicy)
   constexpr int kMpolPreferred = 1;
   constexpr int kMaskWords = 16;   // nodes 0..1023
-  if (node < 0 || node >= 64 * kMaskWords) return QSG_ERR_UNSUPPORTED;
-  void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE,
-                 MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-  if (p == MAP_FAILED) return QSG_ERR_OOM;
+  constexpr unsigned long kMaxNode = 64 * kMaskWords;
+  if (node < 0 || node >= int(kMaxNode)) return QSG_ERR_UNSUPPORTED;
+  int old_mode = 0;
+  unsigned long old_mask[kMaskWords] = {};
+  if (syscall(SYS_get_mempolicy, &old_mode, old_mask, kMaxNode, nullptr,
+              0ul) != 0)
+    return QSG_ERR_UNSUPPORTED;
   unsigned long mask[kMaskWords] = {};
   mask[node / 64] = 1ul << (node % 64);
   // maxnode counts one bit more than the mask holds (the kernel drops the
   // last one), as libnuma passes it.
-  if (syscall(SYS_mbind, p, bytes, kMpolPreferred, mask,
-              (unsigned long)(64 * kMaskWords + 1), 0u) != 0) {
-    munmap(p, bytes);
+  if (syscall(SYS_set_mempolicy, kMpolPreferred, mask, kMaxNode + 1) != 0)
     return QSG_ERR_UNSUPPORTED;
-  }
-  const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+  const cudaError_t e = cudaMallocHost(out, bytes);
+  syscall(SYS_set_mempolicy, old_mode, old_mode ? old_mask : nullptr,
+          old_mode ? kMaxNode + 1 : 0ul);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    munmap(p, bytes);
-    return QSG_ERR_UNSUPPORTED;
+    *out = nullptr;
+    return QSG_ERR_OOM;
   }
-  {
-    std::lock_guard<std::mutex> lock(g_near_mu);
-    g_near_bufs[p] = bytes;
-  }
-  *out = p;
   return QSG_OK;
 #else
   (void)node; (void)bytes; (void)out;
@@ -325,22 +315,7 @@ int qsg_host_alloc_near(int device, size_t bytes, void** out) {
 }
 
 int qsg_host_free(void* p) {
-  if (!p) return QSG_OK;
-  size_t bytes = 0;
-  {
-    std::lock_guard<std::mutex> lock(g_near_mu);
-    auto it = g_near_bufs.find(p);
-    if (it != g_near_bufs.end()) {
-      bytes = it->second;
-      g_near_bufs.erase(it);
-    }
-  }
-  if (bytes) {
-    QSG_CUDA(cudaHostUnregister(p));
-    munmap(p, bytes);
-    return QSG_OK;
-  }
-  QSG_CUDA(cudaFreeHost(p));
+  if (p) QSG_CUDA(cudaFreeHost(p));
   return QSG_OK;
 }
 

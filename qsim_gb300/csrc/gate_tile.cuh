@@ -19,16 +19,16 @@
 //  * When qubit 0 is not a target ("pair" mode) one work item holds two
 //    groups that differ in bit 0, so each 16-byte unit feeds both.  When
 //    qubit 0 is a target, a unit holds members (2p, 2p+1) of one group.
-// //  * For k <= 3 the matrix sits in kernel-parameter (constant) space and is
+//  * For k <= 3 the matrix sits in kernel-parameter (constant) space and is
 //    read with compile-time offsets, so FFMAs take it as a constant operand.
-//    For k >= 4 it is staged column-major in shared memory and 2^(k-3)
-//    threads split the rows of one work item (8 rows each), which keeps the
-//    code small and the register count low enough for five or more CTAs per
-//    SM.  For k = 4, 5 each entry is staged as the pairs (re, re) and
-//    (-im, im) so that a complex multiply-add is two packed two-lane FMAs
-//    (fma.rn.f32x2, sm_100 and later) with the same roundings in the same
-//    order as four scalar FMAs: the k = 4 pass needs 64 FMAs per amplitude
-//    and was issue-bound with scalar FFMAs.
+//    For k >= 4 it is staged column-major in shared memory (broadcast
+//    128-bit reads of two rows) and 2^(k-3) threads split the rows of one
+//    work item (8 rows each), which keeps the code small and the register
+//    count low enough for five or more CTAs per SM.  (Measured slower for
+//    k = 4 on GB300: packed two-lane FMAs, fma.rn.f32x2, which issue to one
+//    of the two FMA sub-pipes only; and the matrix as constant-bank
+//    operands with a fully unrolled code path per row block, which
+//    overflows the instruction cache.)
 #pragma once
 
 #include "common.cuh"
@@ -85,17 +85,13 @@ struct TileShape {
   static constexpr int ITEMS = kTileThreads / S;
   static constexpr int LOG_ITEMS = 7 - LOG_S;
   static constexpr bool SMEM_MAT = K >= 4;
-  // Shared-memory matrix layout of the single-gate kernel: 2 = packed pairs
-  // (16 B per entry, k = 4, 5), 1 = plain float2 (k = 6: 64 KiB of pairs
-  // would cost a CTA per SM), 0 = no shared-memory matrix.
-  static constexpr int SMAT_MODE = !SMEM_MAT ? 0 : (K <= 5 ? 2 : 1);
   static constexpr int TB = LOG_ITEMS + K + (PAIR ? 1 : 0);  // full tile
   static constexpr int UNITS = 1 << (TB - 1);
   static constexpr int LPT = UNITS / kTileThreads;  // 16-B units per thread
-  static constexpr size_t MAT_BYTES =
-      SMAT_MODE == 2 ? size_t(D) * D * 16 : (SMAT_MODE == 1 ? size_t(D) * D * 8 : 0);
+  static constexpr int MAT_FLOAT2 = SMEM_MAT ? D * D : 0;
   static constexpr int STAGES = 2;
-  static constexpr size_t SMEM = size_t(STAGES) * UNITS * 16 + MAT_BYTES;
+  static constexpr size_t SMEM =
+      size_t(STAGES) * UNITS * 16 + size_t(MAT_FLOAT2) * 8;
 };
 
 __device__ __forceinline__ uint64_t expand_outer(uint64_t t,
@@ -211,33 +207,14 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float2 m, float vr,
   ai = fmaf(m.y, vr, ai);
 }
 
-// d = a * b + d on two FP32 lanes at once (fma.rn.f32x2: each lane rounds
-// like fmaf).
-__device__ __forceinline__ void ffma2(float2& d, float2 a, float2 b) {
-  unsigned long long dd = *reinterpret_cast<unsigned long long*>(&d);
-  const unsigned long long aa = *reinterpret_cast<const unsigned long long*>(&a);
-  const unsigned long long bb = *reinterpret_cast<const unsigned long long*>(&b);
-  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(dd) : "l"(aa), "l"(bb));
-  d = *reinterpret_cast<float2*>(&dd);
-}
-
-// Complex d += m * v with m staged as mm = (re, re, -im, im): the lanes
-// compute re: fma(re, vr), fma(-im, vi); im: fma(re, vi), fma(im, vr), the
-// order and roundings of cmac.
-__device__ __forceinline__ void cmac2(float2& d, float4 mm, float2 v) {
-  ffma2(d, make_float2(mm.x, mm.y), v);
-  ffma2(d, make_float2(mm.z, mm.w), make_float2(v.y, v.x));
-}
-
 // One CTA's share of a gate pass: tiles t0, t0 + step, ... of geometry g,
 // pipelined through STAGES shared-memory tile buffers (cp.async).  MODE 0
-// applies the matrix, MODE 1 accumulates <s|M|s> into (er, ei).  SMAT 1: the
+// applies the matrix, MODE 1 accumulates <s|M|s> into (er, ei).  SMAT: the
 // matrix is read column-major from `smat` (2^k x 2^k float2, staged by the
-// caller); SMAT 2: column-major packed pairs (float4 (re, re, -im, im) per
-// entry); SMAT 0: from the accessor M.  Used by the tile kernel below
+// caller); otherwise from the accessor M.  Used by the tile kernel below
 // (grid-stride over tiles) and by the packed-batch kernel (one CTA walks all
 // tiles of a trajectory's gate).
-template <int K, bool PAIR, int MODE, int SMAT, int STAGES, class MA>
+template <int K, bool PAIR, int MODE, bool SMAT, int STAGES, class MA>
 __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
                                           const TileGeom& g, const MA& M,
                                           const float2* smat, float4* tile,
@@ -277,56 +254,7 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
       for (int j = 0; j < NACC; ++j) acc[r][j] = 0.f;
 
     if (active) {
-      if constexpr (SMAT == 2) {
-        // Entry (r, c) at float4 index c * D + r; this thread's rows
-        // rb*R .. rb*R+R-1 of column c are contiguous.
-        const float4* mbase = reinterpret_cast<const float4*>(smat) + rb * R;
-        if constexpr (PAIR) {
-          float2 a0[R], a1[R];
-#pragma unroll
-          for (int r = 0; r < R; ++r) a0[r] = a1[r] = make_float2(0.f, 0.f);
-#pragma unroll 2
-          for (int c = 0; c < D; ++c) {
-            const float4 v = cur[((e | g.moff[c]) >> 1) ^ swe];
-            const float2 v0 = make_float2(v.x, v.y), v1 = make_float2(v.z, v.w);
-            const float4* mc = mbase + c * D;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              const float4 mm = mc[r];
-              cmac2(a0[r], mm, v0);
-              cmac2(a1[r], mm, v1);
-            }
-          }
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            acc[r][0] = a0[r].x;
-            acc[r][1] = a0[r].y;
-            acc[r][2] = a1[r].x;
-            acc[r][3] = a1[r].y;
-          }
-        } else {
-          float2 a0[R];
-#pragma unroll
-          for (int r = 0; r < R; ++r) a0[r] = make_float2(0.f, 0.f);
-#pragma unroll 2
-          for (int p = 0; p < D / 2; ++p) {
-            const float4 v = cur[((e | g.moff[2 * p]) >> 1) ^ swe];
-            const float2 v0 = make_float2(v.x, v.y), v1 = make_float2(v.z, v.w);
-            const float4* mc0 = mbase + (2 * p) * D;
-            const float4* mc1 = mbase + (2 * p + 1) * D;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              cmac2(a0[r], mc0[r], v0);
-              cmac2(a0[r], mc1[r], v1);
-            }
-          }
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            acc[r][0] = a0[r].x;
-            acc[r][1] = a0[r].y;
-          }
-        }
-      } else if constexpr (SMAT == 1) {
+      if constexpr (SMAT) {
         // Rows rb*R .. rb*R+R-1 of column c are contiguous in smat.
         const float4* mbase = reinterpret_cast<const float4*>(smat + rb * R);
         if constexpr (PAIR) {
@@ -461,16 +389,7 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
   constexpr int D = SH::D;
   extern __shared__ float4 smem[];
   float2* smat = reinterpret_cast<float2*>(smem + SH::STAGES * SH::UNITS);
-  if constexpr (SH::SMAT_MODE == 2) {
-    // Column-major packed pairs: entry (r, c) at float4 c * D + r.
-    float4* smat4 = reinterpret_cast<float4*>(smat);
-    for (int i = threadIdx.x; i < D * D; i += kTileThreads) {
-      const int r = i / D, c = i % D;
-      const float re = a.m[2 * i], im = a.m[2 * i + 1];
-      smat4[c * D + r] = make_float4(re, re, -im, im);
-    }
-    __syncthreads();
-  } else if constexpr (SH::SMAT_MODE == 1) {
+  if constexpr (SH::SMEM_MAT) {
     // Column-major copy: smat[c * D + r] = M[r][c].
     for (int i = threadIdx.x; i < D * D; i += kTileThreads) {
       const int r = i / D, c = i % D;
@@ -483,7 +402,7 @@ __global__ void __launch_bounds__(kTileThreads, K <= 3 ? 4 : 5)
     __syncthreads();
   }
   double er = 0, ei = 0;
-  tile_pass<K, PAIR, MODE, SH::SMAT_MODE, SH::STAGES>(
+  tile_pass<K, PAIR, MODE, SH::SMEM_MAT, SH::STAGES>(
       st, a.g, MatAccess<K>{a}, smat, smem, blockIdx.x, gridDim.x, er, ei);
 
   if constexpr (MODE == 1) {

@@ -855,12 +855,12 @@ int qsg_find_measured_bits(qsg_ctx* ctx, const float* state, unsigned n,
   return QSG_OK;
 }
 
-int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
-                      uint64_t num_samples, const double* sorted_u,
-                      uint64_t* out_bitstrings) {
-  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_sample_sorted");
-  if (num_samples == 0) return QSG_OK;
-  QSG_CHECK_ARG(sorted_u && out_bitstrings, "qsg_sample_sorted: null");
+// Samples for sorted values `vals`: uniforms in [0,1) scaled on the device
+// by the CDF total (scaled), or thresholds on the running sum of |s|^2.
+static int sample_impl(qsg_ctx* ctx, const float* state, unsigned n,
+                       uint64_t num_samples, const double* vals, bool scaled,
+                       uint64_t* out_bitstrings) {
+  const double* sorted_u = vals;
   const uint64_t nc = num_chunks(n);
   const uint32_t cb = chunk_bits(n);
   const size_t ubytes = num_samples * sizeof(double);
@@ -874,11 +874,16 @@ int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
   double* dr = du + num_samples;
   uint64_t* dout = reinterpret_cast<uint64_t*>(dr + num_samples);
   uint32_t* dchunk = reinterpret_cast<uint32_t*>(dout + num_samples);
-  QSG_CUDA(cudaMemcpyAsync(du, sorted_u, ubytes, cudaMemcpyHostToDevice,
-                           ctx->stream));
-  scale_uniforms_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
-                          ctx->stream>>>(du, num_samples, incl, nc, dr);
-  QSG_LAUNCHED(ctx);
+  if (scaled) {
+    QSG_CUDA(cudaMemcpyAsync(du, sorted_u, ubytes, cudaMemcpyHostToDevice,
+                             ctx->stream));
+    scale_uniforms_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
+                            ctx->stream>>>(du, num_samples, incl, nc, dr);
+    QSG_LAUNCHED(ctx);
+  } else {
+    QSG_CUDA(cudaMemcpyAsync(dr, sorted_u, ubytes, cudaMemcpyHostToDevice,
+                             ctx->stream));
+  }
   sample_locate_kernel<<<grid_for(ctx, num_samples, 256), 256, 0,
                          ctx->stream>>>(incl, nc, dr, num_samples, dchunk);
   QSG_LAUNCHED(ctx);
@@ -891,6 +896,26 @@ int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
                            cudaMemcpyDeviceToHost, ctx->stream));
   QSG_CUDA(cudaStreamSynchronize(ctx->stream));
   return QSG_OK;
+}
+
+int qsg_sample_sorted(qsg_ctx* ctx, const float* state, unsigned n,
+                      uint64_t num_samples, const double* sorted_u,
+                      uint64_t* out_bitstrings) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_sample_sorted");
+  if (num_samples == 0) return QSG_OK;
+  QSG_CHECK_ARG(sorted_u && out_bitstrings, "qsg_sample_sorted: null");
+  return sample_impl(ctx, state, n, num_samples, sorted_u, true,
+                     out_bitstrings);
+}
+
+int qsg_sample_thresholds(qsg_ctx* ctx, const float* state, unsigned n,
+                          uint64_t num_samples, const double* sorted_r,
+                          uint64_t* out_bitstrings) {
+  QSG_CHECK_ARG(ctx && state && n <= kMaxQubits, "qsg_sample_thresholds");
+  if (num_samples == 0) return QSG_OK;
+  QSG_CHECK_ARG(sorted_r && out_bitstrings, "qsg_sample_thresholds: null");
+  return sample_impl(ctx, state, n, num_samples, sorted_r, false,
+                     out_bitstrings);
 }
 
 int qsg_sample(qsg_ctx* ctx, const float* state, unsigned n,

@@ -3,9 +3,11 @@
 // qsim_gb300::SimulatorGB300 / StateSpaceGB300, then measures and samples.
 //
 // Usage: adapter_run <gates.txt> <out-prefix> <measure-seed> <q...>
-// Writes <out>.state (complex64 after the gates), <out>.bits (one
-// Measure(qubits, std::mt19937(seed))), <out>.after (state after it) and
-// <out>.samples (1000 samples, seed 7).
+// Writes <out>.state (complex64 after the gates), <out>.normal and
+// <out>.internal (the state after InternalToNormalOrder, then after
+// NormalToInternalOrder), <out>.bits (one Measure(qubits,
+// std::mt19937(seed))), <out>.after (state after it), <out>.samples (1000
+// samples, seed 7) and <out>.samples_f32 (the same with Sample<float>).
 
 #include <cstdio>
 #include <cstdlib>
@@ -68,9 +70,20 @@ int main(int argc, char** argv) {
     std::fclose(f);
   };
   dump(".state");
+  // The internal order is the normal order: both conversions leave the
+  // state as it is.
+  ss.InternalToNormalOrder(state);
+  dump(".normal");
+  ss.NormalToInternalOrder(state);
+  dump(".internal");
   auto samples = ss.Sample(state, 1000, 7);
   FILE* f = std::fopen((out + ".samples").c_str(), "wb");
   std::fwrite(samples.data(), sizeof(uint64_t), samples.size(), f);
+  std::fclose(f);
+  // Sample<float>: uniforms drawn with uniform_real_distribution<float>.
+  auto samples32 = ss.Sample<float>(state, 1000, 7);
+  f = std::fopen((out + ".samples_f32").c_str(), "wb");
+  std::fwrite(samples32.data(), sizeof(uint64_t), samples32.size(), f);
   std::fclose(f);
   std::vector<unsigned> mq;
   for (int i = 4; i < argc; ++i) mq.push_back(std::atoi(argv[i]));

@@ -338,6 +338,7 @@ def mt_case():
             subprocess.run([DRIVER, "mt", str(seed), "2000", p], check=True)
             out[f"raw_{seed}"] = np.fromfile(p + ".raw", np.uint32)
             out[f"u01_{seed}"] = np.fromfile(p + ".u01", np.float64)
+            out[f"f073_{seed}"] = np.fromfile(p + ".f073", np.float32)
         np.savez_compressed(os.path.join(HERE, "mt19937.npz"), **out)
         print("mt19937 written")
 
@@ -964,6 +965,9 @@ def main():
         return
     if sys.argv[1:] == ["pybind"]:
         pybind_cases()
+        return
+    if sys.argv[1:] == ["mt"]:
+        mt_case()
         return
     if sys.argv[1:] == ["refplan"]:
         ref_plan_case()

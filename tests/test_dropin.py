@@ -101,3 +101,30 @@ def test_adapter_program_matches_reference(tmp_path, oracle):
     samples = np.fromfile(out + ".samples", np.uint64)
     want = oracle.sample(state.astype(np.complex128), n, 1000, 7)
     assert np.mean(samples == want) >= 0.999
+    # InternalToNormalOrder / NormalToInternalOrder: the internal order is
+    # the normal order (lib/statespace_cuda.h:85-107 transposes the
+    # reference's 32/32 blocks), so both leave the amplitudes in place.
+    for ext in (".normal", ".internal"):
+        assert np.array_equal(np.fromfile(out + ext, np.float32).view(np.complex64),
+                              state)
+    # Sample<float>: draws of uniform_real_distribution<float>(0, norm).
+    import ctypes as C
+    s128 = state.astype(np.complex128)
+    rs = np.zeros(1000, np.float32)
+    oracle.L.orc_generate_random_values_f32.argtypes = [
+        C.c_uint64, C.c_uint32, C.c_float, C.POINTER(C.c_float)]
+    oracle.L.orc_generate_random_values_f32(
+        1000, 7, np.float32(np.vdot(s128, s128).real),
+        rs.ctypes.data_as(C.POINTER(C.c_float)))
+    r64 = rs.astype(np.float64)
+    want32 = np.zeros(1000, np.uint64)
+    oracle.L.orc_sample_thresholds_f64.argtypes = [
+        C.POINTER(C.c_double), C.c_uint, C.c_uint64, C.POINTER(C.c_double),
+        C.POINTER(C.c_uint64)]
+    oracle.L.orc_sample_thresholds_f64(
+        s128.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)), n, 1000,
+        r64.ctypes.data_as(C.POINTER(C.c_double)),
+        want32.ctypes.data_as(C.POINTER(C.c_uint64)))
+    samples32 = np.fromfile(out + ".samples_f32", np.uint64)
+    assert np.mean(samples32 == want32) >= 0.999
+    assert not np.array_equal(samples32, samples)   # float draws differ

@@ -20,6 +20,20 @@ def test_mt19937_and_canonical(oracle):
         assert np.array_equal(u, d[f"u01_{seed}"])
 
 
+def test_float_uniforms_match_libstdcxx(oracle):
+    """GenerateRandomValues<float> (lib/util.h:67-85), the draws of
+    Sample<float>: uniform_real_distribution<float>(0, 0.73) from
+    mt19937(seed), sorted, bit-identical to the reference's build."""
+    import ctypes as C
+    d = load_golden("mt19937")
+    f = oracle.L.orc_generate_random_values_f32
+    f.argtypes = [C.c_uint64, C.c_uint32, C.c_float, C.POINTER(C.c_float)]
+    for seed in (0, 1, 5489, 123456789, 4294967295):
+        out = np.zeros(2000, np.float32)
+        f(2000, seed, np.float32(0.73), out.ctypes.data_as(C.POINTER(C.c_float)))
+        assert np.array_equal(out, np.sort(d[f"f073_{seed}"]))
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_oracle_state_matches_reference_fp64(oracle, case):
     """Unfused FP64 application equals SimulatorBasic<For,double>."""
