@@ -417,7 +417,13 @@ enum {
   QSG_CHANNEL_PHASE_DAMPING = 2,     /* :313-345, gamma                     */
   QSG_CHANNEL_BIT_FLIP = 3,          /* :425-447, p                         */
   QSG_CHANNEL_PHASE_FLIP = 4,        /* :393-415, p                         */
-  QSG_CHANNEL_RESET = 5              /* :359-380                            */
+  QSG_CHANNEL_RESET = 5,             /* :359-380                            */
+  /* Depolarizing on k <= 3 qubits as the reference's multi-qubit factory
+   * builds it (:147-189): the Pauli of index digit j acts on register qubit
+   * j, not on the channel's j-th qubit (the same as kind 0 when the channel
+   * acts on qubits 0..k-1).  For trajectories identical to the reference's
+   * on circuits that use that factory. */
+  QSG_CHANNEL_DEPOLARIZING_REGISTER = 6
 };
 typedef struct qsg_noisy qsg_noisy;
 int qsg_noisy_create(unsigned num_qubits, qsg_noisy** out);

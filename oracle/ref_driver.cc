@@ -42,6 +42,8 @@
 //         D|A|P|B|F <time> <q> <param>   depolarizing, amplitude damping,
 //                                        phase damping, bit flip, phase flip
 //         R <time> <q>                   reset
+//         Q <time> <k> <q...> <p>        depolarizing on k qubits (the
+//                                        reference's multi-qubit factory)
 //       Runs QuantumTrajectorySimulator::RunBatch over repetitions [r0, r1)
 //       with QSimRunner + MultiQubitGateFuser, collect_kop_stat and
 //       collect_mea_stat on, in float (host SIMD simulator) and in double
@@ -114,7 +116,8 @@ struct GateSpec {
 };
 
 static bool IsChannel(char k) {
-  return k == 'D' || k == 'A' || k == 'P' || k == 'B' || k == 'F' || k == 'R';
+  return k == 'D' || k == 'A' || k == 'P' || k == 'B' || k == 'F' || k == 'R' ||
+         k == 'Q';
 }
 
 static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
@@ -131,6 +134,18 @@ static std::vector<GateSpec> ReadGates(const char* path, unsigned& n) {
     }
     GateSpec g;
     g.kind = tag[0];
+    if (g.kind == 'Q') {
+      // Q <time> <k> <q...> <p>: multi-qubit depolarizing channel.
+      unsigned k;
+      ss >> g.time >> k;
+      g.qs.resize(k);
+      for (auto& q : g.qs) ss >> q;
+      std::string t;
+      ss >> t;
+      g.param = std::strtod(t.c_str(), nullptr);
+      out.push_back(std::move(g));
+      continue;
+    }
     if (IsChannel(g.kind)) {
       g.qs.resize(1);
       ss >> g.time >> g.qs[0];
@@ -174,6 +189,8 @@ static Operation<FP> ToOp(const GateSpec& g) {
   switch (g.kind) {
     case 'D':
       return Cirq::DepolarizingChannel<FP>::Create(g.time, q, g.param);
+    case 'Q':
+      return Cirq::DepolarizingChannel<FP>::Create(g.time, g.qs, g.param);
     case 'A':
       return Cirq::AmplitudeDampingChannel<FP>::Create(g.time, q, g.param);
     case 'P':

@@ -39,12 +39,29 @@ def _f32(x):
     return float(np.float32(x))
 
 
-def channel_kops(code: int, q: int, p: float, fp32: bool = True):
+def channel_kops(code: int, q: int, p: float, fp32: bool = True, qs=None):
     """Kraus operators of a one-qubit channel of lib/channels_cirq.h as
     (unitary, prob, [(qubits, matrix)], kd_k diagonal or None).  With fp32,
     matrix and kd_k entries hold the single-precision values of the
-    reference's float channels, else those of its double channels."""
+    reference's float channels, else those of its double channels.  Code 6:
+    the reference's multi-qubit depolarizing factory on the channel qubits
+    `qs` (:147-189), whose Pauli of index digit j acts on register qubit j."""
     rnd = np.float32 if fp32 else np.float64
+    if code == 6:
+        k = len(qs)
+        p1, p2 = 1 - p, p / 3
+        out = []
+        for i in range(4 ** k):
+            prob, ops = 1.0, []
+            for j in range(k):
+                pauli = (i >> (2 * j)) & 3
+                if pauli == 0:
+                    prob *= p1
+                else:
+                    prob *= p2
+                    ops.append(([j], (PX, PY, PZ)[pauli - 1]))
+            out.append((True, prob, ops, None))
+        return out
     if code == 0:  # depolarizing, :127-199
         p1, p2 = 1 - p, p / 3
         return [(True, p1, [], None), (True, p2, [([q], PX)], None),
@@ -108,7 +125,8 @@ def run_trajectory(orc, n: int, ops, rep: int,
                                           op["cvals"], op["m"])
             stats.append(0)
             continue
-        kops = channel_kops(op["channel"], op["q"], op["p"], fp32)
+        kops = channel_kops(op["channel"], op["q"], op["p"], fp32,
+                            op.get("qs"))
         cp = 0.0
         chosen = None
         for i, (uni, prob, kops_ops, _) in enumerate(kops):
@@ -147,9 +165,11 @@ def ops_from_fixture(d, unpack_ops):
     """The op list of a tests/golden/traj_*.npz fixture."""
     gates = iter(unpack_ops(d))
     ops = []
-    for code, q, p in zip(d["op_channel"], d["op_q"], d["op_p"]):
+    qmask = d["op_qmask"] if "op_qmask" in d else np.zeros(len(d["op_q"]))
+    for code, q, p, qm in zip(d["op_channel"], d["op_q"], d["op_p"], qmask):
         if code < 0:
             ops.append(next(gates))
         else:
-            ops.append(dict(channel=int(code), q=int(q), p=float(p)))
+            qs = [b for b in range(64) if (int(qm) >> b) & 1] or [int(q)]
+            ops.append(dict(channel=int(code), q=int(q), p=float(p), qs=qs))
     return ops

@@ -38,7 +38,6 @@ import numpy as np
 from traj_oracle import channel_kops
 
 P = C.POINTER
-_CODES = {"D": 0, "A": 1, "P": 2, "B": 3, "F": 4, "R": 5}
 
 
 def noisy_ops(clean_ops, n, p_depol, gamma, cycle_len=2):
@@ -129,7 +128,8 @@ class TrajectoryPort:
             if "channel" not in op:
                 self._defer(op["qs"], op["m"])
                 continue
-            kops = channel_kops(op["channel"], op["q"], op["p"], True)
+            kops = channel_kops(op["channel"], op["q"], op["p"], True,
+                                op.get("qs"))
             cp, chosen = 0.0, None
             for i, (uni, prob, _, _) in enumerate(kops):
                 cp += prob

@@ -255,10 +255,11 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
 
     if (active) {
       if constexpr (SMAT) {
-        // Rows rb*R .. rb*R+R-1 of column c are contiguous in smat.
+        // Rows rb*R .. rb*R+R-1 of column c are contiguous in smat.  Columns
+        // unrolled by 4 for k = 4 (3 % faster than 2 on GB300), by 2 above.
         const float4* mbase = reinterpret_cast<const float4*>(smat + rb * R);
         if constexpr (PAIR) {
-#pragma unroll 2
+#pragma unroll (K == 4 ? 4 : 2)
           for (int c = 0; c < D; ++c) {
             const float4 v = cur[((e | g.moff[c]) >> 1) ^ swe];
             const float4* mc = mbase + c * (D / 2);
@@ -274,7 +275,7 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
             }
           }
         } else {
-#pragma unroll 2
+#pragma unroll (K == 4 ? 4 : 2)
           for (int p = 0; p < D / 2; ++p) {
             const float4 v = cur[((e | g.moff[2 * p]) >> 1) ^ swe];
             const float4* mc0 = mbase + (2 * p) * (D / 2);

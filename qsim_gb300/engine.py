@@ -351,6 +351,9 @@ class Plan:
 
 CHANNEL_DEPOLARIZING, CHANNEL_AMPLITUDE_DAMPING, CHANNEL_PHASE_DAMPING = 0, 1, 2
 CHANNEL_BIT_FLIP, CHANNEL_PHASE_FLIP, CHANNEL_RESET = 3, 4, 5
+# The reference's multi-qubit depolarizing factory: Pauli of digit j on
+# register qubit j (lib/channels_cirq.h:147-189).
+CHANNEL_DEPOLARIZING_REGISTER = 6
 NO_STAT = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 

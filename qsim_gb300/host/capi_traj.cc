@@ -88,7 +88,8 @@ int qsg_noisy_add_channel(qsg_noisy* h, int kind, unsigned time,
   if (!distinct_lt(qs, nq, h->nc.num_qubits)) return invalid("bad qubits");
   std::vector<unsigned> q(qs, qs + nq);
   std::sort(q.begin(), q.end());
-  if (kind != QSG_CHANNEL_DEPOLARIZING && nq != 1)
+  if (kind != QSG_CHANNEL_DEPOLARIZING &&
+      kind != QSG_CHANNEL_DEPOLARIZING_REGISTER && nq != 1)
     return invalid("this channel acts on one qubit");
   if (kind != QSG_CHANNEL_RESET && !(p >= 0 && p <= 1))
     return invalid("channel parameter must lie in [0, 1]");
@@ -96,6 +97,11 @@ int qsg_noisy_add_channel(qsg_noisy* h, int kind, unsigned time,
     case QSG_CHANNEL_DEPOLARIZING:
       if (nq > 3) return invalid("depolarizing channels on at most 3 qubits");
       h->nc.ops.push_back(depolarizing_channel(time, q, p));
+      break;
+    case QSG_CHANNEL_DEPOLARIZING_REGISTER:
+      if (nq > 3) return invalid("depolarizing channels on at most 3 qubits");
+      if (nq > h->nc.num_qubits) return invalid("more channel qubits than qubits");
+      h->nc.ops.push_back(depolarizing_channel(time, q, p, true));
       break;
     case QSG_CHANNEL_AMPLITUDE_DAMPING:
       h->nc.ops.push_back(amplitude_damping_channel(time, q[0], p));

@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <future>
+#include <utility>
+#include <vector>
 #include <cstring>
 
 #include "engine.h"
@@ -432,24 +434,42 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
   // also with a 3-gate seed window), each block on its predicted-faster
   // path; the plan of lowest predicted total time wins.
   // The fixed-size plans of the gate-count rule are among the candidates.
-  Plan best;
-  double best_t = 0;
-  bool have = false;
+  // The candidates are independent: each runs on a host thread of its own
+  // (futures), and the lowest predicted time wins, the first in candidate
+  // order on ties, so the result does not depend on the threads.
+  struct Cand {
+    unsigned ff, w;
+    int pg;
+  };
+  std::vector<Cand> cands;
   for (unsigned ff = 1; ff <= f; ++ff) {
     for (int pg = 0; pg < 2; ++pg) {
       if (ff == 1 && pg) continue;
       for (unsigned w : {opt.seeds, 3u}) {
         if (w == 3u && (opt.seeds == 3u || ff < 5)) continue;
-        FuseOptions o = opt;
-        o.seeds = w;
-        Plan p = fuse_greedy(c, o, ff, pg != 0);
-        const double t = plan_cost(c, p, *opt.cost);
-        if (!have || t < best_t) {
-          best = std::move(p);
-          best_t = t;
-          have = true;
-        }
+        cands.push_back({ff, w, pg});
       }
+    }
+  }
+  std::vector<std::future<std::pair<Plan, double>>> runs;
+  for (const Cand& cd : cands) {
+    runs.push_back(std::async(std::launch::async, [&c, &opt, cd] {
+      FuseOptions o = opt;
+      o.seeds = cd.w;
+      Plan p = fuse_greedy(c, o, cd.ff, cd.pg != 0);
+      const double t = plan_cost(c, p, *opt.cost);
+      return std::make_pair(std::move(p), t);
+    }));
+  }
+  Plan best;
+  double best_t = 0;
+  bool have = false;
+  for (auto& r : runs) {
+    auto pt = r.get();
+    if (!have || pt.second < best_t) {
+      best = std::move(pt.first);
+      best_t = pt.second;
+      have = true;
     }
   }
   return best;

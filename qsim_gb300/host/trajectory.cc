@@ -95,8 +95,11 @@ void compute_kdk(KrausOp& k) {
 }
 
 NoisyOp depolarizing_channel(unsigned time, const std::vector<unsigned>& qs,
-                             double p) {
-  // lib/channels_cirq.h:127-199; the Pauli of index digit j acts on qs[j].
+                             double p, bool register_qubits) {
+  // lib/channels_cirq.h:127-199; the Pauli of index digit j acts on qs[j],
+  // or, with register_qubits, on register qubit j as the reference's
+  // multi-qubit factory places it (:147-189).  The channel then occupies
+  // qubits 0..k-1, where its operators act.
   const double p1 = 1 - p, p2 = p / 3;
   const unsigned nq = qs.size();
   std::vector<KrausOp> kops;
@@ -113,10 +116,15 @@ NoisyOp depolarizing_channel(unsigned time, const std::vector<unsigned>& qs,
       }
       prob *= p2;
       const Mat& m = pauli == 1 ? kPauliX : pauli == 2 ? kPauliY : kPauliZ;
-      k.ops.push_back(gate_on(time, {qs[j]}, m));
+      k.ops.push_back(gate_on(time, {register_qubits ? j : qs[j]}, m));
     }
     k.prob = prob;
     kops.push_back(std::move(k));
+  }
+  if (register_qubits) {
+    std::vector<unsigned> acted(nq);
+    for (unsigned j = 0; j < nq; ++j) acted[j] = j;
+    return channel_of(time, acted, std::move(kops));
   }
   return channel_of(time, qs, std::move(kops));
 }

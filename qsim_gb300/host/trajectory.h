@@ -61,7 +61,7 @@ struct NoisyCircuit {
 // Channels of lib/channels_cirq.h.  Matrices hold the single-precision
 // values the reference's float channels hold.
 NoisyOp depolarizing_channel(unsigned time, const std::vector<unsigned>& qs,
-                             double p);
+                             double p, bool register_qubits = false);
 NoisyOp amplitude_damping_channel(unsigned time, unsigned q, double gamma);
 NoisyOp phase_damping_channel(unsigned time, unsigned q, double gamma);
 NoisyOp bit_flip_channel(unsigned time, unsigned q, double p);

@@ -102,6 +102,8 @@ def write_gate_list(path, n, ops):
                 f.write(f"m {o['time']} {k} {q}\n")
             elif o["kind"] == "R":
                 f.write(f"R {o['time']} {q}\n")
+            elif o["kind"] == "Q":
+                f.write(f"Q {o['time']} {k} {q} {float(o['p']).hex()}\n")
             else:  # one-qubit channel with one parameter
                 f.write(f"{o['kind']} {o['time']} {q} {float(o['p']).hex()}\n")
 
@@ -343,7 +345,7 @@ def mt_case():
         print("mt19937 written")
 
 
-CHANNEL_CODES = {"D": 0, "A": 1, "P": 2, "B": 3, "F": 4, "R": 5}
+CHANNEL_CODES = {"D": 0, "A": 1, "P": 2, "B": 3, "F": 4, "R": 5, "Q": 6}
 
 
 def noisy_chain_ops(n, cycles, seed, p_depol, gamma, cycle_len=2):
@@ -410,6 +412,9 @@ def pack_noisy(ops):
     data["op_q"] = np.array([o["qs"][0] if o["kind"] in CHANNEL_CODES else -1
                              for o in ops], np.int32)
     data["op_p"] = np.array([o.get("p", 0.0) for o in ops], np.float64)
+    data["op_qmask"] = np.array(
+        [sum(1 << q for q in o["qs"]) if o["kind"] in CHANNEL_CODES else 0
+         for o in ops], np.int64)
     return data
 
 
@@ -444,6 +449,24 @@ def traj_case(name, n, ops, fsize, r0, r1, states_c64=False):
         print(name, "written")
 
 
+def depol_register_ops(rng, n, layers):
+    """Random one- and two-qubit gates with two-qubit depolarizing channels
+    (p = 0.3) on qubit pairs away from qubits 0 and 1, through the
+    reference's multi-qubit factory, whose Pauli of digit j acts on
+    register qubit j (lib/channels_cirq.h:147-189)."""
+    ops, t = [], 0
+    for layer in range(layers):
+        for q in range(n):
+            ops.append(dict(kind="g", time=t, qs=[q], m=random_unitary(rng, 1)))
+        for q in range(layer % 2, n - 1, 2):
+            ops.append(dict(kind="g", time=t + 1, qs=[q, q + 1],
+                            m=random_unitary(rng, 2)))
+        qs = sorted(rng.choice(np.arange(2, n), size=2, replace=False).tolist())
+        ops.append(dict(kind="Q", time=t + 2, qs=qs, p=0.3))
+        t += 3
+    return ops
+
+
 def traj_cases():
     traj_case("traj_depol8", 8, noisy_chain_ops(8, 4, 3, 0.05, 0.0), 2, 0, 48)
     traj_case("traj_ad8", 8, noisy_chain_ops(8, 4, 4, 0.02, 0.1), 3, 0, 48)
@@ -452,6 +475,12 @@ def traj_cases():
     # The batched-trajectory workload's noise model at n = 12, depth 12.
     traj_case("traj_chain12", 12, noisy_chain_ops(12, 12, 5, 1e-3, 5e-3), 4,
               0, 8, states_c64=True)
+    traj_depol_register_case()
+
+
+def traj_depol_register_case():
+    rng = np.random.default_rng(123)
+    traj_case("traj_depol2q_reg", 6, depol_register_ops(rng, 6, 5), 2, 0, 40)
 
 
 def unitary_case(name, n, ops):
@@ -959,6 +988,9 @@ def main():
         sys.exit(f"{DRIVER} missing: run `make -C oracle ref` first")
     if sys.argv[1:] == ["traj"]:
         traj_cases()
+        return
+    if sys.argv[1:] == ["traj_depol_register"]:
+        traj_depol_register_case()
         return
     if sys.argv[1:] == ["unitary"]:
         unitary_cases()

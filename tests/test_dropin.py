@@ -17,7 +17,8 @@ import pytest
 from conftest import ROOT, load_golden, rel_l2, unpack_ops
 
 LIBDIR = os.path.join(ROOT, "qsim_gb300", "_build")
-REF = os.environ.get("QSG_REFERENCE", "/root/reference")
+REF = os.environ.get("QSG_REFERENCE",
+                     os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def compile_prog(src, out, extra=()):

@@ -20,11 +20,12 @@ import traj_oracle  # noqa: E402
 
 from qsim_gb300 import engine as E  # noqa: E402
 
-CASES = ["traj_depol8", "traj_ad8", "traj_mixed6", "traj_chain12"]
+CASES = ["traj_depol8", "traj_ad8", "traj_mixed6", "traj_chain12",
+         "traj_depol2q_reg"]
 # Fraction of repetitions whose choices must agree: all of them when every
 # channel is unitary, nearly all when a choice can depend on round-off.
 MIN_AGREE = {"traj_depol8": 1.0, "traj_ad8": 0.95, "traj_mixed6": 0.95,
-             "traj_chain12": 1.0}
+             "traj_chain12": 1.0, "traj_depol2q_reg": 1.0}
 STATE_TOL = 1e-5
 
 
@@ -39,7 +40,10 @@ def build_noisy(d):
     n = int(d["n"])
     nc = E.NoisyCircuit(n)
     gates = iter(unpack_ops(d))
-    for code, t, q, p in zip(d["op_channel"], d["op_time"], d["op_q"], d["op_p"]):
+    qmask = d["op_qmask"] if "op_qmask" in d else np.zeros(len(d["op_q"]))
+    for code, t, q, p, qm in zip(d["op_channel"], d["op_time"], d["op_q"],
+                                 d["op_p"], qmask):
+        qs = [b for b in range(64) if (int(qm) >> b) & 1] or [int(q)]
         if code < 0:
             o = next(gates)
             if o["kind"] == 0:
@@ -49,7 +53,7 @@ def build_noisy(d):
             else:
                 nc.add_measurement(int(t), o["qs"])
         else:
-            nc.add_channel(int(code), int(t), [int(q)], float(p))
+            nc.add_channel(int(code), int(t), qs, float(p))
     return nc
 
 
