@@ -394,6 +394,86 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
 
 }  // namespace
 
+// A controlled op as a plain gate on its targets and controls (sorted):
+// the identity except on the rows and columns whose control bits equal
+// cvals, where the target matrix acts.  Same op index, so block members
+// still name circuit ops.
+namespace {
+
+Op expand_controlled_op(const Op& op) {
+  Op e;
+  e.kind = OpKind::kGate;
+  e.time = op.time;
+  e.qs = op.qs;
+  e.qs.insert(e.qs.end(), op.cqs.begin(), op.cqs.end());
+  std::sort(e.qs.begin(), e.qs.end());
+  const unsigned k = op.qs.size(), nc = op.cqs.size(), u = e.qs.size();
+  auto pos = [&](unsigned q) {
+    return unsigned(std::find(e.qs.begin(), e.qs.end(), q) - e.qs.begin());
+  };
+  unsigned tpos[6], cpos[6];
+  for (unsigned j = 0; j < k; ++j) tpos[j] = pos(op.qs[j]);
+  for (unsigned i = 0; i < nc; ++i) cpos[i] = pos(op.cqs[i]);
+  const unsigned d = 1u << u, dk = 1u << k;
+  auto tidx = [&](unsigned x) {
+    unsigned t = 0;
+    for (unsigned j = 0; j < k; ++j) t |= ((x >> tpos[j]) & 1u) << j;
+    return t;
+  };
+  auto cval = [&](unsigned x) {
+    uint64_t v = 0;
+    for (unsigned i = 0; i < nc; ++i) v |= uint64_t((x >> cpos[i]) & 1u) << i;
+    return v;
+  };
+  e.m.assign(size_t(d) * d, 0.0);
+  for (unsigned r = 0; r < d; ++r) {
+    for (unsigned col = 0; col < d; ++col) {
+      if (cval(r) != cval(col)) continue;
+      const unsigned tr = tidx(r), tc = tidx(col);
+      if (cval(r) == op.cvals) {
+        e.m[size_t(r) * d + col] = op.m[size_t(tr) * dk + tc];
+      } else if (tr == tc) {
+        e.m[size_t(r) * d + col] = 1.0;
+      }
+    }
+  }
+  return e;
+}
+
+// The circuit with every controlled op on at most f qubits (targets and
+// controls) expanded to a plain gate; op indices unchanged.
+Circuit expand_controlled(const Circuit& c, unsigned f) {
+  Circuit e = c;
+  for (auto& op : e.ops)
+    if (op.kind == OpKind::kControlled && op.qs.size() + op.cqs.size() <= f)
+      op = expand_controlled_op(op);
+  return e;
+}
+
+// A plan of the expanded circuit with every block that holds one expanded
+// controlled op alone turned back into that controlled op (a controlled
+// pass touches only the amplitudes its controls select).
+Plan restore_lone_controlled(const Circuit& c, Plan p) {
+  for (auto& po : p.ops) {
+    if (po.kind != OpKind::kGate || po.members.size() != 1) continue;
+    const Op& op = c.ops[po.members[0]];
+    if (op.kind != OpKind::kControlled) continue;
+    PlanOp r;
+    r.kind = op.kind;
+    r.time = op.time;
+    r.qs = op.qs;
+    r.cqs = op.cqs;
+    r.cvals = op.cvals;
+    r.m = op.m;
+    r.members = po.members;
+    finish(c, r);
+    po = std::move(r);
+  }
+  return p;
+}
+
+}  // namespace
+
 // Seed windows tried by the multi-start search: the greedy rule is not
 // monotonic in the window (on the 30-qubit depth-20 grid circuit at f = 6,
 // windows of 3 and 4 gates give 36 blocks, 12 gives 37, 5 gives 41).
@@ -434,29 +514,45 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
   // also with a 3-gate seed window), each block on its predicted-faster
   // path; the plan of lowest predicted total time wins.
   // The fixed-size plans of the gate-count rule are among the candidates.
+  // Circuits with controlled ops also get candidates in which those ops are
+  // plain gates on targets and controls that blocks may absorb (the
+  // reference's fuser always passes them through unfused), each lone one
+  // turned back into a controlled pass; the predicted times decide.
+  //
   // The candidates are independent: each runs on a host thread of its own
   // (futures), and the lowest predicted time wins, the first in candidate
   // order on ties, so the result does not depend on the threads.
+  bool has_controlled = false;
+  for (const auto& op : c.ops) has_controlled |= op.kind == OpKind::kControlled;
+  std::vector<Circuit> expanded(f + 1);
+  if (has_controlled)
+    for (unsigned ff = 2; ff <= f; ++ff) expanded[ff] = expand_controlled(c, ff);
   struct Cand {
     unsigned ff, w;
     int pg;
+    bool expand;
   };
   std::vector<Cand> cands;
-  for (unsigned ff = 1; ff <= f; ++ff) {
-    for (int pg = 0; pg < 2; ++pg) {
-      if (ff == 1 && pg) continue;
-      for (unsigned w : {opt.seeds, 3u}) {
-        if (w == 3u && (opt.seeds == 3u || ff < 5)) continue;
-        cands.push_back({ff, w, pg});
+  for (int ex = 0; ex < (has_controlled ? 2 : 1); ++ex) {
+    for (unsigned ff = 1; ff <= f; ++ff) {
+      if (ex && ff < 2) continue;
+      for (int pg = 0; pg < 2; ++pg) {
+        if (ff == 1 && pg) continue;
+        for (unsigned w : {opt.seeds, 3u}) {
+          if (w == 3u && (opt.seeds == 3u || ff < 5)) continue;
+          cands.push_back({ff, w, pg, ex != 0});
+        }
       }
     }
   }
   std::vector<std::future<std::pair<Plan, double>>> runs;
   for (const Cand& cd : cands) {
-    runs.push_back(std::async(std::launch::async, [&c, &opt, cd] {
+    const Circuit& cc = cd.expand ? expanded[cd.ff] : c;
+    runs.push_back(std::async(std::launch::async, [&c, &cc, &opt, cd] {
       FuseOptions o = opt;
       o.seeds = cd.w;
-      Plan p = fuse_greedy(c, o, cd.ff, cd.pg != 0);
+      Plan p = fuse_greedy(cc, o, cd.ff, cd.pg != 0);
+      if (cd.expand) p = restore_lone_controlled(c, std::move(p));
       const double t = plan_cost(c, p, *opt.cost);
       return std::make_pair(std::move(p), t);
     }));

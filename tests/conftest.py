@@ -190,8 +190,8 @@ class Oracle:
                 self.apply_gate_lanes(s, n, o["qs"], o["m"])
             elif o["kind"] == 1:
                 flush(list(o["qs"]) + list(o["cqs"]))
-                self.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"],
-                                           o["m"])
+                qs, m = expand_controlled(o["qs"], o["cqs"], o["cvals"], o["m"])
+                self.apply_gate_lanes(s, n, qs, m)
             else:
                 flush(o.get("qs", ()))
         flush(sorted(pending))
@@ -205,6 +205,30 @@ class Oracle:
             elif o["kind"] == 1:
                 self.apply_controlled_gate(s, n, o["qs"], o["cqs"], o["cvals"], o["m"])
         return s
+
+
+def expand_controlled(qs, cqs, cvals, m):
+    """A controlled gate as a dense gate on sorted(qs + cqs): the identity
+    except where the control bits equal cvals (bit i <-> cqs[i],
+    lib/gate.h:37-70), where the target matrix acts (bit j <-> qs[j])."""
+    u = sorted(list(qs) + list(cqs))
+    pos = {q: i for i, q in enumerate(u)}
+    k, d = len(qs), 1 << len(u)
+    m = np.asarray(m, np.complex128)
+    x = np.arange(d)
+    tid = np.zeros(d, np.int64)
+    cv = np.zeros(d, np.int64)
+    for j, q in enumerate(qs):
+        tid |= ((x >> pos[q]) & 1) << j
+    for i, q in enumerate(cqs):
+        cv |= ((x >> pos[q]) & 1) << i
+    full = np.zeros((d, d), np.complex128)
+    same_c = cv[:, None] == cv[None, :]
+    on = same_c & (cv[:, None] == cvals)
+    full[on] = m[tid[:, None], tid[None, :]][on]
+    off = same_c & (cv[:, None] != cvals) & (tid[:, None] == tid[None, :])
+    full[off] = 1.0
+    return u, full
 
 
 @pytest.fixture(scope="session")

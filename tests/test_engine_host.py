@@ -199,3 +199,23 @@ def test_pauli_sum(E):
     for qs, letters, coeff in terms:
         assert 1 <= len(qs) <= 6 and qs == sorted(qs) and len(set(qs)) == len(qs)
         assert set(letters) <= set("XYZ") and -1 <= coeff <= 1
+
+
+def test_learned_plan_absorbs_controlled_gates_and_keeps_the_state(E, oracle):
+    """With the cost model, the planner may absorb controlled gates into
+    blocks (as dense gates on targets and controls); the plan still applies
+    the same circuit (FP64 oracle, unfused vs plan ops), and it has fewer
+    controlled passes and fewer passes than the fixed fuser at f = 6."""
+    from qsim_gb300 import learned as L
+    m = L.CostMLP.load()
+    c = E.Circuit.layered_u3(12, 8, 8, 5)
+    n = c.num_qubits
+    want = oracle.run_ops(n, c.ops())
+    fixed = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5)
+    learned = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=2,
+                     cost_model=m)
+    got = oracle_run_circuit(oracle, n, learned.ops())
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+    ctrl = lambda p: sum(1 for o in p.ops() if o["kind"] == 1)  # noqa: E731
+    assert ctrl(learned) < ctrl(fixed)
+    assert len(learned) < len(fixed)

@@ -177,3 +177,48 @@ def test_gpu_learned_plan_same_state_and_timed(ctx):
     print("plan times (ms):", {k: round(v, 3) for k, v in times.items()})
     assert times["learned"] <= 1.05 * best_fixed
     assert times["learned"] < times["f4"]
+
+
+@pytest.mark.gpu
+def test_gpu_learned_plan_gains_on_controlled_circuit(ctx, oracle):
+    """What the trained network gains over the method without it.  On the
+    layered U3 + CZ/CNOT circuit with 8 controlled U3 gates per layer (24
+    qubits, 20 layers), the fixed fusers pass controlled gates through
+    unfused (the reference's MultiQubitGateFuser does the same); the learned
+    planner may absorb them into blocks, and its predicted times choose the
+    candidate.  Its state equals the FP64 oracle's (relative L2 <= 1e-5,
+    fidelity >= 1 - 1e-6), and it is faster than every fixed plan by at
+    least 20 % (best of 5 runs each; run-to-run spread ~1 %)."""
+    import qsim_gb300 as q
+    ss = q.StateSpace(ctx=ctx)
+    m = L.CostMLP.load(WEIGHTS)
+    c = E.Circuit.layered_u3(24, 20, 8, 3)
+    n = c.num_qubits
+    want = oracle.run_ops_fp64_fused(n, c.ops())
+    st = ss.Create(n)
+    plans = {f"f{f}" + ("_tc" if tc else ""): E.Plan(c, max_fused_size=f,
+                                                     tensor_path=tc, tc_min_k=5)
+             for f in (4, 5, 6) for tc in (False, True) if tc or f < 6}
+    plans["learned"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                              tc_min_k=2, cost_model=m)
+    times = {}
+    for name, p in plans.items():
+        ss.SetStateZero(st)
+        p.run(ctx, st)
+        got = ss.to_numpy(st)
+        fid = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real *
+                                               np.vdot(want, want).real)
+        assert rel_l2(got, want) <= 1e-5, name
+        assert fid >= 1 - 1e-6, name
+        p.capture(ctx, st)
+        runs = []
+        for _ in range(5):
+            ss.SetStateZero(st)
+            ctx.timer_start()
+            p.replay(ctx)
+            runs.append(ctx.timer_stop())
+        times[name] = min(runs)
+    best_fixed = min(v for k, v in times.items() if k != "learned")
+    print("plan times (ms):", {k: round(v, 3) for k, v in times.items()},
+          "passes:", {k: len(p) for k, p in plans.items()})
+    assert times["learned"] * 1.2 <= best_fixed
