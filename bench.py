@@ -575,6 +575,13 @@ def run_engine(args, world, rank, local, dist):
                                 "latency_ms_p50": alt["latency_ms_p50"],
                                 "latency_ms_p99": alt["latency_ms_p99"],
                                 "gpu_launches": alt["gpu_launches"]}
+        # Every trajectory in the one persistent packed-batch kernel.
+        pk = bench_trajectories(args.traj_streams, 4, mode="packed",
+                                device=local)
+        traj["packed_only"] = {"value": pk["value"], "wall_s": pk["wall_s"],
+                               "latency_ms_p50": pk["latency_ms_p50"],
+                               "latency_ms_p99": pk["latency_ms_p99"],
+                               "gpu_launches": pk["gpu_launches"]}
         if rank == 0 and world == 1 and not args.no_cpu:
             traj["cpu_baseline"] = traj_cpu_baseline()
             traj["speedup_vs_cpu"] = (traj["value"]

@@ -283,6 +283,39 @@ def test_samples_exact_against_oracle_on_same_state(eng, oracle):
         assert np.all(np.diff(got.astype(np.int64)) >= 0)
 
 
+def test_samples_and_measure_with_two_level_prefix(eng, oracle):
+    """States of >= 26 qubits (more than 4096 chunks) take the two-level
+    chunk prefix: 2000 samples of a 27-qubit state against the oracle's FP64
+    CDF scan on the same amplitudes, and a measurement's index against the
+    oracle's search for the same uniform."""
+    import ctypes as C
+    from qsim_gb300 import _native as N
+    q, ss, sim = eng
+    n = 27
+    rng = np.random.default_rng(27)
+    st = ss.Create(n)
+    ss.SetStateUniform(st)
+    for _ in range(6):
+        k = int(rng.integers(1, 4))
+        qs = sorted(rng.choice(n, size=k, replace=False).tolist())
+        sim.ApplyGate(qs, mat32(random_unitary(rng, k)), st)
+    s = ss.to_numpy(st)
+    want = oracle.sample(s.copy(), n, 2000, 5)
+    got = np.array(ss.Sample(st, 2000, 5), np.uint64)
+    assert np.mean(got == want) >= 0.999
+    cdf = np.cumsum(np.abs(s) ** 2)
+    for u in (0.0, 0.3, 0.999999):
+        bits = C.c_uint64()
+        N.check(N.lib.qsg_measure(ss.ctx.h, st.get(), n, (1 << n) - 1, u, 0,
+                                  C.byref(bits)))
+        k = int(bits.value)
+        r = u * cdf[-1]
+        # k is the first index whose running sum exceeds r, up to the
+        # rounding of FP32 products in the FP64 sums.
+        assert cdf[k] >= r * (1 - 1e-9)
+        assert k == 0 or cdf[k - 1] <= r * (1 + 1e-9) + 1e-300
+
+
 def test_sample_edge_cases(eng):
     q, ss, sim = eng
     st = ss.Create(10)
