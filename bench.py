@@ -469,8 +469,13 @@ def run_engine(args, world, rank, local, dist):
     # Roofline of the dominant kernel of the headline plan: per-op CUDA-event
     # times; algorithmic bytes per launch = 16 * 2^n (one read + one write
     # of the state).
-    ss.SetStateZero(st)
-    prof = head.profile(ctx, st)
+    # Three profiled runs (CUDA events around every launch); per launch the
+    # median of the three.
+    runs = []
+    for _ in range(3):
+        ss.SetStateZero(st)
+        runs.append(np.asarray(head.profile(ctx, st), dtype=np.float64))
+    prof = np.median(np.stack(runs), axis=0)
     hops = head.ops()
     kern_of = lambda o: "tc_gate_kernel" if o["path"] == 1 else "gate_tile_kernel"
     per_kernel = {}

@@ -387,7 +387,8 @@ __global__ void __launch_bounds__(1024)
 // Two-level prefix for many chunks: the one-CTA kernel above reads every
 // chunk sum twice from one SM (33 us of a 230 us Sample at 27 qubits).
 // Level 1: the sum of each block of kPrefixBlock chunk sums (fixed-order
-// tree); level 2: chunk_prefix_kernel over the block sums; level 3: each
+// tree); level 2: a one-block scan of the block sums (chunk_prefix_kernel
+// beyond 1024 blocks); level 3: each
 // block's inclusive scan plus the inclusive sum of the blocks before it.
 // Every order is fixed, so the result does not vary between runs.
 constexpr int kPrefixBlock = 256;
@@ -410,13 +411,15 @@ __global__ void __launch_bounds__(kPrefixBlock)
   }
 }
 
-__global__ void __launch_bounds__(kPrefixBlock)
+// Any block size that is a multiple of 32 up to 1024; block_incl null: no
+// offset (a one-block scan of the block sums).
+__global__ void __launch_bounds__(1024)
     prefix_block_apply_kernel(const double* __restrict__ sums,
                               uint64_t nchunks,
                               const double* __restrict__ block_incl,
                               double* __restrict__ incl) {
-  __shared__ double ws[kPrefixBlock / 32];
-  const uint64_t i = blockIdx.x * uint64_t(kPrefixBlock) + threadIdx.x;
+  __shared__ double ws[32];
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   double x = i < nchunks ? sums[i] : 0.0;
   const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
 #pragma unroll
@@ -427,8 +430,8 @@ __global__ void __launch_bounds__(kPrefixBlock)
   if (lane == 31) ws[w] = x;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double acc = blockIdx.x == 0 ? 0.0 : block_incl[blockIdx.x - 1];
-    for (int k = 0; k < kPrefixBlock / 32; ++k) {
+    double acc = (blockIdx.x == 0 || !block_incl) ? 0.0 : block_incl[blockIdx.x - 1];
+    for (int k = 0; k < int(blockDim.x / 32); ++k) {
       const double t = ws[k];
       ws[k] = acc;
       acc += t;
@@ -630,10 +633,17 @@ static int chunk_prefix(qsg_ctx* ctx, const float* s, unsigned n,
   prefix_block_sums_kernel<<<(unsigned)nb, kPrefixBlock, 0, ctx->stream>>>(
       *sums, nc, block_tot);
   QSG_LAUNCHED(ctx);
-  chunk_prefix_kernel<<<1, 1024, 0, ctx->stream>>>(block_tot, nb, block_incl);
+  if (nb <= 1024) {
+    // One block, one block sum per thread.
+    const unsigned t = unsigned((nb + 31) / 32 * 32);
+    prefix_block_apply_kernel<<<1, t, 0, ctx->stream>>>(block_tot, nb, nullptr,
+                                                        block_incl);
+  } else {
+    chunk_prefix_kernel<<<1, 1024, 0, ctx->stream>>>(block_tot, nb, block_incl);
+  }
   QSG_LAUNCHED(ctx);
   prefix_block_apply_kernel<<<(unsigned)nb, kPrefixBlock, 0, ctx->stream>>>(
-      *sums, nc, block_incl, *incl);
+      *sums, nc, block_incl, *incl);  // blockDim = kPrefixBlock per block
   QSG_LAUNCHED(ctx);
   return QSG_OK;
 }

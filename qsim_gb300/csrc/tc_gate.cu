@@ -516,24 +516,35 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t obuf = kOffOp + s * kOpBytes;
       float tile_in = 0.f;
 #pragma unroll
+      // All raw reads of the tile first, then the splits and the operand
+      // stores: the stores go to another buffer, but the compiler cannot
+      // move a later shared-memory load above an earlier store, so
+      // interleaving them would expose one load latency per quad.
+      float2 xv[kSplitPerRole][4];
+      uint32_t tso[kSplitPerRole];
+#pragma unroll
       for (int j = 0; j < kSplitPerRole; ++j) {
         const uint32_t e0 = my_se ^ tab_se[j];
-        float x[8];
-        float2 x0, x1, x2, x3;
+        tso[j] = tab_so[j];
         if (e_m1 == 1) {
           // Members 4q, 4q+1 (and 4q+2, 4q+3) are 16-byte units.
           const float4* raw4 = reinterpret_cast<const float4*>(raw);
           const float4 p0 = raw4[e0 >> 1], p1 = raw4[(e0 ^ e_m2) >> 1];
-          x0 = make_float2(p0.x, p0.y);
-          x1 = make_float2(p0.z, p0.w);
-          x2 = make_float2(p1.x, p1.y);
-          x3 = make_float2(p1.z, p1.w);
+          xv[j][0] = make_float2(p0.x, p0.y);
+          xv[j][1] = make_float2(p0.z, p0.w);
+          xv[j][2] = make_float2(p1.x, p1.y);
+          xv[j][3] = make_float2(p1.z, p1.w);
         } else {
-          x0 = raw[e0];
-          x1 = raw[e0 ^ e_m1];
-          x2 = raw[e0 ^ e_m2];
-          x3 = raw[e0 ^ e_m1 ^ e_m2];
+          xv[j][0] = raw[e0];
+          xv[j][1] = raw[e0 ^ e_m1];
+          xv[j][2] = raw[e0 ^ e_m2];
+          xv[j][3] = raw[e0 ^ e_m1 ^ e_m2];
         }
+      }
+#pragma unroll
+      for (int j = 0; j < kSplitPerRole; ++j) {
+        const float2 x0 = xv[j][0], x1 = xv[j][1], x2 = xv[j][2], x3 = xv[j][3];
+        float x[8];
         if (a.out) {
           tile_in = fmaf(x0.x, x0.x, fmaf(x0.y, x0.y, tile_in));
           tile_in = fmaf(x1.x, x1.x, fmaf(x1.y, x1.y, tile_in));
@@ -552,7 +563,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           hp[c] = *reinterpret_cast<const uint32_t*>(&hh);
           lp[c] = pack_half2(x[2 * c] - hf.x, x[2 * c + 1] - hf.y);
         }
-        const uint32_t o = my_so | tab_so[j];
+        const uint32_t o = my_so | tso[j];
         *reinterpret_cast<uint4*>(smem + obuf + o) = h;
         *reinterpret_cast<uint4*>(smem + obuf + kBImgBytes + o) = l;
       }
