@@ -118,6 +118,8 @@ struct Block {
 // count absorbed and fills `cands` with expansion candidates: fusible ops
 // that are not blocked but need qubits outside `mask`, with
 // popcount(mask | q) <= f, in scan order.
+constexpr size_t kCandWindow = 256;
+
 template <typename Fusible>
 size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
                    std::vector<char>& in_block, size_t first, size_t end,
@@ -144,7 +146,11 @@ size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
         cands->push_back(i);
       blocked |= m;
     }
-    if ((mask & ~blocked) == 0 && (!cands || cands->size() >= max_cands))
+    // Once every qubit of the block is blocked nothing more can be absorbed;
+    // the candidate scan then goes on only while it has found fewer than
+    // max_cands candidates and stays within a window of ops.
+    if ((mask & ~blocked) == 0 &&
+        (!cands || cands->size() >= max_cands || i - first > kCandWindow))
       break;
   }
   if (commit) {
