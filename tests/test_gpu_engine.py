@@ -51,6 +51,12 @@ def test_config1_grid20_against_reference(eng, oracle):
     assert rel_l2(got[d["idx"]], d["amp64"]) < TOL
     assert rel_l2(got, oracle_state(oracle, c)) < TOL
     smp = np.array(ss.Sample(st, 1000, 1), np.uint64)
+    # On the same amplitudes the sampling is the reference's algorithm: at
+    # least 99.9 % identical indices to the oracle's FP64 CDF scan.
+    assert np.mean(smp == oracle.sample(got.copy(), n, 1000, 1)) >= 0.999
+    # Against the reference's own samples the states differ by FP32
+    # rounding (the reference's FP32 and FP64 runs themselves agree on
+    # 99.8 % of these samples), so 99.5 %.
     assert np.mean(smp == d["s64"]) >= 0.995
     assert np.mean(smp == d["s32"]) >= 0.995
 
