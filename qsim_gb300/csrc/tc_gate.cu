@@ -41,6 +41,7 @@
 // offset is an OR of a per-thread part and a per-iteration table entry.
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -117,14 +118,14 @@ struct TcGeom {
   uint32_t tile_is_target[kTileBits];
   uint32_t target_slot[kTileBits];   // member bit of a target tile bit
   uint32_t group_slot[kTileBits];    // group bit of a non-target tile bit
-  // XOR swizzles of tile indices, X(e) = OR_i bit(e, src[i]) << dst[i] with
-  // src >= 4 and dst < 4, so that the accesses of a half-warp fall on
+  // XOR swizzles of tile indices, X(e) = XOR_i bit(e, src[i]) * msk[i]
+  // with src >= 4 and msk < 16, so that the accesses of a half-warp fall on
   // distinct banks.  `out`: epilogue staging (8-byte writes by member x
   // group-bit-4 lanes, 16-byte linear reads).  `raw`: raw tile buffer
   // (16-byte cp.async writes, 8-byte split reads by group-bits-0..2 x
   // member-bit-2 lanes); it never touches bit 0.
-  uint32_t out_src[4], out_dst[4], out_n;
-  uint32_t raw_src[4], raw_dst[4], raw_n;
+  uint32_t out_src[8], out_msk[8], out_n;
+  uint32_t raw_src[8], raw_msk[8], raw_n;
 };
 
 struct TcArgs {
@@ -279,6 +280,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "r"(taddr));
 }
 
+// 16 lanes x 32 columns: thread t gets, for x < 4, words 4x, 4x+1 of lane
+// t / 4 and words 4x+2, 4x+3 of lane t / 4 + 8, at columns 8x + 2 (t % 4)
+// and 8x + 2 (t % 4) + 1.
+__device__ __forceinline__ void tmem_ld16x256_x4(uint32_t taddr,
+                                                 uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.16x256b.x4.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+        "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
@@ -293,7 +309,7 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // Tile index e (12 bits) -> state offset: OR of the state bits of e's bits.
-__device__ __forceinline__ uint64_t tile_goff(uint32_t e, const TcGeom& g) {
+__host__ __device__ __forceinline__ uint64_t tile_goff(uint32_t e, const TcGeom& g) {
   uint64_t o = 0;
 #pragma unroll
   for (int j = 0; j < kTileBits; ++j)
@@ -302,7 +318,7 @@ __device__ __forceinline__ uint64_t tile_goff(uint32_t e, const TcGeom& g) {
 }
 
 // Group n (6 bits) and member m (6 bits) -> tile index e.
-__device__ __forceinline__ uint32_t tile_e(uint32_t n, uint32_t m,
+__host__ __device__ __forceinline__ uint32_t tile_e(uint32_t n, uint32_t m,
                                            const TcGeom& g) {
   uint32_t e = 0;
 #pragma unroll
@@ -318,33 +334,38 @@ __device__ __forceinline__ uint32_t tile_e(uint32_t n, uint32_t m,
 // n bits 3-5 << 7): the 16-byte operand row chunk (8 FP16 K-elements) of
 // group n, members 4q .. 4q+3.  Lanes 0..7 of a warp cover the 8 rows of one
 // core matrix, so the 128-bit operand stores are conflict free.
-__device__ __forceinline__ uint32_t split_n(uint32_t idx) {
+__host__ __device__ __forceinline__ uint32_t split_n(uint32_t idx) {
   return (idx & 7) | ((idx >> 7) << 3);
 }
-__device__ __forceinline__ uint32_t split_q(uint32_t idx) {
+__host__ __device__ __forceinline__ uint32_t split_q(uint32_t idx) {
   return (idx >> 3) & 15;
 }
 __host__ __device__ __forceinline__ uint32_t op_off(uint32_t n, uint32_t q) {
   return (n / 8) * kSBOB + q * kLBO + (n % 8) * 16;
 }
 
-__device__ __forceinline__ uint32_t swz_x(uint32_t e, const uint32_t* src,
-                                          const uint32_t* dst, uint32_t n) {
+// N: the most entries a swizzle can have (4 for one access pattern, 8 for
+// the two-gate mid tile).
+template <int N = 8>
+__host__ __device__ __forceinline__ uint32_t swz_x(uint32_t e, const uint32_t* src,
+                                          const uint32_t* msk, uint32_t n) {
   uint32_t x = 0;
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
-    if (i < int(n)) x |= ((e >> src[i]) & 1u) << dst[i];
+  for (int i = 0; i < N; ++i)
+    if (i < int(n) && ((e >> src[i]) & 1u)) x ^= msk[i];
   return x;
 }
 // s(e) = e ^ X(e); for disjoint a, b: s(a | b) = s(a) ^ s(b).
-__device__ __forceinline__ uint32_t swz_out(uint32_t e, const TcGeom& g) {
-  return e ^ swz_x(e, g.out_src, g.out_dst, g.out_n);
+template <int N = 8>
+__host__ __device__ __forceinline__ uint32_t swz_out(uint32_t e, const TcGeom& g) {
+  return e ^ swz_x<N>(e, g.out_src, g.out_msk, g.out_n);
 }
-__device__ __forceinline__ uint32_t swz_raw(uint32_t e, const TcGeom& g) {
-  return e ^ swz_x(e, g.raw_src, g.raw_dst, g.raw_n);
+template <int N = 8>
+__host__ __device__ __forceinline__ uint32_t swz_raw(uint32_t e, const TcGeom& g) {
+  return e ^ swz_x<N>(e, g.raw_src, g.raw_msk, g.raw_n);
 }
 
-__device__ __forceinline__ uint64_t expand_outer_tc(uint64_t t,
+__host__ __device__ __forceinline__ uint64_t expand_outer_tc(uint64_t t,
                                                     const TcGeom& g) {
   uint64_t x = t << g.b;
   for (uint32_t i = 0; i < g.n_ins; ++i) {
@@ -421,16 +442,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   // tile is tile index e = 2u: bits 1..8 from rtid, bits 9..11 from j.
   if (tid < kUnitsPerRole) {
     tab_g[tid] = tile_goff(uint32_t(tid) << (kRoleBits + 1), g);
-    tab_rd[tid] = swz_out(uint32_t(tid) << (kRoleBits + 1), g);
-    tab_wr[tid] = swz_raw(uint32_t(tid) << (kRoleBits + 1), g);
+    tab_rd[tid] = swz_out<4>(uint32_t(tid) << (kRoleBits + 1), g);
+    tab_wr[tid] = swz_raw<4>(uint32_t(tid) << (kRoleBits + 1), g);
   }
   if (tid < kSplitPerRole) {
     // Split item idx = rtid + 256 j: j supplies idx bits 8, 9 (n bits 4, 5).
     const uint32_t idx = tid << kRoleBits;
-    tab_se[tid] = swz_raw(tile_e(split_n(idx), 4 * split_q(idx), g), g);
+    tab_se[tid] = swz_raw<4>(tile_e(split_n(idx), 4 * split_q(idx), g), g);
     tab_so[tid] = op_off(split_n(idx), split_q(idx));
   }
-  if (tid < kGroups) tab_ge[tid] = swz_out(tile_e(tid, 0, g), g);
+  if (tid < kGroups) tab_ge[tid] = swz_out<4>(tile_e(tid, 0, g), g);
   if (tid == 0) {
     for (uint32_t i = 0; i < kNumBars; ++i) mbar_init(&bars[i], 1);
     *flag = 0;
@@ -458,8 +479,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ======================== producers ==================================
     const uint32_t rt = tid;
     const uint64_t my_g = tile_goff(rt << 1, g);
-    const uint32_t my_wr = swz_raw(rt << 1, g);
-    const uint32_t my_se = swz_raw(tile_e(split_n(rt), 4 * split_q(rt), g), g);
+    const uint32_t my_wr = swz_raw<4>(rt << 1, g);
+    const uint32_t my_se = swz_raw<4>(tile_e(split_n(rt), 4 * split_q(rt), g), g);
     const uint32_t my_so = op_off(split_n(rt), split_q(rt));
     // Swizzled tile offsets of member bits 0 and 1 (members 4q + 1, + 2).
     uint32_t e_m1 = 0, e_m2 = 0;
@@ -467,8 +488,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (g.tile_is_target[j] && g.target_slot[j] == 0) e_m1 = 1u << j;
       if (g.tile_is_target[j] && g.target_slot[j] == 1) e_m2 = 1u << j;
     }
-    e_m1 = swz_raw(e_m1, g);
-    e_m2 = swz_raw(e_m2, g);
+    e_m1 = swz_raw<4>(e_m1, g);
+    e_m2 = swz_raw<4>(e_m2, g);
     // Norm carry: the previous pass's (sum in, sum out), reduced by each
     // producer warp in the same order (identical results in every warp).
     float carry = 1.f;
@@ -599,13 +620,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = (32 * quad) << 16;
     const uint32_t row = 32 * quad + lane;
     // Gate into tensor memory: rows of this quadrant, columns of this half
-    // (A_hi and A_lo, 64 columns of FP16 pairs each).  Row 2r + pr of the
-    // real form [[Mr, -Mi], [Mi, Mr]] interleaved by (member, re/im); word w
-    // holds columns 2w, 2w + 1, i.e. (Mr, -Mi) or (Mi, Mr) of M[r][w], split
-    // into FP16 hi and lo parts.
+    // (A_hi and A_lo, 64 columns of FP16 pairs each).  Row 16a + 8p + b is
+    // the real (p = 0) or imaginary (p = 1) part of member 8a + b, so that a
+    // 16x256b load gives one thread both parts of an output amplitude; word
+    // w holds columns 2w, 2w + 1 of that row of [[Mr, -Mi], [Mi, Mr]]
+    // interleaved by (member, re/im), i.e. (Mr, -Mi) or (Mi, Mr) of M[r][w],
+    // split into FP16 hi and lo parts.
     {
-      const float2* mrow = a.operands + size_t(row / 2) * kD + 32 * chalf;
-      const bool im_row = row & 1;
+      const uint32_t member = 8 * (row >> 4) + (row & 7);
+      const float2* mrow = a.operands + size_t(member) * kD + 32 * chalf;
+      const bool im_row = (row >> 3) & 1;
       uint32_t hw[32], lw[32];
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
@@ -625,8 +649,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (et == 0) mbar_arrive(gate_ready);  // gate loaded: MMAs may start
     }
     const uint64_t my_g = tile_goff(et << 1, g);
-    const uint32_t my_rd = swz_out(et << 1, g);
-    const uint32_t my_me = swz_out(tile_e(0, row / 2, g), g);
+    const uint32_t my_rd = swz_out<4>(et << 1, g);
+    // Drain (16x256b loads of lane halves h = 0, 1 of this quadrant): this
+    // thread holds member 8 (2 quad + h) + lane / 4 of groups
+    // 32 chalf + 2 (lane % 4) + 8x + {0, 1}, x < 4; my_me[h] is the staging
+    // slot of its first group, tab_ge[8x + e] the offset of the others.
+    const uint32_t col0 = 32 * chalf + 2 * (lane & 3);
+    uint32_t my_me[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      my_me[h] = swz_out<4>(tile_e(col0, 8 * (2 * quad + h) + lane / 4, g), g);
     const float inv = a.inv_scale;
     // sum |output|^2 over this thread's outputs: FP32 per tile, Kahan FP32
     // across tiles.
@@ -639,27 +671,26 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (bar_or(2, kEpiThreads, bad)) break;
       tc_fence_after();
       uint32_t v[32];
-      tmem_ld32(tmem + lane_base + kTmemD + 64 * s + 32 * chalf, v);
+      const uint32_t taddr = tmem + lane_base + kTmemD + 64 * s + 32 * chalf;
+      tmem_ld16x256_x4(taddr, v);
+      tmem_ld16x256_x4(taddr + (16u << 16), v + 16);
       tmem_wait_ld();
       tc_fence_before();
       bar_sync(2, kEpiThreads);
       if (et == 0) mbar_arrive(&acc_free[s]);  // accumulator s drained
       float2* stage = reinterpret_cast<float2*>(smem + kOffOp + s * kOpBytes);
-      const bool odd = lane & 1;
       float fo = 0.f;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        // Of this warp's 32 columns, even lanes (re rows) keep the first 16
-        // groups and odd lanes (im rows) the last 16.
-        const uint32_t send = odd ? v[j] : v[16 + j];
-        const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        const uint32_t mine = odd ? v[16 + j] : v[j];
-        const float re = __uint_as_float(odd ? recv : mine) * inv;
-        const float im = __uint_as_float(odd ? mine : recv) * inv;
-        const uint32_t grp = 32 * chalf + (odd ? 16 + j : j);
-        stage[my_me ^ tab_ge[grp]] = make_float2(re, im);
-        fo = fmaf(re, re, fmaf(im, im, fo));
-      }
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const float re = __uint_as_float(v[16 * h + 4 * x + e]) * inv;
+            const float im = __uint_as_float(v[16 * h + 4 * x + 2 + e]) * inv;
+            stage[my_me[h] ^ tab_ge[8 * x + e]] = make_float2(re, im);
+            fo = fmaf(re, re, fmaf(im, im, fo));
+          }
       {
         const float y = fo - sout_c;
         const float t2 = sout_s + y;
@@ -784,6 +815,118 @@ static void pad_to_6(unsigned n, const unsigned* qs, unsigned k,
   for (unsigned j = 0; j < 6; ++j) qs6[j] = all[j];
 }
 
+// XOR swizzle (src, msk, n) for which each set of four tile bits in
+// `sets` maps its 16 index combinations onto 16 distinct values modulo 16
+// (distinct banks for a half-warp of 8-byte accesses, or a quarter-warp of
+// 16-byte ones when bit 0 is not among them and masks keep bit 0 clear):
+// a tile bit v < 4 contributes the unit vector e_v, a bit v >= 4 the mask
+// chosen for it, and each set's four vectors must be linearly independent
+// over GF(2).  Depth-first search over the masks of the high bits; false if
+// none exists.
+static bool solve_swizzle(const std::vector<std::vector<unsigned>>& sets,
+                          unsigned allowed, uint32_t* src, uint32_t* msk,
+                          uint32_t* n) {
+  std::vector<unsigned> high;
+  for (const auto& v : sets)
+    for (unsigned b : v)
+      if (b >= 4 && std::find(high.begin(), high.end(), b) == high.end())
+        high.push_back(b);
+  if (high.size() > 8) return false;
+  std::vector<uint32_t> m(high.size(), 0);
+  auto vec = [&](unsigned b, size_t assigned, bool* known) -> uint32_t {
+    if (b < 4) {
+      *known = true;
+      return 1u << b;
+    }
+    const size_t i = size_t(std::find(high.begin(), high.end(), b) - high.begin());
+    *known = i < assigned;
+    return *known ? m[i] : 0;
+  };
+  // Independence of the known vectors of every set (rank by elimination).
+  auto ok = [&](size_t assigned) {
+    for (const auto& v : sets) {
+      uint32_t basis[4] = {0, 0, 0, 0};
+      for (unsigned b : v) {
+        bool known;
+        uint32_t x = vec(b, assigned, &known);
+        if (!known) continue;
+        for (int bit = 3; bit >= 0; --bit) {
+          if (!((x >> bit) & 1)) continue;
+          if (!basis[bit]) {
+            basis[bit] = x;
+            break;
+          }
+          x ^= basis[bit];
+        }
+        if (!x) return false;
+      }
+    }
+    return true;
+  };
+  std::function<bool(size_t)> dfs = [&](size_t i) {
+    if (i == high.size()) return true;
+    for (uint32_t c = 1; c < 16; ++c) {
+      if (c & ~allowed) continue;
+      m[i] = c;
+      if (ok(i + 1) && dfs(i + 1)) return true;
+    }
+    return false;
+  };
+  if (!ok(0) || !dfs(0)) return false;
+  *n = unsigned(high.size());
+  for (size_t i = 0; i < high.size(); ++i) {
+    src[i] = high[i];
+    msk[i] = m[i];
+  }
+  return true;
+}
+
+// Member / group roles of the tile bits of a gate with sorted targets qs6
+// (the tile's bit -> state-bit map already set), and the swizzles of its
+// raw buffer and epilogue staging.
+static bool tc_roles(TcGeom& g, const unsigned* qs6) {
+  unsigned tslot = 0, gslot = 0;
+  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
+    const unsigned sb = unsigned(g.bitpos_state[j]);
+    const bool is_t = std::find(qs6, qs6 + kK, sb) != qs6 + kK;
+    g.tile_is_target[j] = is_t;
+    g.target_slot[j] = 0;
+    g.group_slot[j] = 0;
+    if (is_t) {
+      // member bit = index of this target in the sorted target list
+      g.target_slot[j] = unsigned(std::find(qs6, qs6 + kK, sb) - qs6);
+      ++tslot;
+    } else {
+      g.group_slot[j] = gslot++;
+    }
+  }
+  if (tslot != unsigned(kK) || gslot != 6) return false;
+  unsigned gpos[6], tpos[6];
+  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
+    if (g.tile_is_target[j]) tpos[g.target_slot[j]] = j;
+    else gpos[g.group_slot[j]] = j;
+  }
+  // Epilogue writes: half-warp lanes vary member bits 0, 1 (lane / 4) and
+  // group bits 1, 2 (lane % 4).
+  if (!solve_swizzle({{tpos[0], tpos[1], gpos[1], gpos[2]}}, 0xF, g.out_src,
+                     g.out_msk, &g.out_n))
+    return false;
+  // Split reads: lanes vary group bits 0..2 and (half-warp) member bit 2;
+  // 16-byte units keep bit 0 in place.  With qubit 0 a target (member bit 0
+  // = tile bit 0) members 4q, 4q+1 are one 16-byte unit read by one LDS.128,
+  // and the quarter-warp lanes (group bits 0..2) must hit distinct units
+  // (bits 1..3 of the swizzled index).
+  if (g.tile_is_target[0]) {
+    if (!solve_swizzle({{0, gpos[0], gpos[1], gpos[2]}}, 0xE, g.raw_src,
+                       g.raw_msk, &g.raw_n))
+      return false;
+  } else if (!solve_swizzle({{gpos[0], gpos[1], gpos[2], tpos[2]}}, 0xE,
+                            g.raw_src, g.raw_msk, &g.raw_n)) {
+    return false;
+  }
+  return true;
+}
+
 static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
   std::memset(&g, 0, sizeof(g));
   if (n < kTileBits) return false;
@@ -800,63 +943,536 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
   // Tile bit j < b is state bit j; tile bit b + i is the i-th high target.
   for (unsigned j = 0; j < b; ++j) g.bitpos_state[j] = j;
   for (unsigned i = 0; i < h; ++i) g.bitpos_state[b + i] = qs6[kK - h + i];
-  unsigned tslot = 0, gslot = 0;
-  for (unsigned j = 0; j < tb; ++j) {
-    const unsigned sb = g.bitpos_state[j];
-    bool is_t = std::find(qs6, qs6 + kK, sb) != qs6 + kK;
-    g.tile_is_target[j] = is_t;
-    if (is_t) {
-      // member bit = index of this target in the sorted target list
-      g.target_slot[j] = unsigned(std::find(qs6, qs6 + kK, sb) - qs6);
-      ++tslot;
-    } else {
-      g.group_slot[j] = gslot++;
-    }
-  }
-  if (tslot != kK || gslot != 6) return false;
-  // Swizzles.  Tile positions of group bits and member bits:
-  unsigned gpos[6], tpos[6];
-  for (unsigned j = 0; j < tb; ++j) {
-    if (g.tile_is_target[j]) tpos[g.target_slot[j]] = j;
-    else gpos[g.group_slot[j]] = j;
-  }
-  auto build = [](const std::vector<unsigned>& vary, unsigned allowed,
-                  uint32_t* src, uint32_t* dst, uint32_t* n) {
-    unsigned covered = 0;
-    std::vector<unsigned> srcs;
-    for (unsigned p : vary) {
-      if (p < 4) covered |= 1u << p;
-      else srcs.push_back(p);
-    }
-    std::vector<unsigned> dsts;
-    for (unsigned b2 = 0; b2 < 4; ++b2)
-      if (((allowed >> b2) & 1) && !((covered >> b2) & 1)) dsts.push_back(b2);
-    *n = unsigned(std::min(srcs.size(), dsts.size()));
-    for (unsigned i = 0; i < *n; ++i) {
-      src[i] = srcs[i];
-      dst[i] = dsts[i];
-    }
-  };
-  // Epilogue writes: half-warp lanes vary member bits 0..2 and group bit 4
-  // (even lanes keep groups 0..15 of a warp's 32 columns, odd lanes 16..31).
-  build({tpos[0], tpos[1], tpos[2], gpos[4]}, 0xF, g.out_src, g.out_dst,
-        &g.out_n);
-  // Split reads: lanes vary group bits 0..2 and (half-warp) member bit 2;
-  // 16-byte units keep bit 0 in place.  With qubit 0 a target (member bit 0
-  // = tile bit 0) members 4q, 4q+1 are one 16-byte unit read by one LDS.128,
-  // and the quarter-warp lanes (group bits 0..2) must hit distinct units.
-  if (g.tile_is_target[0])
-    build({gpos[0], gpos[1], gpos[2]}, 0xE, g.raw_src, g.raw_dst, &g.raw_n);
-  else
-    build({gpos[0], gpos[1], gpos[2], tpos[2]}, 0xE, g.raw_src, g.raw_dst,
-          &g.raw_n);
-
+  if (!tc_roles(g, qs6)) return false;
   std::vector<unsigned> ins(qs6 + kK - h, qs6 + kK);
   std::sort(ins.begin(), ins.end());
   g.n_ins = ins.size();
   for (size_t i = 0; i < ins.size(); ++i) g.ins_pos[i] = ins[i];
   g.num_tiles = uint64_t{1} << (n - tb);
   return true;
+}
+
+
+// ===========================================================================
+// Two gates per pass.  Gates A and B (6 targets each, padded) whose qubits
+// fit one 12-bit tile (|A u B| <= 12) are applied in one read and one write
+// of the state: the tile is split and multiplied by A, the epilogue writes
+// A's result (FP32, still scaled by sigma) back into shared memory ("mid"),
+// the producers split that for B, and the epilogue stores B's result.  Both
+// gates share the tile's bit -> state-bit map; each has its own member /
+// group roles of the tile bits (geometries ga, gb).  Every role walks the
+// same job list, A(0), A(1), B(0), A(2), B(1), ..., A(T-1), B(T-2), B(T-1),
+// so that a tile's B job finds its A result ready while the next tile's A
+// job keeps the tensor cores busy.  Job k uses operand buffer k % kNB2 and
+// accumulator k % kNA2; an A job's buffer then holds its mid tile until the
+// producers have split it for B.  Numerically a pass is two passes of the
+// one-gate kernel without the FP32 round trip through HBM in between.
+constexpr int kNB2 = 5;                  // operand / mid / staging buffers
+constexpr int kNA2 = 4;                  // accumulators (64 columns each)
+constexpr uint32_t kTmemGateB = 128;     // columns of gate B (A at 0)
+constexpr uint32_t kTmemD2 = 256;        // first accumulator column
+constexpr uint32_t kOffOp2 = kOffRaw + kRawStages * kTileBytes;
+constexpr uint32_t kOffTabG2 = kOffOp2 + kNB2 * kOpBytes;  // 8 x u64
+constexpr uint32_t kOffTabSE2 = kOffTabG2 + 64;            // 2 x 4 x u32
+constexpr uint32_t kOffTabSO2 = kOffTabSE2 + 32;           // 4 x u32
+constexpr uint32_t kOffTabGE2 = kOffTabSO2 + 16;           // 2 x 64 x u32
+constexpr uint32_t kOffTabRd2 = kOffTabGE2 + 512;          // 8 x u32 (B)
+constexpr uint32_t kOffTabWr2 = kOffTabRd2 + 32;           // 8 x u32 (A)
+constexpr uint32_t kNumBars2 = 2 * kNB2 + 2 * kNA2 + 2 + 1;
+constexpr uint32_t kOffBar2 = kOffTabWr2 + 32;
+constexpr uint32_t kOffFlag2 = kOffBar2 + 8 * kNumBars2;
+constexpr uint32_t kOffNorm2 = kOffFlag2 + 16;             // 16 x f64
+constexpr uint32_t kOffTmem2 = kOffNorm2 + 16 * 8 + 16;
+constexpr uint32_t kSmemBytes2 = kOffTmem2 + 16;
+static_assert(kSmemBytes2 <= 232448, "shared memory budget (two gates)");
+static_assert(kTmemD2 + kNA2 * 64 <= kTmemCols, "tensor memory budget");
+
+struct Tc2Args {
+  TcGeom ga, gb;          // the same tile bits; A's and B's member roles
+  const float2* opa;      // padded 64 x 64 complex FP32 gates
+  const float2* opb;
+  float scale, inv_scale;
+  int* error;
+  const double* prev;     // norm carry, as TcArgs
+  uint32_t prev_count;
+  double* out;
+  long long wait_cycles;
+};
+
+// Job k of a CTA with T tiles: its tile index i and whether it is gate B.
+__device__ __forceinline__ void tc2_job(uint64_t k, uint64_t T, uint64_t* i,
+                                        bool* is_b) {
+  if (k == 0) {
+    *i = 0;
+    *is_b = false;
+  } else if (k == 2 * T - 1) {
+    *i = T - 1;
+    *is_b = true;
+  } else if (k & 1) {
+    *i = (k + 1) / 2;
+    *is_b = false;
+  } else {
+    *i = k / 2 - 1;
+    *is_b = true;
+  }
+}
+
+// Job index of tile i's A job.
+__device__ __forceinline__ uint64_t tc2_job_a(uint64_t i) {
+  return i == 0 ? 0 : 2 * i - 1;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gate2_kernel(float2* __restrict__ st,
+                    const __grid_constant__ Tc2Args a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const TcGeom& ga = a.ga;
+  const TcGeom& gb = a.gb;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t warp = tid / 32, lane = tid % 32;
+  uint64_t* tab_g = reinterpret_cast<uint64_t*>(smem + kOffTabG2);
+  uint32_t* tab_se = reinterpret_cast<uint32_t*>(smem + kOffTabSE2);  // [2][4]
+  uint32_t* tab_so = reinterpret_cast<uint32_t*>(smem + kOffTabSO2);
+  uint32_t* tab_ge = reinterpret_cast<uint32_t*>(smem + kOffTabGE2);  // [2][64]
+  uint32_t* tab_rd = reinterpret_cast<uint32_t*>(smem + kOffTabRd2);
+  uint32_t* tab_wr = reinterpret_cast<uint32_t*>(smem + kOffTabWr2);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kOffBar2);
+  uint64_t* op_full = bars;                        // [kNB2] producers -> MMA
+  uint64_t* op_free = bars + kNB2;                 // [kNB2] buffer reusable
+  uint64_t* acc_full = bars + 2 * kNB2;            // [kNA2] MMA -> epilogue
+  uint64_t* acc_free = bars + 2 * kNB2 + kNA2;     // [kNA2] epilogue -> MMA
+  uint64_t* mid_full = bars + 2 * kNB2 + 2 * kNA2;  // [2] epilogue -> producers
+  uint64_t* gate_ready = mid_full + 2;             // epilogue -> MMA
+  volatile int* flag = reinterpret_cast<volatile int*>(smem + kOffFlag2);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kOffTmem2);
+  const uint32_t sbase = smem_u32(smem);
+
+  // ---- set-up ------------------------------------------------------------
+  if (tid < kUnitsPerRole) {
+    tab_g[tid] = tile_goff(uint32_t(tid) << (kRoleBits + 1), ga);
+    tab_rd[tid] = swz_out<4>(uint32_t(tid) << (kRoleBits + 1), gb);
+    tab_wr[tid] = swz_raw<4>(uint32_t(tid) << (kRoleBits + 1), ga);
+  }
+  if (tid < kSplitPerRole) {
+    const uint32_t idx = tid << kRoleBits;
+    // A splits the raw tile (A's raw swizzle); B splits the mid tile, which
+    // A's epilogue wrote with A's output swizzle.
+    tab_se[tid] = swz_raw<4>(tile_e(split_n(idx), 4 * split_q(idx), ga), ga);
+    tab_se[kSplitPerRole + tid] =
+        swz_out(tile_e(split_n(idx), 4 * split_q(idx), gb), ga);
+    tab_so[tid] = op_off(split_n(idx), split_q(idx));
+  }
+  if (tid < kGroups) {
+    tab_ge[tid] = swz_out(tile_e(tid, 0, ga), ga);
+    tab_ge[kGroups + tid] = swz_out<4>(tile_e(tid, 0, gb), gb);
+  }
+  if (tid == 0) {
+    for (uint32_t i = 0; i < kNumBars2; ++i) mbar_init(&bars[i], 1);
+    *flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  const uint32_t mma_warp = kProdWarps + kEpiWarps;
+  if (warp == mma_warp) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+            smem_u32(tmem_slot)),
+        "r"(kTmemCols)
+        : "memory");
+    asm volatile(
+        "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::
+            : "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint64_t step = gridDim.x;
+  const uint64_t t0 = blockIdx.x;
+  const uint64_t T =
+      t0 < ga.num_tiles ? (ga.num_tiles - t0 + step - 1) / step : 0;
+  const uint64_t jobs = 2 * T;
+
+  if (warp < kProdWarps) {
+    // ======================== producers ==================================
+    const uint32_t rt = tid;
+    const uint64_t my_g = tile_goff(rt << 1, ga);
+    const uint32_t my_wr = swz_raw<4>(rt << 1, ga);
+    const uint32_t my_se_a =
+        swz_raw<4>(tile_e(split_n(rt), 4 * split_q(rt), ga), ga);
+    const uint32_t my_se_b =
+        swz_out(tile_e(split_n(rt), 4 * split_q(rt), gb), ga);
+    const uint32_t my_so = op_off(split_n(rt), split_q(rt));
+    // Tile offsets of member bits 0 and 1 in each gate, swizzled like the
+    // buffer the gate's split reads (raw for A, mid for B).
+    uint32_t am1 = 0, am2 = 0, bm1 = 0, bm2 = 0;
+    for (int j = 0; j < kTileBits; ++j) {
+      if (ga.tile_is_target[j] && ga.target_slot[j] == 0) am1 = 1u << j;
+      if (ga.tile_is_target[j] && ga.target_slot[j] == 1) am2 = 1u << j;
+      if (gb.tile_is_target[j] && gb.target_slot[j] == 0) bm1 = 1u << j;
+      if (gb.tile_is_target[j] && gb.target_slot[j] == 1) bm2 = 1u << j;
+    }
+    const bool a_units = am1 == 1;  // members 4q, 4q+1 are 16-byte units
+    am1 = swz_raw<4>(am1, ga);
+    am2 = swz_raw<4>(am2, ga);
+    bm1 = swz_out(bm1, ga);
+    bm2 = swz_out(bm2, ga);
+    float carry = 1.f;
+    if (a.prev) {
+      double pin = 0, pout = 0;
+      for (uint32_t i = lane; i < a.prev_count; i += 32) {
+        pin += a.prev[2 * i];
+        pout += a.prev[2 * i + 1];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        pin += __shfl_xor_sync(0xffffffffu, pin, o);
+        pout += __shfl_xor_sync(0xffffffffu, pout, o);
+      }
+      if (pout > 0) carry = float(sqrt(pin / pout));
+    }
+    const float sc = a.scale * carry;
+    float sin_s = 0.f, sin_c = 0.f;
+    auto issue_loads = [&](uint64_t i) {
+      const uint64_t t = t0 + i * step;
+      if (i < T) {
+        const float4* gp = reinterpret_cast<const float4*>(
+            st + (expand_outer_tc(t, ga) | my_g));
+        const uint32_t sdst = sbase + kOffRaw + (i % kRawStages) * kTileBytes;
+#pragma unroll
+        for (int j = 0; j < kUnitsPerRole; ++j)
+          cp_async16(sdst + 8 * (my_wr ^ tab_wr[j]), gp + (tab_g[j] >> 1));
+      }
+      cp_commit();
+    };
+    for (int q = 0; q < kRawStages; ++q) issue_loads(q);
+    for (uint64_t k = 0; k < jobs; ++k) {
+      uint64_t i;
+      bool is_b;
+      tc2_job(k, T, &i, &is_b);
+      const int b = int(k % kNB2);
+      bool bad = false;
+      if (k >= kNB2)
+        bad = !mbar_wait(&op_free[b], uint32_t((k - kNB2) / kNB2) & 1, flag,
+                         a.wait_cycles);
+      if (!is_b) {
+        cp_wait<kRawStages - 1>();
+      } else if (!bad) {
+        bad = !mbar_wait(&mid_full[i & 1], uint32_t(i >> 1) & 1, flag,
+                         a.wait_cycles);
+      }
+      if (bar_or(1, kProdThreads, bad)) break;
+      const uint32_t obuf = kOffOp2 + b * kOpBytes;
+      const float2* src;
+      uint32_t se0, m1, m2, set;
+      float scl;
+      if (!is_b) {
+        src = reinterpret_cast<const float2*>(
+            smem + kOffRaw + (i % kRawStages) * kTileBytes);
+        se0 = my_se_a;
+        m1 = am1;
+        m2 = am2;
+        set = 0;
+        scl = sc;
+      } else {
+        src = reinterpret_cast<const float2*>(
+            smem + kOffOp2 + (tc2_job_a(i) % kNB2) * kOpBytes);
+        se0 = my_se_b;
+        m1 = bm1;
+        m2 = bm2;
+        set = kSplitPerRole;
+        scl = 1.f;  // the mid tile is already scaled
+      }
+      float2 xv[kSplitPerRole][4];
+#pragma unroll
+      for (int j = 0; j < kSplitPerRole; ++j) {
+        const uint32_t e0 = se0 ^ tab_se[set + j];
+        if (!is_b && a_units) {
+          const float4* raw4 = reinterpret_cast<const float4*>(src);
+          const float4 p0 = raw4[e0 >> 1], p1 = raw4[(e0 ^ m2) >> 1];
+          xv[j][0] = make_float2(p0.x, p0.y);
+          xv[j][1] = make_float2(p0.z, p0.w);
+          xv[j][2] = make_float2(p1.x, p1.y);
+          xv[j][3] = make_float2(p1.z, p1.w);
+        } else {
+          xv[j][0] = src[e0];
+          xv[j][1] = src[e0 ^ m1];
+          xv[j][2] = src[e0 ^ m2];
+          xv[j][3] = src[e0 ^ m1 ^ m2];
+        }
+      }
+      float tile_in = 0.f;
+#pragma unroll
+      for (int j = 0; j < kSplitPerRole; ++j) {
+        const float2 x0 = xv[j][0], x1 = xv[j][1], x2 = xv[j][2], x3 = xv[j][3];
+        if (a.out && !is_b) {
+          tile_in = fmaf(x0.x, x0.x, fmaf(x0.y, x0.y, tile_in));
+          tile_in = fmaf(x1.x, x1.x, fmaf(x1.y, x1.y, tile_in));
+          tile_in = fmaf(x2.x, x2.x, fmaf(x2.y, x2.y, tile_in));
+          tile_in = fmaf(x3.x, x3.x, fmaf(x3.y, x3.y, tile_in));
+        }
+        float x[8];
+        x[0] = x0.x * scl; x[1] = x0.y * scl; x[2] = x1.x * scl; x[3] = x1.y * scl;
+        x[4] = x2.x * scl; x[5] = x2.y * scl; x[6] = x3.x * scl; x[7] = x3.y * scl;
+        uint4 h, l;
+        uint32_t* hp = &h.x;
+        uint32_t* lp = &l.x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const __half2 hh = __floats2half2_rn(x[2 * c], x[2 * c + 1]);
+          const float2 hf = __half22float2(hh);
+          hp[c] = *reinterpret_cast<const uint32_t*>(&hh);
+          lp[c] = pack_half2(x[2 * c] - hf.x, x[2 * c + 1] - hf.y);
+        }
+        const uint32_t o = my_so | tab_so[j];
+        *reinterpret_cast<uint4*>(smem + obuf + o) = h;
+        *reinterpret_cast<uint4*>(smem + obuf + kBImgBytes + o) = l;
+      }
+      if (a.out && !is_b) {
+        const float y = tile_in - sin_c;
+        const float t2 = sin_s + y;
+        sin_c = (t2 - sin_s) - y;
+        sin_s = t2;
+      }
+      fence_async_smem();
+      bar_sync(1, kProdThreads);
+      if (rt == 0) {
+        mbar_arrive(&op_full[b]);
+        // B's split has read the mid tile: A's buffer is free.
+        if (is_b) mbar_arrive(&op_free[tc2_job_a(i) % kNB2]);
+      }
+      if (!is_b) issue_loads(i + kRawStages);  // raw[i] is consumed
+    }
+    cp_wait<0>();
+    if (a.out) {
+      double sum_in = (double(sin_s) - double(sin_c)) * double(carry) *
+                      double(carry);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        sum_in += __shfl_xor_sync(0xffffffffu, sum_in, o);
+      if (lane == 0)
+        reinterpret_cast<double*>(smem + kOffNorm2)[warp] = sum_in;
+    }
+  } else if (warp < kProdWarps + kEpiWarps) {
+    // ======================== epilogue ===================================
+    const uint32_t et = tid - kProdThreads;
+    const uint32_t ew = warp - kProdWarps;
+    const uint32_t quad = warp % 4, chalf = ew / 4;
+    const uint32_t lane_base = (32 * quad) << 16;
+    const uint32_t row = 32 * quad + lane;
+    // Both gates into tensor memory (A at column 0, B at kTmemGateB), rows
+    // ordered as in the one-gate kernel.
+#pragma unroll 1
+    for (int gi = 0; gi < 2; ++gi) {
+      const uint32_t member = 8 * (row >> 4) + (row & 7);
+      const float2* mrow = (gi ? a.opb : a.opa) + size_t(member) * kD + 32 * chalf;
+      const bool im_row = (row >> 3) & 1;
+      uint32_t hw[32], lw[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const float2 m = mrow[q];
+        const float x0 = im_row ? m.y : m.x;
+        const float x1 = im_row ? m.x : -m.y;
+        const __half2 h = __floats2half2_rn(x0, x1);
+        const float2 hf = __half22float2(h);
+        hw[q] = *reinterpret_cast<const uint32_t*>(&h);
+        lw[q] = pack_half2(x0 - hf.x, x1 - hf.y);
+      }
+      const uint32_t base = gi ? kTmemGateB : 0;
+      tmem_st32(tmem + lane_base + base + kTmemAhi + 32 * chalf, hw);
+      tmem_st32(tmem + lane_base + base + kTmemAlo + 32 * chalf, lw);
+    }
+    tmem_wait_st();
+    tc_fence_before();
+    bar_sync(2, kEpiThreads);
+    if (et == 0) mbar_arrive(gate_ready);
+    const uint64_t my_g = tile_goff(et << 1, ga);
+    const uint32_t my_rd = swz_out<4>(et << 1, gb);
+    const uint32_t col0 = 32 * chalf + 2 * (lane & 3);
+    uint32_t my_me_a[2], my_me_b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t m = 8 * (2 * quad + h) + lane / 4;
+      my_me_a[h] = swz_out(tile_e(col0, m, ga), ga);
+      my_me_b[h] = swz_out<4>(tile_e(col0, m, gb), gb);
+    }
+    const float inv = a.inv_scale;
+    float sout_s = 0.f, sout_c = 0.f;
+    for (uint64_t k = 0; k < jobs; ++k) {
+      uint64_t i;
+      bool is_b;
+      tc2_job(k, T, &i, &is_b);
+      const int acc = int(k % kNA2);
+      const int b = int(k % kNB2);
+      const bool bad = !mbar_wait(&acc_full[acc], uint32_t(k / kNA2) & 1, flag,
+                                  a.wait_cycles);
+      if (bar_or(2, kEpiThreads, bad)) break;
+      tc_fence_after();
+      uint32_t v[32];
+      const uint32_t taddr =
+          tmem + lane_base + kTmemD2 + 64 * acc + 32 * chalf;
+      tmem_ld16x256_x4(taddr, v);
+      tmem_ld16x256_x4(taddr + (16u << 16), v + 16);
+      tmem_wait_ld();
+      tc_fence_before();
+      bar_sync(2, kEpiThreads);
+      if (et == 0) mbar_arrive(&acc_free[acc]);
+      float2* stage = reinterpret_cast<float2*>(smem + kOffOp2 + b * kOpBytes);
+      const uint32_t* ge = tab_ge + (is_b ? kGroups : 0);
+      const float f = is_b ? inv : 1.f;  // A's result stays scaled (mid)
+      float fo = 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint32_t me = is_b ? my_me_b[h] : my_me_a[h];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const float re = __uint_as_float(v[16 * h + 4 * x + e]) * f;
+            const float im = __uint_as_float(v[16 * h + 4 * x + 2 + e]) * f;
+            stage[me ^ ge[8 * x + e]] = make_float2(re, im);
+            if (is_b) fo = fmaf(re, re, fmaf(im, im, fo));
+          }
+      }
+      bar_sync(2, kEpiThreads);
+      if (!is_b) {
+        // The mid tile is complete: B's split may read it.
+        if (et == 0) mbar_arrive(&mid_full[i & 1]);
+        continue;
+      }
+      {
+        const float y = fo - sout_c;
+        const float t2 = sout_s + y;
+        sout_c = (t2 - sout_s) - y;
+        sout_s = t2;
+      }
+      const uint64_t base = expand_outer_tc(t0 + i * step, ga);
+      float4* gp = reinterpret_cast<float4*>(st + (base | my_g));
+      const float4* so = reinterpret_cast<const float4*>(stage);
+#pragma unroll
+      for (int j = 0; j < kUnitsPerRole; ++j) {
+        const uint32_t sidx = my_rd ^ tab_rd[j];
+        float4 w = so[sidx >> 1];
+        if (sidx & 1) w = make_float4(w.z, w.w, w.x, w.y);
+        gp[tab_g[j] >> 1] = w;
+      }
+      bar_sync(2, kEpiThreads);
+      if (et == 0) mbar_arrive(&op_free[b]);  // staging buffer free
+    }
+    if (a.out) {
+      double sum_out = double(sout_s) - double(sout_c);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        sum_out += __shfl_xor_sync(0xffffffffu, sum_out, o);
+      if (lane == 0)
+        reinterpret_cast<double*>(smem + kOffNorm2)[kProdWarps + ew] = sum_out;
+    }
+  } else if (lane == 0) {
+    // ======================== MMA issuer =================================
+    for (uint64_t k = 0; k < jobs; ++k) {
+      uint64_t i;
+      bool is_b;
+      tc2_job(k, T, &i, &is_b);
+      const int b = int(k % kNB2);
+      const int acc = int(k % kNA2);
+      if (!mbar_wait(&op_full[b], uint32_t(k / kNB2) & 1, flag, a.wait_cycles))
+        break;
+      if (k == 0) {
+        if (!mbar_wait(gate_ready, 0, flag, a.wait_cycles)) break;
+      } else if (k >= kNA2) {
+        if (!mbar_wait(&acc_free[acc], uint32_t((k - kNA2) / kNA2) & 1, flag,
+                       a.wait_cycles))
+          break;
+      }
+      tc_fence_after();
+      const uint32_t obuf = kOffOp2 + b * kOpBytes;
+      const uint32_t d = tmem + kTmemD2 + 64 * acc;
+      const uint32_t gbase = tmem + (is_b ? kTmemGateB : 0);
+      const uint64_t dhi = make_desc(sbase + obuf, kLBO, kSBOB);
+      const uint64_t dlo = make_desc(sbase + obuf + kBImgBytes, kLBO, kSBOB);
+#pragma unroll
+      for (int kk = 0; kk < kReal / 16; ++kk) {
+        const uint64_t ko = uint64_t(kk) * (2 * kLBO >> 4);
+        mma_f16_ts(d, gbase + kTmemAhi + 8 * kk, dhi + ko, kk > 0);
+        mma_f16_ts(d, gbase + kTmemAhi + 8 * kk, dlo + ko, 1);
+        mma_f16_ts(d, gbase + kTmemAlo + 8 * kk, dhi + ko, 1);
+      }
+      mma_commit(&acc_full[acc]);
+    }
+  }
+
+  // ---- tear-down -----------------------------------------------------------
+  __syncthreads();
+  if (a.out && tid == 0) {
+    const double* nsum = reinterpret_cast<const double*>(smem + kOffNorm2);
+    double si = 0, so = 0;
+    for (int w = 0; w < kProdWarps; ++w) si += nsum[w];
+    for (int w = 0; w < kEpiWarps; ++w) so += nsum[kProdWarps + w];
+    a.out[2 * blockIdx.x] = si;
+    a.out[2 * blockIdx.x + 1] = so;
+  }
+  if (warp == mma_warp) {
+    if (*flag) {
+      if (lane == 0) atomicExch(a.error, 1);
+      const long long c0 = clock64();
+      while (clock64() - c0 < a.wait_cycles / 4) {
+      }
+    }
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(
+                     tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// Geometry of a pair: the 12 tile bits are the union `u` of the two gates'
+// (padded) targets, completed with the lowest other qubits; both geometries
+// share the tile-bit -> state-bit map and differ in member / group roles.
+// A's staging swizzle is the layout of the mid tile, which A's epilogue
+// writes and B's split reads: it is solved for both access patterns.
+static bool plan_tc2(unsigned n, const unsigned* qa6, const unsigned* qb6,
+                     TcGeom& ga, TcGeom& gb) {
+  std::vector<unsigned> u(qa6, qa6 + kK);
+  for (unsigned j = 0; j < kK; ++j)
+    if (std::find(u.begin(), u.end(), qb6[j]) == u.end()) u.push_back(qb6[j]);
+  if (u.size() > kTileBits || n < kTileBits) return false;
+  for (unsigned q = 0; u.size() < kTileBits && q < n; ++q)
+    if (std::find(u.begin(), u.end(), q) == u.end()) u.push_back(q);
+  std::sort(u.begin(), u.end());
+  // Run bits: tile bits j < b are state bits j; the h = 12 - b highest
+  // members of u are the tile's high bits.
+  unsigned h = 0, b = kTileBits;
+  for (h = 0; h <= kTileBits; ++h) {
+    b = kTileBits - h;
+    unsigned cnt = 0;
+    for (unsigned q : u) cnt += q >= b;
+    if (cnt == h) break;
+  }
+  // Tile bit 0 must be state bit 0: the kernel moves amplitudes in pairs of
+  // neighbours (16-byte units).
+  if (h > kTileBits || b < 1) return false;
+  for (int gi = 0; gi < 2; ++gi) {
+    TcGeom& g = gi ? gb : ga;
+    std::memset(&g, 0, sizeof(g));
+    g.b = b;
+    for (unsigned j = 0; j < b; ++j) g.bitpos_state[j] = j;
+    for (unsigned i = 0; i < h; ++i) g.bitpos_state[b + i] = u[kTileBits - h + i];
+    if (!tc_roles(g, gi ? qb6 : qa6)) return false;
+    g.n_ins = h;
+    for (unsigned i = 0; i < h; ++i) g.ins_pos[i] = u[kTileBits - h + i];
+    g.num_tiles = uint64_t{1} << (n - kTileBits);
+  }
+  unsigned gpa[6], tpa[6], gpb[6], tpb[6];
+  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
+    if (ga.tile_is_target[j]) tpa[ga.target_slot[j]] = j;
+    else gpa[ga.group_slot[j]] = j;
+    if (gb.tile_is_target[j]) tpb[gb.target_slot[j]] = j;
+    else gpb[gb.group_slot[j]] = j;
+  }
+  return solve_swizzle({{tpa[0], tpa[1], gpa[1], gpa[2]},
+                        {gpb[0], gpb[1], gpb[2], tpb[2]}},
+                       0xF, ga.out_src, ga.out_msk, &ga.out_n);
 }
 
 }  // namespace tc
@@ -886,21 +1502,28 @@ void tc_pad_gate(unsigned n, const unsigned* qs, unsigned k, const float* m32,
 int apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n, const unsigned* qs,
                   unsigned k, const float* m32, const void* operands);
 
+// Pinned staging slots and device slots of the context's operand ring.
+static int tc_ring_init(qsg_ctx* ctx) {
+  constexpr size_t kSlot = (tc::kOperandBytes + 1023) & ~size_t(1023);
+  if (ctx->tc_ring_dev) return QSG_OK;
+  void* d = nullptr;
+  void* h = nullptr;
+  QSG_CUDA(cudaMalloc(&d, kSlot * qsg_ctx::kTcRingSlots));
+  QSG_CUDA(cudaMallocHost(&h, kSlot * qsg_ctx::kTcRingSlots));
+  ctx->tc_ring_dev = static_cast<unsigned char*>(d);
+  ctx->tc_ring_host = static_cast<unsigned char*>(h);
+  for (int i = 0; i < qsg_ctx::kTcRingSlots; ++i)
+    QSG_CUDA(cudaEventCreateWithFlags(&ctx->tc_ring_ev[i],
+                                      cudaEventDisableTiming));
+  return QSG_OK;
+}
+
 int apply_gate_tc_host(qsg_ctx* ctx, float* state, unsigned n,
                        const unsigned* qs, unsigned k, const float* m32) {
   using namespace tc;
   constexpr size_t kSlot = (kOperandBytes + 1023) & ~size_t(1023);
-  if (!ctx->tc_ring_dev) {
-    void* d = nullptr;
-    void* h = nullptr;
-    QSG_CUDA(cudaMalloc(&d, kSlot * qsg_ctx::kTcRingSlots));
-    QSG_CUDA(cudaMallocHost(&h, kSlot * qsg_ctx::kTcRingSlots));
-    ctx->tc_ring_dev = static_cast<unsigned char*>(d);
-    ctx->tc_ring_host = static_cast<unsigned char*>(h);
-    for (int i = 0; i < qsg_ctx::kTcRingSlots; ++i)
-      QSG_CUDA(cudaEventCreateWithFlags(&ctx->tc_ring_ev[i],
-                                        cudaEventDisableTiming));
-  }
+  int rc = tc_ring_init(ctx);
+  if (rc) return rc;
   unsigned qs6[6];
   std::vector<float> m6;
   pad_to_6(n, qs, k, m32, qs6, m6);
@@ -945,6 +1568,9 @@ int tc_setup() {
     QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate_kernel,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(tc::kSmemBytes)));
+    QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate2_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(tc::kSmemBytes2)));
   }
   return QSG_OK;
 }
@@ -1008,6 +1634,90 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
   return QSG_OK;
 }
 
+// Two padded 6-qubit gates (sorted targets qa6, qb6; device operands opa,
+// opb) in one pass; the second gate is applied after the first.
+int apply_gate_tc2_carry(qsg_ctx* ctx, float* state, unsigned n,
+                         const unsigned* qa6, const void* opa,
+                         const unsigned* qb6, const void* opb,
+                         const double* prev, unsigned prev_count,
+                         double* out) {
+  using namespace tc;
+  Tc2Args a;
+  if (!plan_tc2(n, qa6, qb6, a.ga, a.gb)) {
+    set_error("two-gate tensor-core pass: targets do not fit one 12-qubit "
+              "tile (n = %u)", n);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  if (!opa || !opb) {
+    set_error("tensor-core gate without device operands");
+    return QSG_ERR_INVALID;
+  }
+  a.opa = static_cast<const float2*>(opa);
+  a.opb = static_cast<const float2*>(opb);
+  const int e = std::min(int(n / 2), 14);
+  a.scale = std::ldexp(1.0f, e);
+  a.inv_scale = std::ldexp(1.0f, -e);
+  int rc0 = tc_setup();
+  if (rc0) return rc0;
+  a.error = g_tc_err;
+  a.prev = prev;
+  a.prev_count = prev ? prev_count : 0;
+  a.out = out;
+  a.wait_cycles = g_tc_wait_cycles;
+  const uint64_t grid = std::min<uint64_t>(a.ga.num_tiles, ctx->num_sms);
+  tc_gate2_kernel<<<unsigned(grid), kThreads, kSmemBytes2, ctx->stream>>>(
+      reinterpret_cast<float2*>(state), a);
+  QSG_LAUNCHED(ctx);
+  return QSG_OK;
+}
+
+// Run bits b of the two-gate tile of two padded 6-qubit gates (tile bits
+// 0..b-1 are state bits 0..b-1, i.e. 2^b contiguous amplitudes per row of
+// the tile), or -1 if the pair does not fit a two-gate pass.
+int tc2_run_bits(unsigned n, const unsigned* qa6, const unsigned* qb6) {
+  tc::TcGeom ga, gb;
+  if (!tc::plan_tc2(n, qa6, qb6, ga, gb)) return -1;
+  return int(ga.b);
+}
+
+// Test entry of the two-gate pass: pads both host matrices to 6 targets,
+// uploads them through the context's operand ring and launches.
+int apply_gate_tc2_host(qsg_ctx* ctx, float* state, unsigned n,
+                        const unsigned* qa, unsigned ka, const float* ma,
+                        const unsigned* qb, unsigned kb, const float* mb) {
+  using namespace tc;
+  constexpr size_t kSlot = (kOperandBytes + 1023) & ~size_t(1023);
+  unsigned qa6[6], qb6[6];
+  std::vector<float> ma6, mb6;
+  pad_to_6(n, qa, ka, ma, qa6, ma6);
+  pad_to_6(n, qb, kb, mb, qb6, mb6);
+  if (tc2_run_bits(n, qa6, qb6) < 1) {
+    set_error("two-gate tensor-core pass: the padded targets of the two "
+              "gates span more than 12 qubits, or a 12-qubit tile of them "
+              "does not start at qubit 0");
+    return QSG_ERR_UNSUPPORTED;
+  }
+  int rc = tc_ring_init(ctx);
+  if (rc) return rc;
+  unsigned char* dev[2];
+  const std::vector<float>* src[2] = {&ma6, &mb6};
+  for (int gi = 0; gi < 2; ++gi) {
+    const int slot = ctx->tc_ring_next;
+    ctx->tc_ring_next = (slot + 1) % qsg_ctx::kTcRingSlots;
+    if (ctx->tc_ring_used[slot])
+      QSG_CUDA(cudaEventSynchronize(ctx->tc_ring_ev[slot]));
+    unsigned char* h = ctx->tc_ring_host + slot * kSlot;
+    dev[gi] = ctx->tc_ring_dev + slot * kSlot;
+    std::memcpy(h, src[gi]->data(), kOperandBytes);
+    QSG_CUDA(cudaMemcpyAsync(dev[gi], h, kOperandBytes, cudaMemcpyHostToDevice,
+                             ctx->stream));
+    QSG_CUDA(cudaEventRecord(ctx->tc_ring_ev[slot], ctx->stream));
+    ctx->tc_ring_used[slot] = true;
+  }
+  return apply_gate_tc2_carry(ctx, state, n, qa6, dev[0], qb6, dev[1],
+                              nullptr, 0, nullptr);
+}
+
 // Reads and clears the tensor-core kernels' error flag (1 = a bounded wait
 // gave up).
 int tc_check_error(qsg_ctx* ctx, int* out) {
@@ -1042,6 +1752,23 @@ int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
   // Operands built on the host and uploaded through the context's ring
   // (asynchronous; the call does not wait for the stream).
   return apply_gate_tc_host(ctx, state, n, qs, k, matrix);
+}
+
+int qsg_apply_gate_tc2(qsg_ctx* ctx, float* state, unsigned n,
+                       const unsigned* qa, unsigned ka, const float* ma,
+                       const unsigned* qb, unsigned kb, const float* mb) {
+  QSG_CHECK_ARG(ctx && state && ma && mb, "qsg_apply_gate_tc2: null argument");
+  if (ka > 6 || kb > 6) {
+    set_error("gates on more than 6 qubits are not supported");
+    return QSG_ERR_UNSUPPORTED;
+  }
+  QSG_CHECK_ARG(valid_qubits(qa, ka, n) && valid_qubits(qb, kb, n),
+                "qsg_apply_gate_tc2: bad qubits");
+  if (n < unsigned(tc::kTileBits)) {
+    set_error("tensor-core path needs n >= %d qubits", tc::kTileBits);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  return apply_gate_tc2_host(ctx, state, n, qa, ka, ma, qb, kb, mb);
 }
 
 int qsg_tc_error(qsg_ctx* ctx, int* out) {

@@ -178,3 +178,70 @@ def test_tc_bounded_wait_runs_out_and_context_recovers(eng, oracle, n):
     assert rel_l2(ss.to_numpy(st), ref) <= 1e-5
     # Out-of-range budgets are argument errors, not launches.
     assert N.lib.qsg_tc_stall_test(ctx.h, st.get(), n, C.c_longlong(10)) == 1
+
+
+def apply_tc2(N, ctx, st, n, qa, ma, qb, mb):
+    a32 = np.ascontiguousarray(ma.astype(np.complex64)).view(np.float32)
+    b32 = np.ascontiguousarray(mb.astype(np.complex64)).view(np.float32)
+    return N.lib.qsg_apply_gate_tc2(ctx.h, st.get(), n, N.u32_array(qa), len(qa),
+                                    a32.ctypes.data_as(N.P_f32), N.u32_array(qb),
+                                    len(qb), b32.ctypes.data_as(N.P_f32))
+
+
+def tc2_cases(rng, n):
+    """Pairs of target sets: disjoint, interleaved, equal, partly shared,
+    high qubits, padded (k < 6) and random subsets of 12 qubits that
+    include qubit 0."""
+    cases = [([0, 1, 2, 3, 4, 5], [6, 7, 8, 9, 10, 11]),
+             ([0, 2, 4, 6, 8, 10], [1, 3, 5, 7, 9, 11]),
+             ([3, 4, 5, 6, 7, 8], [3, 4, 5, 6, 7, 8]),
+             ([0, 1, 2, 3, 4, 5], [3, 4, 5, 6, 7, 8]),
+             (list(range(n - 6, n)), [0, 1, 2] + list(range(n - 3, n))),
+             ([0, n - 1], [1, 5, n - 2]),
+             ([2, n - 4, n - 3, n - 2, n - 1], [0, 1, n - 6, n - 5, n - 4])]
+    for _ in range(4):
+        pool = [0] + rng.choice(np.arange(1, n), 11, replace=False).tolist()
+        a = sorted(rng.choice(pool, 6, replace=False).tolist())
+        b = sorted(rng.choice(pool, 6, replace=False).tolist())
+        cases.append((a, b))
+    return cases
+
+
+@pytest.mark.parametrize("n", [12, 13, 16, 22])
+def test_tc2_pairs_match_oracle(eng, oracle, n):
+    """Two gates in one tensor-core pass equal the two gates applied one
+    after the other in FP64 (relative L2 <= 1e-5, the one-gate bar), for
+    tiles of 1 tile per CTA (n <= 16) up to many (n = 22: 1024 tiles)."""
+    q, E, N, ctx, ss, sim = eng
+    rng = np.random.default_rng(90 + n)
+    s0 = random_state(rng, n)
+    st = ss.Create(n)
+    for qa, qb in tc2_cases(rng, n):
+        ma = random_unitary(rng, len(qa))
+        mb = random_unitary(rng, len(qb))
+        ref = s0.copy()
+        oracle.apply_gate(ref, n, qa, ma)
+        oracle.apply_gate(ref, n, qb, mb)
+        ss.from_numpy(s0, st)
+        N.check(apply_tc2(N, ctx, st, n, qa, ma, qb, mb))
+        assert rel_l2(ss.to_numpy(st), ref) < 1e-5, (qa, qb)
+    assert tc_error(N, ctx) == 0
+
+
+def test_tc2_rejects_pairs_that_do_not_fit(eng):
+    """Two 6-qubit gates on 12 distinct qubits none of which is qubit 0
+    leave no tile that starts at qubit 0: refused before any launch (the
+    state is left as it was)."""
+    q, E, N, ctx, ss, sim = eng
+    n = 16
+    rng = np.random.default_rng(2)
+    s0 = random_state(rng, n)
+    st = ss.Create(n)
+    ss.from_numpy(s0, st)
+    m = random_unitary(rng, 6)
+    rc = apply_tc2(N, ctx, st, n, [1, 2, 3, 4, 5, 6], m,
+                   [7, 8, 9, 10, 11, 12], m)
+    assert rc == 4, N.lib.qsg_last_error()         # QSG_ERR_UNSUPPORTED
+    assert b"qubit 0" in N.lib.qsg_last_error()
+    assert np.array_equal(ss.to_numpy(st), s0.astype(np.complex64))
+    assert tc_error(N, ctx) == 0
