@@ -311,6 +311,12 @@ typedef struct qsg_fuse_options {
   int tensor_path;          /* route blocks of >= tc_min_k qubits to tcgen05 */
   unsigned tc_min_k;        /* 0: default 5 */
   const void* cost_model;   /* a qsg_mlp* (NULL: gate-count rule) */
+  /* Two-gate tensor-core passes (qsg_apply_gate_tc2): consecutive
+   * tensor-core blocks share one pass over the state when their 12-qubit
+   * tile has at least this many run bits (low qubits 0..b-1 in the tile);
+   * the most such pairs are taken, and plans are compared by passes.
+   * 0: one pass per block.  No counterpart in the reference. */
+  unsigned tc_pair_bits;
 } qsg_fuse_options;
 int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* opts,
                     qsg_plan** out);
@@ -319,6 +325,11 @@ int qsg_plan_create_unfused(const qsg_circuit* c, qsg_plan** out);
 int qsg_plan_destroy(qsg_plan* p);
 int qsg_plan_info(const qsg_plan* p, uint64_t* num_ops, unsigned* max_k,
                   uint64_t* num_tensor_ops);
+/* Two-gate tensor-core passes of the plan (qsg_fuse_options.tc_pair_bits),
+ * and per op whether it starts one (pair_next[i] = 1 for the first op of a
+ * pair; may be NULL, else num_ops entries). */
+int qsg_plan_tc_pairs(const qsg_plan* p, uint64_t* num_pairs,
+                      unsigned char* pair_next);
 int qsg_plan_get_op(const qsg_plan* p, uint64_t i, int* kind, unsigned* k,
                     unsigned* qs, unsigned* nc, unsigned* cqs,
                     uint64_t* cvals, int* path, uint64_t* num_members,

@@ -105,6 +105,7 @@ SIGNATURES = {
     "qsg_plan_create_unfused": (i32, [vp, C.POINTER(vp)]),
     "qsg_plan_destroy": (i32, [vp]),
     "qsg_plan_info": (i32, [vp, P_u64, P_u32, P_u64]),
+    "qsg_plan_tc_pairs": (i32, [vp, P_u64, C.POINTER(C.c_ubyte)]),
     "qsg_plan_get_op": (i32, [vp, u64, C.POINTER(C.c_int), P_u32, P_u32,
                               P_u32, P_u32, P_u64, C.POINTER(C.c_int), P_u64,
                               P_f64]),
@@ -181,7 +182,7 @@ class FuseOptions(C.Structure):
     """qsg_fuse_options."""
     _fields_ = [("max_fused_size", C.c_uint), ("seeds", C.c_uint),
                 ("tensor_path", C.c_int), ("tc_min_k", C.c_uint),
-                ("cost_model", C.c_void_p)]
+                ("cost_model", C.c_void_p), ("tc_pair_bits", C.c_uint)]
 
 
 class HybridOptions(C.Structure):

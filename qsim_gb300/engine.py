@@ -197,21 +197,23 @@ class PlanCache:
         self._ctxs = []   # device buffers of cached plans belong to these
 
     @staticmethod
-    def _opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model):
+    def _opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model,
+              tc_pairs=0):
         if cost_model is not None and hasattr(cost_model, "h"):
             cost_model = cost_model.h.value
         return N.FuseOptions(max_fused_size, seeds, int(tensor_path), tc_min_k,
-                             cost_model)
+                             cost_model, tc_pairs)
 
     def run(self, ctx, circuit, state, seed: int = 1, max_meas: int = 1024,
             max_fused_size: int = 4, tensor_path: bool = False,
             tc_min_k: int = 5, seeds: int = 0, cost_model=None,
-            maxtime: int = 0xFFFFFFFF):
+            maxtime: int = 0xFFFFFFFF, tc_pairs: int = 0):
         """QSimRunner::Run of `circuit` (a Circuit, or qsim text as str) on
         `state`; returns (measured bits, hit)."""
         if not any(c is ctx for c in self._ctxs):
             self._ctxs.append(ctx)
-        o = self._opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model)
+        o = self._opts(max_fused_size, tensor_path, tc_min_k, seeds, cost_model,
+                       tc_pairs)
         bits = np.zeros(max_meas, dtype=np.uint64)
         nm, hit = C.c_uint64(), C.c_int()
         if isinstance(circuit, str):
@@ -247,7 +249,9 @@ class Plan:
 
     def __init__(self, circuit: Circuit, max_fused_size: int = 4,
                  tensor_path: bool = False, tc_min_k: int = 5, seeds: int = 0,
-                 cost_model=None, unfused: bool = False):
+                 cost_model=None, unfused: bool = False, tc_pairs: int = 0):
+        """tc_pairs: minimum run bits of two-gate tensor-core passes (0: one
+        pass per block; 3 is where a pair measured faster than two passes)."""
         self.circuit = circuit
         h = C.c_void_p()
         if unfused:
@@ -256,14 +260,25 @@ class Plan:
             if cost_model is not None and hasattr(cost_model, "h"):
                 cost_model = cost_model.h.value   # a learned.CostMLP
             o = N.FuseOptions(max_fused_size, seeds, int(tensor_path), tc_min_k,
-                              cost_model)
+                              cost_model, tc_pairs)
             check(N.lib.qsg_plan_create(circuit.h, C.byref(o), C.byref(h)))
         self.h = h
 
     def info(self):
         n, k, t = C.c_uint64(), C.c_uint(), C.c_uint64()
         check(N.lib.qsg_plan_info(self.h, C.byref(n), C.byref(k), C.byref(t)))
-        return dict(num_ops=n.value, max_k=k.value, num_tensor_ops=t.value)
+        pairs = C.c_uint64()
+        check(N.lib.qsg_plan_tc_pairs(self.h, C.byref(pairs), None))
+        return dict(num_ops=n.value, max_k=k.value, num_tensor_ops=t.value,
+                    num_tc_pairs=pairs.value)
+
+    def tc_pair_next(self) -> np.ndarray:
+        """Per op: 1 if it starts a two-gate tensor-core pass."""
+        n = self.info()["num_ops"]
+        out = np.zeros(max(1, n), dtype=np.uint8)
+        check(N.lib.qsg_plan_tc_pairs(self.h, None,
+                                      out.ctypes.data_as(C.POINTER(C.c_ubyte))))
+        return out[:n]
 
     def __len__(self):
         return self.info()["num_ops"]

@@ -33,6 +33,7 @@ bool fuse_options_from(const qsg_fuse_options* o, FuseOptions* out) {
     fo.seeds = o->seeds ? o->seeds : fo.seeds;
     fo.tensor_path = o->tensor_path != 0;
     fo.tc_min_k = o->tc_min_k ? o->tc_min_k : fo.tc_min_k;
+    fo.tc_pair_bits = o->tc_pair_bits;
     fo.cost = qsg::cost_model_from_handle(o->cost_model);
   }
   *out = fo;
@@ -319,6 +320,19 @@ int qsg_plan_info(const qsg_plan* p, uint64_t* num_ops, unsigned* max_k,
     for (const auto& op : p->rt.plan.ops) t += op.path == Path::kTensor;
     *num_tensor_ops = t;
   }
+  return QSG_OK;
+}
+
+int qsg_plan_tc_pairs(const qsg_plan* p, uint64_t* num_pairs,
+                      unsigned char* pair_next) {
+  if (!p) return invalid("null plan");
+  uint64_t t = 0;
+  const auto& ops = p->rt.plan.ops;
+  for (size_t i = 0; i < ops.size(); ++i) {
+    t += ops[i].tc_pair_next;
+    if (pair_next) pair_next[i] = ops[i].tc_pair_next ? 1 : 0;
+  }
+  if (num_pairs) *num_pairs = t;
   return QSG_OK;
 }
 

@@ -100,6 +100,9 @@ struct PlanOp {
   std::vector<float> m32;       // interleaved FP32 copy used for launches
   std::vector<int> members;     // indices of the circuit ops it contains
   Path path = Path::kCudaCore;
+  // Tensor-core ops only: this op and the next one run as one two-gate
+  // tensor-core pass (one read and one write of the state).
+  bool tc_pair_next = false;
 };
 
 struct Plan {
@@ -121,7 +124,19 @@ struct FuseOptions {
   bool tensor_path = false;     // route k >= tc_min_k blocks to tcgen05
   unsigned tc_min_k = 5;
   const CostModel* cost = nullptr;  // null: maximise gates per block
+  // Two-gate tensor-core passes: consecutive tensor-core blocks whose
+  // 12-qubit tile has at least this many run bits (contiguous low qubits)
+  // share one pass; 0: one pass per block.
+  unsigned tc_pair_bits = 0;
 };
+
+// Measured cost of a two-gate tensor-core pass relative to the two one-gate
+// passes it replaces (0.89 - 0.92 on GB300 at >= 3 run bits, 30 qubits).
+constexpr double kTcPairCostFactor = 0.9;
+// Marks pairs of consecutive tensor-core ops (tc_pair_next) that fit a
+// two-gate pass with >= `bits` run bits, the most pairs possible; returns
+// their number.
+size_t pair_tensor_ops(Plan& plan, unsigned bits);
 
 Plan fuse(const Circuit& c, const FuseOptions& opt);
 // Unfused plan: one plan op per circuit op (matrices as given).

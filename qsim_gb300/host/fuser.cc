@@ -24,6 +24,12 @@
 #include "engine.h"
 
 namespace qsg {
+// Run bits of the two-gate tensor-core tile of two padded 6-qubit gates, or
+// -1 if they cannot share a pass (tc_gate.cu).
+int tc2_run_bits(unsigned n, const unsigned* qa6, const unsigned* qb6);
+}
+
+namespace qsg {
 namespace host {
 
 unsigned Plan::max_k() const {
@@ -389,13 +395,30 @@ Plan fuse_greedy(const Circuit& c, const FuseOptions& opt, unsigned f,
   return plan;
 }
 
+// Predicted time of a plan; a two-gate tensor-core pass costs
+// kTcPairCostFactor of its two blocks' one-gate passes.
 double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
   double t = 0;
-  for (const auto& op : p.ops) {
+  for (size_t i = 0; i < p.ops.size(); ++i) {
+    const auto& op = p.ops[i];
     if (op.kind == OpKind::kMeasure) continue;
-    t += m.cost_us(c.num_qubits, op.qs, unsigned(op.cqs.size()), op.path);
+    double ti = m.cost_us(c.num_qubits, op.qs, unsigned(op.cqs.size()), op.path);
+    if (op.tc_pair_next) {
+      const auto& nx = p.ops[i + 1];
+      ti += m.cost_us(c.num_qubits, nx.qs, unsigned(nx.cqs.size()), nx.path);
+      ti *= kTcPairCostFactor;
+      ++i;
+    }
+    t += ti;
   }
   return t;
+}
+
+// Passes over the state: ops minus the ones that share a two-gate pass.
+size_t plan_passes(const Plan& p) {
+  size_t n = 0;
+  for (const auto& op : p.ops) n += op.kind != OpKind::kMeasure && !op.tc_pair_next;
+  return n;
 }
 
 }  // namespace
@@ -485,6 +508,65 @@ Plan restore_lone_controlled(const Circuit& c, Plan p) {
 // windows of 3 and 4 gates give 36 blocks, 12 gives 37, 5 gives 41).
 constexpr unsigned kStartWindows[] = {2, 3, 4, 6, 8};
 
+namespace {
+
+// Run bits of the 12-qubit tile of two sorted 6-qubit target sets (their
+// union completed with the lowest other qubits; tile bits 0..b-1 are
+// qubits 0..b-1), without the kernel geometry: a quick filter before
+// tc2_run_bits, which also builds the geometry and its swizzles.
+int tile_run_bits(unsigned n, const std::vector<unsigned>& a,
+                  const std::vector<unsigned>& b) {
+  uint64_t u = 0;
+  for (unsigned q : a) u |= uint64_t{1} << q;
+  for (unsigned q : b) u |= uint64_t{1} << q;
+  int cnt = __builtin_popcountll(u);
+  if (cnt > 12) return -1;
+  for (unsigned q = 0; cnt < 12 && q < n; ++q)
+    if (!((u >> q) & 1)) {
+      u |= uint64_t{1} << q;
+      ++cnt;
+    }
+  int run = 0;
+  while (run < 64 && ((u >> run) & 1)) ++run;
+  return run;
+}
+
+}  // namespace
+
+size_t pair_tensor_ops(Plan& plan, unsigned bits) {
+  const size_t n = plan.ops.size();
+  for (auto& op : plan.ops) op.tc_pair_next = false;
+  if (bits == 0 || n < 2) return 0;
+  auto tensor6 = [&](const PlanOp& op) {
+    return op.kind == OpKind::kGate && op.path == Path::kTensor &&
+           op.qs.size() == 6 && op.cqs.empty();
+  };
+  // ok[i]: ops i, i + 1 fit one pass.  best[i]: most pairs among ops >= i.
+  std::vector<char> ok(n, 0);
+  for (size_t i = 0; i + 1 < n; ++i)
+    ok[i] = tensor6(plan.ops[i]) && tensor6(plan.ops[i + 1]) &&
+            tile_run_bits(plan.num_qubits, plan.ops[i].qs,
+                          plan.ops[i + 1].qs) >= int(bits) &&
+            tc2_run_bits(plan.num_qubits, plan.ops[i].qs.data(),
+                         plan.ops[i + 1].qs.data()) >= int(bits);
+  std::vector<size_t> best(n + 2, 0);
+  for (size_t i = n; i-- > 0;) {
+    best[i] = best[i + 1];
+    if (ok[i]) best[i] = std::max(best[i], 1 + best[i + 2]);
+  }
+  size_t pairs = 0;
+  for (size_t i = 0; i < n;) {
+    if (ok[i] && 1 + best[i + 2] >= best[i + 1]) {
+      plan.ops[i].tc_pair_next = true;
+      ++pairs;
+      i += 2;
+    } else {
+      ++i;
+    }
+  }
+  return pairs;
+}
+
 Plan fuse(const Circuit& c, const FuseOptions& opt) {
   const unsigned f = std::max(1u, std::min(6u, opt.max_fused_size));
   if (!opt.cost) {
@@ -499,20 +581,24 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
     // std::async futures carry a worker's exception (bad_alloc, say) to
     // get() on this thread, and their destructors wait for the worker, so
     // an exception here never leaves a joinable thread behind.
+    // With two-gate passes the count is of passes (pairs count once).
     std::vector<Plan> plans(windows.size());
     std::vector<std::future<Plan>> pool;
     for (size_t i = 1; i < windows.size(); ++i) {
       pool.push_back(std::async(std::launch::async, [&, i] {
         FuseOptions o = opt;
         o.seeds = windows[i];
-        return fuse_greedy(c, o, f, false);
+        Plan p = fuse_greedy(c, o, f, false);
+        pair_tensor_ops(p, opt.tc_pair_bits);
+        return p;
       }));
     }
     plans[0] = fuse_greedy(c, opt, f, false);
+    pair_tensor_ops(plans[0], opt.tc_pair_bits);
     for (size_t i = 1; i < windows.size(); ++i) plans[i] = pool[i - 1].get();
     size_t best = 0;
     for (size_t i = 1; i < plans.size(); ++i)
-      if (plans[i].ops.size() < plans[best].ops.size()) best = i;
+      if (plan_passes(plans[i]) < plan_passes(plans[best])) best = i;
     return std::move(plans[best]);
   }
   // Learned planner: candidate plans for every block-size limit up to f,
@@ -559,6 +645,7 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
       o.seeds = cd.w;
       Plan p = fuse_greedy(cc, o, cd.ff, cd.pg != 0);
       if (cd.expand) p = restore_lone_controlled(c, std::move(p));
+      if (opt.tensor_path) pair_tensor_ops(p, opt.tc_pair_bits);
       const double t = plan_cost(c, p, *opt.cost);
       return std::make_pair(std::move(p), t);
     }));

@@ -50,6 +50,7 @@ void put_options(std::string* s, const FuseOptions& fo) {
   put(s, fo.seeds);
   put(s, uint8_t(fo.tensor_path));
   put(s, fo.tc_min_k);
+  put(s, fo.tc_pair_bits);
   // A cost model is keyed by its identity: a model changed in place (more
   // training) needs qsg_plan_cache_clear.
   put(s, reinterpret_cast<uintptr_t>(fo.cost));

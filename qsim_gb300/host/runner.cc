@@ -165,6 +165,10 @@ int PlanRuntime::launch_op(size_t i, float* state) {
   const float* dm = (dmat && dmat_off[i] != size_t(-1)) ? dmat + dmat_off[i]
                                                         : nullptr;
   if (op.kind == OpKind::kGate && op.path == Path::kTensor) {
+    if (op.tc_pair_next)
+      return apply_gate_tc2_carry(ctx, state, n, op.qs.data(), tc_operands(i),
+                                  plan.ops[i + 1].qs.data(),
+                                  tc_operands(i + 1), nullptr, 0, nullptr);
     return apply_gate_tc(ctx, state, n, op.qs.data(), op.qs.size(),
                          op.m32.data(), tc_operands(i));
   }
@@ -188,9 +192,15 @@ int PlanRuntime::launch_all(float* state) {
     int rc;
     if (restore_norm && op.kind == OpKind::kGate && op.path == Path::kTensor) {
       double* out = norm_buf + which * half;
-      rc = apply_gate_tc_carry(ctx, state, n, op.qs.data(), op.qs.size(),
-                               op.m32.data(), tc_operands(i), prev, prev_count,
-                               out);
+      if (op.tc_pair_next) {
+        rc = apply_gate_tc2_carry(ctx, state, n, op.qs.data(), tc_operands(i),
+                                  plan.ops[i + 1].qs.data(),
+                                  tc_operands(i + 1), prev, prev_count, out);
+      } else {
+        rc = apply_gate_tc_carry(ctx, state, n, op.qs.data(), op.qs.size(),
+                                 op.m32.data(), tc_operands(i), prev,
+                                 prev_count, out);
+      }
       prev = out;
       prev_count = tc_grid(ctx, n);
       which ^= 1;
@@ -198,6 +208,7 @@ int PlanRuntime::launch_all(float* state) {
       rc = launch_op(i, state);
     }
     if (rc) return rc;
+    if (op.tc_pair_next) ++i;
   }
   return QSG_OK;
 }
@@ -227,6 +238,7 @@ int PlanRuntime::run(qsg_ctx* c, float* state, unsigned seed,
     }
     rc = launch_op(i, state);
     if (rc) return rc;
+    if (op.tc_pair_next) ++i;
   }
   return QSG_OK;
 }
@@ -303,6 +315,11 @@ int PlanRuntime::profile(qsg_ctx* c, float* state, std::vector<float>* ms) {
       if (rc) break;
     }
     cudaEventRecord(ev[i + 1], s);
+    if (plan.ops[i].tc_pair_next) {
+      // The pair's time is op i's; op i + 1 gets 0.
+      cudaEventRecord(ev[i + 2], s);
+      ++i;
+    }
   }
   cudaEventSynchronize(ev[nops]);
   ms->assign(nops, 0.f);

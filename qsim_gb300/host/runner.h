@@ -21,6 +21,14 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
                         const unsigned* qs, unsigned k, const float* m32,
                         const void* operands, const double* prev,
                         unsigned prev_count, double* out);
+// Two padded 6-qubit gates (sorted targets qa6 then qb6, device operands
+// opa, opb) in one tensor-core pass, with the norm carry as above (sums of
+// the first gate's input and the second gate's output).
+int apply_gate_tc2_carry(qsg_ctx* ctx, float* state, unsigned n,
+                         const unsigned* qa6, const void* opa,
+                         const unsigned* qb6, const void* opb,
+                         const double* prev, unsigned prev_count,
+                         double* out);
 // CTAs of a tensor-core pass on n qubits.
 unsigned tc_grid(qsg_ctx* ctx, unsigned n);
 // A gate given as a host matrix (k <= 6, n >= 12) on the tensor cores, its
@@ -71,6 +79,8 @@ struct PlanRuntime {
   int upload(qsg_ctx* ctx);
   int prepare_tc();
   const void* tc_operands(size_t i) const;
+  // Launches op i, and op i + 1 with it when op i starts a two-gate
+  // tensor-core pass (plan.ops[i].tc_pair_next).
   int launch_op(size_t i, float* state);
   // Every gate op in order (with the norm restoration); no measurements.
   int launch_all(float* state);
@@ -79,7 +89,8 @@ struct PlanRuntime {
           std::vector<uint64_t>* mbits);
   int capture(qsg_ctx* ctx, float* state);
   // Runs the gate ops with a CUDA event around each; per-op milliseconds
-  // (measurements are skipped and get 0).
+  // (measurements are skipped and get 0; a two-gate tensor-core pass is
+  // timed as its first op, the second gets 0).
   int profile(qsg_ctx* ctx, float* state, std::vector<float>* ms);
   int replay(qsg_ctx* ctx);
 };

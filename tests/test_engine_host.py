@@ -219,3 +219,50 @@ def test_learned_plan_absorbs_controlled_gates_and_keeps_the_state(E, oracle):
     ctrl = lambda p: sum(1 for o in p.ops() if o["kind"] == 1)  # noqa: E731
     assert ctrl(learned) < ctrl(fixed)
     assert len(learned) < len(fixed)
+
+
+def run_bits(a, b):
+    """Run bits of the two-gate tile of two padded 6-qubit target sets: the
+    union completed with the lowest other qubits to 12, then the longest
+    prefix 0..b-1 it holds with the rest above b (-1 without qubit 0)."""
+    u = sorted(set(a) | set(b))
+    q = 0
+    while len(u) < 12:
+        if q not in u:
+            u.append(q)
+        q += 1
+    u.sort()
+    h = next(h for h in range(13) if sum(x >= 12 - h for x in u) == h)
+    return 12 - h if 12 - h >= 1 else -1
+
+
+@pytest.mark.parametrize("bits", [1, 3, 5])
+def test_two_gate_pass_pairing(E, bits):
+    """Pairs of consecutive tensor-core blocks marked for two-gate passes:
+    no op in two pairs, both ops 6-qubit tensor-core gates, their tile has
+    >= `bits` run bits, the most pairs possible (checked here by the same
+    recursion over the chain of consecutive ops), and no more passes over
+    the state than the plan chosen without pairs (the fixed planner
+    compares its candidate plans by passes)."""
+    c = E.Circuit.grid(5, 6, 0, 20, 1)
+    base = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5)
+    plan = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5,
+                  tc_pairs=bits)
+    pn = plan.tc_pair_next()
+    assert plan.info()["num_tc_pairs"] == int(pn.sum())
+    ops = plan.ops()
+    assert len(ops) - int(pn.sum()) <= len(base)
+    ok = [i + 1 < len(ops) and ops[i]["path"] == 1 and ops[i + 1]["path"] == 1
+          and len(ops[i]["qs"]) == 6 and len(ops[i + 1]["qs"]) == 6
+          and run_bits(ops[i]["qs"], ops[i + 1]["qs"]) >= bits
+          for i in range(len(ops))]
+    for i in np.flatnonzero(pn):
+        assert ok[i]
+        assert i + 1 < len(ops) and not pn[i + 1]
+    best = [0] * (len(ops) + 2)
+    for i in range(len(ops) - 1, -1, -1):
+        best[i] = max(best[i + 1], (1 + best[i + 2]) if ok[i] else 0)
+    assert int(pn.sum()) == best[0]
+    assert int(pn.sum()) > 0
+    assert E.Plan(c, max_fused_size=6, tensor_path=True,
+                  tc_min_k=5).info()["num_tc_pairs"] == 0

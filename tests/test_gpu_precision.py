@@ -78,7 +78,11 @@ def test_grid_circuit_forms_against_fp64(eng, oracle):
         "tc_f6_all": E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=1),
         "learned_tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True,
                                 tc_min_k=2, cost_model=L.CostMLP.load()),
+        "learned_tc_f6_pairs": E.Plan(c, max_fused_size=6, tensor_path=True,
+                                      tc_min_k=2, cost_model=L.CostMLP.load(),
+                                      tc_pairs=3),
     }
+    assert forms["learned_tc_f6_pairs"].info()["num_tc_pairs"] > 0
     st = ss.Create(n)
     out = {"workload": f"grid{rows}x{cols} ({n} qubits) depth 20, seed 1",
            "forms": {}}
@@ -97,10 +101,11 @@ def test_grid_circuit_forms_against_fp64(eng, oracle):
 def test_headline_circuit_30q_against_fp64(eng, oracle):
     """The 30-qubit 5x6 grid depth-20 circuit (seed 1) at its full size in
     every default run: the plain CUDA-core f = 4 plan, the split-FP16
-    tensor-core f = 6 plan (the form the headline time is measured on) and
-    the learned planner's plan, each against the FP64 oracle (one-qubit
-    gates folded into two-qubit gates in FP64, 16 GiB on the host).  Bar:
-    relative L2 <= 1e-5 and fidelity >= 1 - 1e-6."""
+    tensor-core f = 6 plan, the learned planner's plan and the same with
+    two-gate tensor-core passes (the form the headline time is measured
+    on), each against the FP64 oracle (one-qubit gates folded into
+    two-qubit gates in FP64, 16 GiB on the host).  Bar: relative L2 <= 1e-5
+    and fidelity >= 1 - 1e-6."""
     q, E, ctx, ss, sim = eng
     from qsim_gb300 import learned as L
     c = E.Circuit.grid(5, 6, 0, 20, 1)
@@ -111,6 +116,9 @@ def test_headline_circuit_30q_against_fp64(eng, oracle):
         "tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5),
         "learned_tc_f6": E.Plan(c, max_fused_size=6, tensor_path=True,
                                 tc_min_k=2, cost_model=L.CostMLP.load()),
+        "learned_tc_f6_pairs": E.Plan(c, max_fused_size=6, tensor_path=True,
+                                      tc_min_k=2, cost_model=L.CostMLP.load(),
+                                      tc_pairs=3),
     }
     st = ss.Create(n)
     out = {"workload": "grid5x6 (30 qubits) depth 20, seed 1", "forms": {}}

@@ -245,3 +245,43 @@ def test_tc2_rejects_pairs_that_do_not_fit(eng):
     assert b"qubit 0" in N.lib.qsg_last_error()
     assert np.array_equal(ss.to_numpy(st), s0.astype(np.complex64))
     assert tc_error(N, ctx) == 0
+
+
+@pytest.mark.parametrize("bits", [1, 3])
+def test_tc2_plans_match_oracle(eng, oracle, bits):
+    """Plans whose consecutive tensor-core blocks share two-gate passes
+    (every block on the tensor cores, pairs with >= `bits` run bits):
+    run, captured replay and per-op profile give the oracle's state, with
+    the norm carry across single and paired passes."""
+    q, E, N, ctx, ss, sim = eng
+    for c in (E.Circuit.grid(4, 4, 0, 16, 5), E.Circuit.grid(3, 6, 0, 14, 6)):
+        n = c.num_qubits
+        plan = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=1,
+                      tc_pairs=bits)
+        info = plan.info()
+        assert info["num_tc_pairs"] > 0
+        pn = plan.tc_pair_next()
+        assert pn.sum() == info["num_tc_pairs"]
+        assert not np.any(pn[:-1] & pn[1:])            # pairs do not overlap
+        want = oracle.zero_state(n)
+        for o in c.ops():
+            oracle.apply_gate(want, n, o["qs"], o["m"])
+        st = ss.Create(n)
+        ss.SetStateZero(st)
+        plan.run(ctx, st)
+        got = ss.to_numpy(st)
+        assert rel_l2(got, want) < 1e-5
+        assert abs(np.linalg.norm(got) - 1) < 1e-6
+        plan.capture(ctx, st)
+        ss.SetStateZero(st)
+        plan.replay(ctx)
+        ctx.sync()
+        assert rel_l2(ss.to_numpy(st), want) < 1e-5
+        ss.SetStateZero(st)
+        ms = np.asarray(plan.profile(ctx, st))
+        # Profiled runs launch op by op without the norm carry.
+        assert rel_l2(ss.to_numpy(st), want) < 5e-5
+        # A pair is timed as its first op; its second op's interval spans
+        # no launch (two events recorded back to back).
+        assert np.all(ms[1:][pn[:-1] == 1] < 0.02)
+    assert tc_error(N, ctx) == 0
