@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <future>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 #include <cstring>
@@ -50,10 +51,13 @@ std::vector<cplx> block_matrix_ops(const std::vector<const Op*>& ops,
                                    const std::vector<unsigned>& qs) {
   const unsigned k = qs.size();
   const unsigned d = 1u << k;
-  // Columns of the block matrix evolve as k-qubit states.
-  std::vector<cplx> m(size_t(d) * d, 0.0);
-  for (unsigned i = 0; i < d; ++i) m[i * d + i] = 1.0;
-  std::vector<cplx> tmp(d);
+  // Columns of the block matrix evolve as k-qubit states.  Real and
+  // imaginary parts are kept apart, so the update of a row runs along
+  // contiguous columns (vectorisable); every element gets the same sums in
+  // the same order as a complex column-by-column update.
+  std::vector<double> re(size_t(d) * d, 0.0), im(size_t(d) * d, 0.0);
+  for (unsigned i = 0; i < d; ++i) re[size_t(i) * d + i] = 1.0;
+  std::vector<double> tre(size_t(d) * d), tim(size_t(d) * d);
   for (const Op* opp : ops) {
     const Op& op = *opp;
     const unsigned gk = op.qs.size();
@@ -64,27 +68,40 @@ std::vector<cplx> block_matrix_ops(const std::vector<const Op*>& ops,
       pos[j] = unsigned(std::find(qs.begin(), qs.end(), op.qs[j]) - qs.begin());
       gmask |= 1u << pos[j];
     }
-    auto expand = [&](unsigned gi) {
+    unsigned off[64];
+    for (unsigned gi = 0; gi < gd; ++gi) {
       unsigned r = 0;
       for (unsigned j = 0; j < gk; ++j)
         if ((gi >> j) & 1) r |= 1u << pos[j];
-      return r;
-    };
-    for (unsigned col = 0; col < d; ++col) {
-      // Row-space update of column `col`: m[:, col] <- G m[:, col].
-      for (unsigned base = 0; base < d; ++base) {
-        if (base & gmask) continue;
-        cplx in[64];
-        for (unsigned gi = 0; gi < gd; ++gi) in[gi] = m[(base | expand(gi)) * d + col];
-        for (unsigned go = 0; go < gd; ++go) {
-          cplx acc = 0.0;
-          for (unsigned gi = 0; gi < gd; ++gi) acc += op.m[go * gd + gi] * in[gi];
-          tmp[go] = acc;
+      off[gi] = r;
+    }
+    const cplx* g = op.m.data();
+    for (unsigned base = 0; base < d; ++base) {
+      if (base & gmask) continue;
+      for (unsigned go = 0; go < gd; ++go) {
+        double* ar = &tre[size_t(go) * d];
+        double* ai = &tim[size_t(go) * d];
+        for (unsigned col = 0; col < d; ++col) ar[col] = ai[col] = 0.0;
+        for (unsigned gi = 0; gi < gd; ++gi) {
+          const double gr = g[go * gd + gi].real(), gm = g[go * gd + gi].imag();
+          const double* xr = &re[size_t(base | off[gi]) * d];
+          const double* xi = &im[size_t(base | off[gi]) * d];
+          for (unsigned col = 0; col < d; ++col) {
+            ar[col] += gr * xr[col] - gm * xi[col];
+            ai[col] += gr * xi[col] + gm * xr[col];
+          }
         }
-        for (unsigned go = 0; go < gd; ++go) m[(base | expand(go)) * d + col] = tmp[go];
+      }
+      for (unsigned go = 0; go < gd; ++go) {
+        std::memcpy(&re[size_t(base | off[go]) * d], &tre[size_t(go) * d],
+                    d * sizeof(double));
+        std::memcpy(&im[size_t(base | off[go]) * d], &tim[size_t(go) * d],
+                    d * sizeof(double));
       }
     }
   }
+  std::vector<cplx> m(size_t(d) * d);
+  for (size_t i = 0; i < m.size(); ++i) m[i] = cplx(re[i], im[i]);
   return m;
 }
 
@@ -126,28 +143,36 @@ struct Block {
 // popcount(mask | q) <= f, in scan order.
 constexpr size_t kCandWindow = 256;
 
-template <typename Fusible>
-size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
+// Per-op qubit masks (targets | controls) and fusibility of a circuit,
+// computed once per planning run.
+struct OpInfo {
+  std::vector<uint64_t> mask;
+  std::vector<char> fusible;
+};
+
+size_t absorb_scan(const OpInfo& info, const std::vector<char>& done,
                    std::vector<char>& in_block, size_t first, size_t end,
-                   uint64_t mask, unsigned f, Fusible&& fusible, bool commit,
+                   uint64_t mask, unsigned f, bool commit,
                    std::vector<int>* members, std::vector<size_t>* cands,
                    size_t max_cands) {
+  // The scan visits each op once, so a trial scan (commit false) needs no
+  // marks; a committed one marks its ops for the scans that follow.
   uint64_t blocked = 0;
   size_t absorbed = 0;
-  std::vector<size_t> taken;
   for (size_t i = first; i < end; ++i) {
-    if (done[i]) continue;
-    const Op& op = c.ops[i];
-    const uint64_t m = qmask(op.qs) | qmask(op.cqs);
-    if (in_block[i]) continue;
+    if (done[i] || in_block[i]) continue;
+    const uint64_t m = info.mask[i];
+    const bool fus = info.fusible[i] != 0;
     if (m & blocked) {
       blocked |= m;
-    } else if (fusible(op) && (m & ~mask) == 0) {
+    } else if (fus && (m & ~mask) == 0) {
       ++absorbed;
-      taken.push_back(i);
-      in_block[i] = 1;
+      if (commit) {
+        members->push_back(int(i));
+        in_block[i] = 1;
+      }
     } else {
-      if (cands && fusible(op) && cands->size() < max_cands &&
+      if (cands && fus && cands->size() < max_cands &&
           unsigned(__builtin_popcountll(mask | m)) <= f)
         cands->push_back(i);
       blocked |= m;
@@ -159,11 +184,6 @@ size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
         (!cands || cands->size() >= max_cands || i - first > kCandWindow))
       break;
   }
-  if (commit) {
-    for (size_t i : taken) members->push_back(int(i));
-  } else {
-    for (size_t i : taken) in_block[i] = 0;
-  }
   return absorbed;
 }
 
@@ -171,27 +191,37 @@ size_t absorb_scan(const Circuit& c, const std::vector<char>& done,
 // set, then expand the set by the candidate whose expanded set absorbs the
 // most ops (one-step lookahead), until the set has f qubits or no
 // candidate fits.
-template <typename Fusible>
-Block grow_block(const Circuit& c, const std::vector<char>& done, size_t first,
-                 size_t end, size_t seed, unsigned f, Fusible&& fusible) {
+Block grow_block(const Circuit& c, const OpInfo& info,
+                 const std::vector<char>& done, size_t first, size_t end,
+                 size_t seed, unsigned f) {
+  // All zero between calls: each call clears the marks it set (its
+  // members), also when it leaves by an exception.
   static thread_local std::vector<char> in_block;
-  in_block.assign(c.ops.size(), 0);
+  if (in_block.size() < c.ops.size()) in_block.assign(c.ops.size(), 0);
   Block b;
+  struct Unmark {
+    std::vector<char>& v;
+    const std::vector<int>& m;
+    ~Unmark() {
+      for (int i : m) v[size_t(i)] = 0;
+    }
+  } unmark{in_block, b.members};
   b.members.push_back(int(seed));
   in_block[seed] = 1;
   b.mask = qmask(c.ops[seed].qs);
   constexpr size_t kMaxCands = 12;
+  std::vector<size_t> cands;
   for (;;) {
-    std::vector<size_t> cands;
-    absorb_scan(c, done, in_block, first, end, b.mask, f, fusible, true,
+    cands.clear();
+    absorb_scan(info, done, in_block, first, end, b.mask, f, true,
                 &b.members, &cands, kMaxCands);
     if (unsigned(__builtin_popcountll(b.mask)) >= f || cands.empty()) break;
     size_t best = cands[0];
     long best_score = -1;
     for (size_t cand : cands) {
       const uint64_t m2 = b.mask | qmask(c.ops[cand].qs);
-      const size_t got = absorb_scan(c, done, in_block, first, end, m2, f,
-                                     fusible, false, nullptr, nullptr, 0);
+      const size_t got = absorb_scan(info, done, in_block, first, end, m2, f,
+                                     false, nullptr, nullptr, 0);
       // Prefer more absorbed ops, then fewer new qubits.
       const long score =
           long(got) * 8 - long(__builtin_popcountll(m2 & ~b.mask));
@@ -279,6 +309,13 @@ Plan fuse_greedy(const Circuit& c, const FuseOptions& opt, unsigned f,
   auto fusible = [&](const Op& op) {
     return op.kind == OpKind::kGate && op.qs.size() <= f;
   };
+  OpInfo info;
+  info.mask.resize(nops);
+  info.fusible.resize(nops);
+  for (size_t i = 0; i < nops; ++i) {
+    info.mask[i] = qmask(c.ops[i].qs) | qmask(c.ops[i].cqs);
+    info.fusible[i] = fusible(c.ops[i]) ? 1 : 0;
+  }
   // With a cost model: the cheaper path for a block (tensor cores only for
   // blocks of >= tc_min_k qubits on >= 12-qubit states) and its cost.
   auto cost_of = [&](const std::vector<unsigned>& qs, Path* path) {
@@ -347,7 +384,7 @@ Plan fuse_greedy(const Circuit& c, const FuseOptions& opt, unsigned f,
                                       1, unsigned(c.ops[seed].qs.size()))
                                 : f;
         for (unsigned lim = lo; lim <= f; ++lim) {
-          Block b = grow_block(c, done, first, seg_end, seed, lim, fusible);
+          Block b = grow_block(c, info, done, first, seg_end, seed, lim);
           std::vector<unsigned> qs;
           for (unsigned q = 0; q < c.num_qubits; ++q)
             if ((b.mask >> q) & 1) qs.push_back(q);
@@ -394,6 +431,46 @@ Plan fuse_greedy(const Circuit& c, const FuseOptions& opt, unsigned f,
   }
   return plan;
 }
+
+// A cost model's answers memoised by (qubit set, controls, path): the greedy
+// search prices the same blocks many times over.  Not thread-safe: one per
+// planning thread.
+class MemoCost : public CostModel {
+ public:
+  explicit MemoCost(const CostModel* m) : m_(m) {}
+  double cost_us(unsigned n, const std::vector<unsigned>& qs,
+                 unsigned ncontrols, Path path) const override {
+    uint64_t mask = 0;
+    bool sorted = n <= 64;
+    for (size_t i = 0; sorted && i < qs.size(); ++i) {
+      sorted = qs[i] < 64 && (i == 0 || qs[i - 1] < qs[i]);
+      if (sorted) mask |= uint64_t{1} << qs[i];
+    }
+    if (!sorted) return m_->cost_us(n, qs, ncontrols, path);
+    const Key k{mask, (uint64_t(n) << 40) | (uint64_t(ncontrols) << 8) |
+                          uint64_t(path == Path::kTensor)};
+    auto it = memo_.find(k);
+    if (it != memo_.end()) return it->second;
+    const double v = m_->cost_us(n, qs, ncontrols, path);
+    memo_.emplace(k, v);
+    return v;
+  }
+
+ private:
+  struct Key {
+    uint64_t mask, rest;
+    bool operator==(const Key& o) const {
+      return mask == o.mask && rest == o.rest;
+    }
+  };
+  struct KeyHash {
+    size_t operator()(const Key& k) const {
+      return size_t(k.mask * 0x9E3779B97F4A7C15ull ^ (k.rest + (k.rest << 17)));
+    }
+  };
+  const CostModel* m_;
+  mutable std::unordered_map<Key, double, KeyHash> memo_;
+};
 
 // Predicted time of a plan; a two-gate tensor-core pass costs
 // kTcPairCostFactor of its two blocks' one-gate passes.
@@ -641,12 +718,14 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
   for (const Cand& cd : cands) {
     const Circuit& cc = cd.expand ? expanded[cd.ff] : c;
     runs.push_back(std::async(std::launch::async, [&c, &cc, &opt, cd] {
+      MemoCost memo(opt.cost);   // one per candidate: no shared state
       FuseOptions o = opt;
       o.seeds = cd.w;
+      o.cost = &memo;
       Plan p = fuse_greedy(cc, o, cd.ff, cd.pg != 0);
       if (cd.expand) p = restore_lone_controlled(c, std::move(p));
       if (opt.tensor_path) pair_tensor_ops(p, opt.tc_pair_bits);
-      const double t = plan_cost(c, p, *opt.cost);
+      const double t = plan_cost(c, p, memo);
       return std::make_pair(std::move(p), t);
     }));
   }
