@@ -113,6 +113,27 @@ uint64_t qmask(const std::vector<unsigned>& qs) {
   return m;
 }
 
+// Run bits of the 12-qubit tile of two sorted 6-qubit target sets (their
+// union completed with the lowest other qubits; tile bits 0..b-1 are
+// qubits 0..b-1), without the kernel geometry: a quick filter before
+// tc2_run_bits, which also builds the geometry and its swizzles.
+int tile_run_bits(unsigned n, const std::vector<unsigned>& a,
+                  const std::vector<unsigned>& b) {
+  uint64_t u = 0;
+  for (unsigned q : a) u |= uint64_t{1} << q;
+  for (unsigned q : b) u |= uint64_t{1} << q;
+  int cnt = __builtin_popcountll(u);
+  if (cnt > 12) return -1;
+  for (unsigned q = 0; cnt < 12 && q < n; ++q)
+    if (!((u >> q) & 1)) {
+      u |= uint64_t{1} << q;
+      ++cnt;
+    }
+  int run = 0;
+  while (run < 64 && ((u >> run) & 1)) ++run;
+  return run;
+}
+
 void finish(const Circuit& c, PlanOp& p) {
   if (p.kind == OpKind::kGate) {
     if (p.members.size() == 1 && c.ops[p.members[0]].qs == p.qs) {
@@ -584,31 +605,6 @@ Plan restore_lone_controlled(const Circuit& c, Plan p) {
 // monotonic in the window (on the 30-qubit depth-20 grid circuit at f = 6,
 // windows of 3 and 4 gates give 36 blocks, 12 gives 37, 5 gives 41).
 constexpr unsigned kStartWindows[] = {2, 3, 4, 6, 8};
-
-namespace {
-
-// Run bits of the 12-qubit tile of two sorted 6-qubit target sets (their
-// union completed with the lowest other qubits; tile bits 0..b-1 are
-// qubits 0..b-1), without the kernel geometry: a quick filter before
-// tc2_run_bits, which also builds the geometry and its swizzles.
-int tile_run_bits(unsigned n, const std::vector<unsigned>& a,
-                  const std::vector<unsigned>& b) {
-  uint64_t u = 0;
-  for (unsigned q : a) u |= uint64_t{1} << q;
-  for (unsigned q : b) u |= uint64_t{1} << q;
-  int cnt = __builtin_popcountll(u);
-  if (cnt > 12) return -1;
-  for (unsigned q = 0; cnt < 12 && q < n; ++q)
-    if (!((u >> q) & 1)) {
-      u |= uint64_t{1} << q;
-      ++cnt;
-    }
-  int run = 0;
-  while (run < 64 && ((u >> run) & 1)) ++run;
-  return run;
-}
-
-}  // namespace
 
 size_t pair_tensor_ops(Plan& plan, unsigned bits) {
   const size_t n = plan.ops.size();
