@@ -211,12 +211,13 @@ int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
 int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
                       const unsigned* qs, unsigned k, const float* matrix);
 /* Two gates (k <= 6 targets each, A first) in one tensor-core pass over the
- * state, when their targets, each padded to 6 as in qsg_apply_gate_tc, span
- * at most 12 qubits and a 12-qubit tile of them starts at qubit 0
- * (QSG_ERR_UNSUPPORTED otherwise); n >= 12, |psi_i| <= 4.  The result is
- * that of two qsg_apply_gate_tc calls, with one read and one write of the
- * state instead of two.  No counterpart in the reference, which applies
- * fused gates one pass each (lib/simulator_cuda.h:333-380). */
+ * state; n >= 12, |psi_i| <= 4.  Their targets, each padded to 6 as in
+ * qsg_apply_gate_tc, must span fewer than 12 qubits or include qubit 0 (a
+ * 12-qubit tile of them starts at qubit 0; QSG_ERR_UNSUPPORTED otherwise);
+ * gates on the same six qubits run as one pass of their product.  The
+ * result is that of two qsg_apply_gate_tc calls, with one read and one
+ * write of the state instead of two.  No counterpart in the reference,
+ * which applies fused gates one pass each (lib/simulator_cuda.h:333-380). */
 int qsg_apply_gate_tc2(qsg_ctx* ctx, float* state, unsigned n,
                        const unsigned* qa, unsigned ka, const float* ma,
                        const unsigned* qb, unsigned kb, const float* mb);

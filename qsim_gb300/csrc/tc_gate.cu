@@ -881,42 +881,45 @@ static bool solve_swizzle(const std::vector<std::vector<unsigned>>& sets,
   return true;
 }
 
-// Member / group roles of the tile bits of a gate with sorted targets qs6
-// (the tile's bit -> state-bit map already set), and the swizzles of its
-// raw buffer and epilogue staging.
-static bool tc_roles(TcGeom& g, const unsigned* qs6) {
-  unsigned tslot = 0, gslot = 0;
+// Member / group roles of the tile bits: tord[m] is the tile bit of member
+// bit m, gord[k] the tile bit of group bit k (together all 12 tile bits,
+// the tile's bit -> state-bit map already set), and the swizzles of the raw
+// buffer (unless `raw` is false: a gate whose operand does not come from a
+// raw tile) and the epilogue staging for those roles.
+static bool tc_roles_ordered(TcGeom& g, const unsigned* tord,
+                             const unsigned* gord, bool raw = true) {
+  unsigned seen = 0;
   for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
-    const unsigned sb = unsigned(g.bitpos_state[j]);
-    const bool is_t = std::find(qs6, qs6 + kK, sb) != qs6 + kK;
-    g.tile_is_target[j] = is_t;
+    g.tile_is_target[j] = 0;
     g.target_slot[j] = 0;
     g.group_slot[j] = 0;
-    if (is_t) {
-      // member bit = index of this target in the sorted target list
-      g.target_slot[j] = unsigned(std::find(qs6, qs6 + kK, sb) - qs6);
-      ++tslot;
-    } else {
-      g.group_slot[j] = gslot++;
-    }
   }
-  if (tslot != unsigned(kK) || gslot != 6) return false;
-  unsigned gpos[6], tpos[6];
-  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
-    if (g.tile_is_target[j]) tpos[g.target_slot[j]] = j;
-    else gpos[g.group_slot[j]] = j;
+  for (unsigned m = 0; m < unsigned(kK); ++m) {
+    if (tord[m] >= unsigned(kTileBits) || gord[m] >= unsigned(kTileBits))
+      return false;
+    g.tile_is_target[tord[m]] = 1;
+    g.target_slot[tord[m]] = m;
+    g.group_slot[gord[m]] = m;
+    seen |= (1u << tord[m]) | (1u << gord[m]);
   }
+  if (seen != (1u << kTileBits) - 1) return false;
+  for (unsigned m = 0; m < unsigned(kK); ++m)
+    if (g.tile_is_target[gord[m]]) return false;
+  const unsigned* tpos = tord;
+  const unsigned* gpos = gord;
   // Epilogue writes: half-warp lanes vary member bits 0, 1 (lane / 4) and
   // group bits 1, 2 (lane % 4).
   if (!solve_swizzle({{tpos[0], tpos[1], gpos[1], gpos[2]}}, 0xF, g.out_src,
                      g.out_msk, &g.out_n))
     return false;
   // Split reads: lanes vary group bits 0..2 and (half-warp) member bit 2;
-  // 16-byte units keep bit 0 in place.  With qubit 0 a target (member bit 0
-  // = tile bit 0) members 4q, 4q+1 are one 16-byte unit read by one LDS.128,
+  // 16-byte units keep bit 0 in place.  With member bit 0 on tile bit 0
+  // (qubit 0) members 4q, 4q+1 are one 16-byte unit read by one LDS.128,
   // and the quarter-warp lanes (group bits 0..2) must hit distinct units
   // (bits 1..3 of the swizzled index).
-  if (g.tile_is_target[0]) {
+  g.raw_n = 0;
+  if (!raw) return true;
+  if (tpos[0] == 0) {
     if (!solve_swizzle({{0, gpos[0], gpos[1], gpos[2]}}, 0xE, g.raw_src,
                        g.raw_msk, &g.raw_n))
       return false;
@@ -925,6 +928,26 @@ static bool tc_roles(TcGeom& g, const unsigned* qs6) {
     return false;
   }
   return true;
+}
+
+// Roles for a gate with sorted targets qs6: member bit m is the tile bit of
+// qs6[m], group bits follow the tile bits in order.
+static bool tc_roles(TcGeom& g, const unsigned* qs6) {
+  unsigned tord[kK], gord[kK], nt = 0, ng = 0;
+  for (unsigned m = 0; m < unsigned(kK); ++m) {
+    tord[m] = unsigned(kTileBits);
+    for (unsigned j = 0; j < unsigned(kTileBits); ++j)
+      if (g.bitpos_state[j] == qs6[m]) tord[m] = j;
+    if (tord[m] == unsigned(kTileBits)) return false;
+    ++nt;
+  }
+  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
+    if (std::find(tord, tord + kK, j) != tord + kK) continue;
+    if (ng == unsigned(kK)) return false;
+    gord[ng++] = j;
+  }
+  if (nt != unsigned(kK) || ng != unsigned(kK)) return false;
+  return tc_roles_ordered(g, tord, gord);
 }
 
 static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
@@ -954,43 +977,57 @@ static bool plan_tc(unsigned n, const unsigned* qs6, TcGeom& g) {
 
 
 // ===========================================================================
-// Two gates per pass.  Gates A and B (6 targets each, padded) whose qubits
-// fit one 12-bit tile (|A u B| <= 12) are applied in one read and one write
-// of the state: the tile is split and multiplied by A, the epilogue writes
-// A's result (FP32, still scaled by sigma) back into shared memory ("mid"),
-// the producers split that for B, and the epilogue stores B's result.  Both
-// gates share the tile's bit -> state-bit map; each has its own member /
-// group roles of the tile bits (geometries ga, gb).  Every role walks the
-// same job list, A(0), A(1), B(0), A(2), B(1), ..., A(T-1), B(T-2), B(T-1),
-// so that a tile's B job finds its A result ready while the next tile's A
-// job keeps the tensor cores busy.  Job k uses operand buffer k % kNB2 and
-// accumulator k % kNA2; an A job's buffer then holds its mid tile until the
-// producers have split it for B.  Numerically a pass is two passes of the
-// one-gate kernel without the FP32 round trip through HBM in between.
-constexpr int kNB2 = 5;                  // operand / mid / staging buffers
-constexpr int kNA2 = 4;                  // accumulators (64 columns each)
+// Two gates per pass.  Gates A and B (6 targets each, padded) whose targets
+// fit one 12-bit tile that starts at qubit 0 are applied in one read and
+// one write of the state.  The producers split the raw tile for A; the
+// epilogue drains A's accumulator (values still scaled by sigma) and writes
+// them, split into FP16 hi / lo, straight into B's operand buffer; the MMA
+// thread multiplies that by B; the epilogue drains B's accumulator, stages
+// and stores the tile.  Both gates share the tile's bit -> state-bit map;
+// each has its own member / group roles of the tile bits (geometries ga,
+// gb), chosen so that a warp's 4-byte operand writes in A's drain fall on
+// 32 distinct banks: the five tile bits a warp's lanes vary (A's member
+// bits 0..2, A's group bits 1, 2) are B's member bits 0, 1 and group bits
+// 0..2.  The gates' members are therefore numbered in that order, not by
+// qubit (pa, pb map member bits to the sorted targets of the matrices).
+// The MMA thread and the epilogue walk one job list, A(0), A(1), B(0),
+// A(2), B(1), ..., A(T-1), B(T-2), B(T-1), so that a tile's B job finds its
+// operand ready while the next tile's A job keeps the tensor cores busy;
+// job k uses accumulator k % kNAcc2.  A operands live in kNA2 buffers
+// (freed by the MMAs' completion), B operands in kNBB2 buffers that also
+// stage B's result.  Numerically a pass is two one-gate passes without the
+// FP32 round trip through HBM.
+constexpr int kNA2 = 3;                  // A operand buffers
+constexpr int kNBB2 = 2;                 // B operand / staging buffers
+constexpr int kNAcc2 = 4;                // accumulators (64 columns each)
 constexpr uint32_t kTmemGateB = 128;     // columns of gate B (A at 0)
 constexpr uint32_t kTmemD2 = 256;        // first accumulator column
-constexpr uint32_t kOffOp2 = kOffRaw + kRawStages * kTileBytes;
-constexpr uint32_t kOffTabG2 = kOffOp2 + kNB2 * kOpBytes;  // 8 x u64
-constexpr uint32_t kOffTabSE2 = kOffTabG2 + 64;            // 2 x 4 x u32
-constexpr uint32_t kOffTabSO2 = kOffTabSE2 + 32;           // 4 x u32
-constexpr uint32_t kOffTabGE2 = kOffTabSO2 + 16;           // 2 x 64 x u32
-constexpr uint32_t kOffTabRd2 = kOffTabGE2 + 512;          // 8 x u32 (B)
-constexpr uint32_t kOffTabWr2 = kOffTabRd2 + 32;           // 8 x u32 (A)
-constexpr uint32_t kNumBars2 = 2 * kNB2 + 2 * kNA2 + 2 + 1;
+constexpr uint32_t kOffOpA2 = kOffRaw + kRawStages * kTileBytes;
+constexpr uint32_t kOffOpB2 = kOffOpA2 + kNA2 * kOpBytes;
+constexpr uint32_t kOffTabG2 = kOffOpB2 + kNBB2 * kOpBytes;  // 8 x u64
+constexpr uint32_t kOffTabSE2 = kOffTabG2 + 64;              // 4 x u32
+constexpr uint32_t kOffTabSO2 = kOffTabSE2 + 16;             // 4 x u32
+constexpr uint32_t kOffTabGE2 = kOffTabSO2 + 16;             // 64 x u32 (B stage)
+constexpr uint32_t kOffTabOB2 = kOffTabGE2 + 256;            // 64 x u32 (B operand)
+constexpr uint32_t kOffTabRd2 = kOffTabOB2 + 256;            // 8 x u32 (B)
+constexpr uint32_t kOffTabWr2 = kOffTabRd2 + 32;             // 8 x u32 (A raw)
+constexpr uint32_t kNumBars2 = 2 * kNA2 + kNBB2 + 2 * kNAcc2 + 1;
 constexpr uint32_t kOffBar2 = kOffTabWr2 + 32;
 constexpr uint32_t kOffFlag2 = kOffBar2 + 8 * kNumBars2;
-constexpr uint32_t kOffNorm2 = kOffFlag2 + 16;             // 16 x f64
+constexpr uint32_t kOffNorm2 = kOffFlag2 + 16;               // 16 x f64
 constexpr uint32_t kOffTmem2 = kOffNorm2 + 16 * 8 + 16;
 constexpr uint32_t kSmemBytes2 = kOffTmem2 + 16;
 static_assert(kSmemBytes2 <= 232448, "shared memory budget (two gates)");
-static_assert(kTmemD2 + kNA2 * 64 <= kTmemCols, "tensor memory budget");
+static_assert(kTmemD2 + kNAcc2 * 64 <= kTmemCols, "tensor memory budget");
+static_assert(kOffBar2 % 8 == 0 && kOffNorm2 % 8 == 0, "alignment");
 
 struct Tc2Args {
   TcGeom ga, gb;          // the same tile bits; A's and B's member roles
-  const float2* opa;      // padded 64 x 64 complex FP32 gates
-  const float2* opb;
+  const float2* opa;      // padded 64 x 64 complex FP32 gates, members in
+  const float2* opb;      // sorted-qubit order
+  // Member bit j of a gate's kernel numbering is member bit pa[j] (pb[j])
+  // of its matrix.
+  uint32_t pa[kK], pb[kK];
   float scale, inv_scale;
   int* error;
   const double* prev;     // norm carry, as TcArgs
@@ -1017,9 +1054,32 @@ __device__ __forceinline__ void tc2_job(uint64_t k, uint64_t T, uint64_t* i,
   }
 }
 
-// Job index of tile i's A job.
-__device__ __forceinline__ uint64_t tc2_job_a(uint64_t i) {
-  return i == 0 ? 0 : 2 * i - 1;
+__host__ __device__ __forceinline__ uint32_t bit_perm(uint32_t m,
+                                                      const uint32_t* p) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int j = 0; j < kK; ++j) r |= ((m >> j) & 1u) << p[j];
+  return r;
+}
+
+// Byte offset, inside a B operand image, of the FP16 (re, im) pair of tile
+// index e under gb's roles: member m of group n sits in row n, K chunk
+// m / 4, at (m % 4) * 4 bytes.  Every tile bit adds a distinct power of two.
+__host__ __device__ __forceinline__ uint32_t opb_off(uint32_t e,
+                                                     const TcGeom& g) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int j = 0; j < kTileBits; ++j) {
+    if (!((e >> j) & 1)) continue;
+    if (g.tile_is_target[j]) {
+      const uint32_t m = g.target_slot[j];
+      o |= m < 2 ? (4u << m) : (kLBO << (m - 2));
+    } else {
+      const uint32_t k = g.group_slot[j];
+      o |= k < 3 ? (16u << k) : (kSBOB << (k - 3));
+    }
+  }
+  return o;
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -1031,18 +1091,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tid = threadIdx.x;
   const uint32_t warp = tid / 32, lane = tid % 32;
   uint64_t* tab_g = reinterpret_cast<uint64_t*>(smem + kOffTabG2);
-  uint32_t* tab_se = reinterpret_cast<uint32_t*>(smem + kOffTabSE2);  // [2][4]
+  uint32_t* tab_se = reinterpret_cast<uint32_t*>(smem + kOffTabSE2);
   uint32_t* tab_so = reinterpret_cast<uint32_t*>(smem + kOffTabSO2);
-  uint32_t* tab_ge = reinterpret_cast<uint32_t*>(smem + kOffTabGE2);  // [2][64]
+  uint32_t* tab_ge = reinterpret_cast<uint32_t*>(smem + kOffTabGE2);
+  uint32_t* tab_ob = reinterpret_cast<uint32_t*>(smem + kOffTabOB2);
   uint32_t* tab_rd = reinterpret_cast<uint32_t*>(smem + kOffTabRd2);
   uint32_t* tab_wr = reinterpret_cast<uint32_t*>(smem + kOffTabWr2);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kOffBar2);
-  uint64_t* op_full = bars;                        // [kNB2] producers -> MMA
-  uint64_t* op_free = bars + kNB2;                 // [kNB2] buffer reusable
-  uint64_t* acc_full = bars + 2 * kNB2;            // [kNA2] MMA -> epilogue
-  uint64_t* acc_free = bars + 2 * kNB2 + kNA2;     // [kNA2] epilogue -> MMA
-  uint64_t* mid_full = bars + 2 * kNB2 + 2 * kNA2;  // [2] epilogue -> producers
-  uint64_t* gate_ready = mid_full + 2;             // epilogue -> MMA
+  uint64_t* opa_full = bars;                        // [kNA2] producers -> MMA
+  uint64_t* opa_free = bars + kNA2;                 // [kNA2] MMA commit -> producers
+  uint64_t* opb_full = bars + 2 * kNA2;             // [kNBB2] epilogue -> MMA
+  uint64_t* acc_full = opb_full + kNBB2;            // [kNAcc2] MMA -> epilogue
+  uint64_t* acc_free = acc_full + kNAcc2;           // [kNAcc2] epilogue -> MMA
+  uint64_t* gate_ready = acc_free + kNAcc2;         // epilogue -> MMA
   volatile int* flag = reinterpret_cast<volatile int*>(smem + kOffFlag2);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kOffTmem2);
   const uint32_t sbase = smem_u32(smem);
@@ -1055,16 +1116,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (tid < kSplitPerRole) {
     const uint32_t idx = tid << kRoleBits;
-    // A splits the raw tile (A's raw swizzle); B splits the mid tile, which
-    // A's epilogue wrote with A's output swizzle.
     tab_se[tid] = swz_raw<4>(tile_e(split_n(idx), 4 * split_q(idx), ga), ga);
-    tab_se[kSplitPerRole + tid] =
-        swz_out(tile_e(split_n(idx), 4 * split_q(idx), gb), ga);
     tab_so[tid] = op_off(split_n(idx), split_q(idx));
   }
   if (tid < kGroups) {
-    tab_ge[tid] = swz_out(tile_e(tid, 0, ga), ga);
-    tab_ge[kGroups + tid] = swz_out<4>(tile_e(tid, 0, gb), gb);
+    tab_ge[tid] = swz_out<4>(tile_e(tid, 0, gb), gb);
+    tab_ob[tid] = opb_off(tile_e(tid, 0, ga), gb);
   }
   if (tid == 0) {
     for (uint32_t i = 0; i < kNumBars2; ++i) mbar_init(&bars[i], 1);
@@ -1093,29 +1150,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint64_t jobs = 2 * T;
 
   if (warp < kProdWarps) {
-    // ======================== producers ==================================
+    // ======================== producers (A splits) =======================
     const uint32_t rt = tid;
     const uint64_t my_g = tile_goff(rt << 1, ga);
     const uint32_t my_wr = swz_raw<4>(rt << 1, ga);
-    const uint32_t my_se_a =
+    const uint32_t my_se =
         swz_raw<4>(tile_e(split_n(rt), 4 * split_q(rt), ga), ga);
-    const uint32_t my_se_b =
-        swz_out(tile_e(split_n(rt), 4 * split_q(rt), gb), ga);
     const uint32_t my_so = op_off(split_n(rt), split_q(rt));
-    // Tile offsets of member bits 0 and 1 in each gate, swizzled like the
-    // buffer the gate's split reads (raw for A, mid for B).
-    uint32_t am1 = 0, am2 = 0, bm1 = 0, bm2 = 0;
+    uint32_t e_m1 = 0, e_m2 = 0;
     for (int j = 0; j < kTileBits; ++j) {
-      if (ga.tile_is_target[j] && ga.target_slot[j] == 0) am1 = 1u << j;
-      if (ga.tile_is_target[j] && ga.target_slot[j] == 1) am2 = 1u << j;
-      if (gb.tile_is_target[j] && gb.target_slot[j] == 0) bm1 = 1u << j;
-      if (gb.tile_is_target[j] && gb.target_slot[j] == 1) bm2 = 1u << j;
+      if (ga.tile_is_target[j] && ga.target_slot[j] == 0) e_m1 = 1u << j;
+      if (ga.tile_is_target[j] && ga.target_slot[j] == 1) e_m2 = 1u << j;
     }
-    const bool a_units = am1 == 1;  // members 4q, 4q+1 are 16-byte units
-    am1 = swz_raw<4>(am1, ga);
-    am2 = swz_raw<4>(am2, ga);
-    bm1 = swz_out(bm1, ga);
-    bm2 = swz_out(bm2, ga);
+    e_m1 = swz_raw<4>(e_m1, ga);
+    e_m2 = swz_raw<4>(e_m2, ga);
     float carry = 1.f;
     if (a.prev) {
       double pin = 0, pout = 0;
@@ -1133,10 +1181,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const float sc = a.scale * carry;
     float sin_s = 0.f, sin_c = 0.f;
     auto issue_loads = [&](uint64_t i) {
-      const uint64_t t = t0 + i * step;
       if (i < T) {
         const float4* gp = reinterpret_cast<const float4*>(
-            st + (expand_outer_tc(t, ga) | my_g));
+            st + (expand_outer_tc(t0 + i * step, ga) | my_g));
         const uint32_t sdst = sbase + kOffRaw + (i % kRawStages) * kTileBytes;
 #pragma unroll
         for (int j = 0; j < kUnitsPerRole; ++j)
@@ -1145,74 +1192,48 @@ __global__ void __launch_bounds__(kThreads, 1)
       cp_commit();
     };
     for (int q = 0; q < kRawStages; ++q) issue_loads(q);
-    for (uint64_t k = 0; k < jobs; ++k) {
-      uint64_t i;
-      bool is_b;
-      tc2_job(k, T, &i, &is_b);
-      const int b = int(k % kNB2);
+    for (uint64_t i = 0; i < T; ++i) {
+      const int ba = int(i % kNA2);
+      cp_wait<kRawStages - 1>();
       bool bad = false;
-      if (k >= kNB2)
-        bad = !mbar_wait(&op_free[b], uint32_t((k - kNB2) / kNB2) & 1, flag,
+      if (i >= kNA2)
+        bad = !mbar_wait(&opa_free[ba], uint32_t((i - kNA2) / kNA2) & 1, flag,
                          a.wait_cycles);
-      if (!is_b) {
-        cp_wait<kRawStages - 1>();
-      } else if (!bad) {
-        bad = !mbar_wait(&mid_full[i & 1], uint32_t(i >> 1) & 1, flag,
-                         a.wait_cycles);
-      }
       if (bar_or(1, kProdThreads, bad)) break;
-      const uint32_t obuf = kOffOp2 + b * kOpBytes;
-      const float2* src;
-      uint32_t se0, m1, m2, set;
-      float scl;
-      if (!is_b) {
-        src = reinterpret_cast<const float2*>(
-            smem + kOffRaw + (i % kRawStages) * kTileBytes);
-        se0 = my_se_a;
-        m1 = am1;
-        m2 = am2;
-        set = 0;
-        scl = sc;
-      } else {
-        src = reinterpret_cast<const float2*>(
-            smem + kOffOp2 + (tc2_job_a(i) % kNB2) * kOpBytes);
-        se0 = my_se_b;
-        m1 = bm1;
-        m2 = bm2;
-        set = kSplitPerRole;
-        scl = 1.f;  // the mid tile is already scaled
-      }
+      const float2* raw = reinterpret_cast<const float2*>(
+          smem + kOffRaw + (i % kRawStages) * kTileBytes);
+      const uint32_t obuf = kOffOpA2 + ba * kOpBytes;
       float2 xv[kSplitPerRole][4];
 #pragma unroll
       for (int j = 0; j < kSplitPerRole; ++j) {
-        const uint32_t e0 = se0 ^ tab_se[set + j];
-        if (!is_b && a_units) {
-          const float4* raw4 = reinterpret_cast<const float4*>(src);
-          const float4 p0 = raw4[e0 >> 1], p1 = raw4[(e0 ^ m2) >> 1];
+        const uint32_t e0 = my_se ^ tab_se[j];
+        if (e_m1 == 1) {
+          const float4* raw4 = reinterpret_cast<const float4*>(raw);
+          const float4 p0 = raw4[e0 >> 1], p1 = raw4[(e0 ^ e_m2) >> 1];
           xv[j][0] = make_float2(p0.x, p0.y);
           xv[j][1] = make_float2(p0.z, p0.w);
           xv[j][2] = make_float2(p1.x, p1.y);
           xv[j][3] = make_float2(p1.z, p1.w);
         } else {
-          xv[j][0] = src[e0];
-          xv[j][1] = src[e0 ^ m1];
-          xv[j][2] = src[e0 ^ m2];
-          xv[j][3] = src[e0 ^ m1 ^ m2];
+          xv[j][0] = raw[e0];
+          xv[j][1] = raw[e0 ^ e_m1];
+          xv[j][2] = raw[e0 ^ e_m2];
+          xv[j][3] = raw[e0 ^ e_m1 ^ e_m2];
         }
       }
       float tile_in = 0.f;
 #pragma unroll
       for (int j = 0; j < kSplitPerRole; ++j) {
         const float2 x0 = xv[j][0], x1 = xv[j][1], x2 = xv[j][2], x3 = xv[j][3];
-        if (a.out && !is_b) {
+        if (a.out) {
           tile_in = fmaf(x0.x, x0.x, fmaf(x0.y, x0.y, tile_in));
           tile_in = fmaf(x1.x, x1.x, fmaf(x1.y, x1.y, tile_in));
           tile_in = fmaf(x2.x, x2.x, fmaf(x2.y, x2.y, tile_in));
           tile_in = fmaf(x3.x, x3.x, fmaf(x3.y, x3.y, tile_in));
         }
         float x[8];
-        x[0] = x0.x * scl; x[1] = x0.y * scl; x[2] = x1.x * scl; x[3] = x1.y * scl;
-        x[4] = x2.x * scl; x[5] = x2.y * scl; x[6] = x3.x * scl; x[7] = x3.y * scl;
+        x[0] = x0.x * sc; x[1] = x0.y * sc; x[2] = x1.x * sc; x[3] = x1.y * sc;
+        x[4] = x2.x * sc; x[5] = x2.y * sc; x[6] = x3.x * sc; x[7] = x3.y * sc;
         uint4 h, l;
         uint32_t* hp = &h.x;
         uint32_t* lp = &l.x;
@@ -1227,7 +1248,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         *reinterpret_cast<uint4*>(smem + obuf + o) = h;
         *reinterpret_cast<uint4*>(smem + obuf + kBImgBytes + o) = l;
       }
-      if (a.out && !is_b) {
+      if (a.out) {
         const float y = tile_in - sin_c;
         const float t2 = sin_s + y;
         sin_c = (t2 - sin_s) - y;
@@ -1235,12 +1256,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       fence_async_smem();
       bar_sync(1, kProdThreads);
-      if (rt == 0) {
-        mbar_arrive(&op_full[b]);
-        // B's split has read the mid tile: A's buffer is free.
-        if (is_b) mbar_arrive(&op_free[tc2_job_a(i) % kNB2]);
-      }
-      if (!is_b) issue_loads(i + kRawStages);  // raw[i] is consumed
+      if (rt == 0) mbar_arrive(&opa_full[ba]);
+      issue_loads(i + kRawStages);  // raw[i] is consumed
     }
     cp_wait<0>();
     if (a.out) {
@@ -1260,16 +1277,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = (32 * quad) << 16;
     const uint32_t row = 32 * quad + lane;
     // Both gates into tensor memory (A at column 0, B at kTmemGateB), rows
-    // ordered as in the one-gate kernel.
+    // ordered as in the one-gate kernel, members in the kernel numbering.
 #pragma unroll 1
     for (int gi = 0; gi < 2; ++gi) {
+      const uint32_t* pm = gi ? a.pb : a.pa;
+      const float2* mat = gi ? a.opb : a.opa;
       const uint32_t member = 8 * (row >> 4) + (row & 7);
-      const float2* mrow = (gi ? a.opb : a.opa) + size_t(member) * kD + 32 * chalf;
+      const float2* mrow = mat + size_t(bit_perm(member, pm)) * kD;
       const bool im_row = (row >> 3) & 1;
       uint32_t hw[32], lw[32];
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
-        const float2 m = mrow[q];
+        const float2 m = mrow[bit_perm(32 * chalf + q, pm)];
         const float x0 = im_row ? m.y : m.x;
         const float x1 = im_row ? m.x : -m.y;
         const __half2 h = __floats2half2_rn(x0, x1);
@@ -1287,13 +1306,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (et == 0) mbar_arrive(gate_ready);
     const uint64_t my_g = tile_goff(et << 1, ga);
     const uint32_t my_rd = swz_out<4>(et << 1, gb);
+    // This thread's amplitudes in a drain: member 8 (2 quad + h) + lane / 4
+    // (A's numbering for A jobs, B's for B jobs) of groups
+    // 32 chalf + 2 (lane % 4) + 8x + {0, 1}.
     const uint32_t col0 = 32 * chalf + 2 * (lane & 3);
-    uint32_t my_me_a[2], my_me_b[2];
+    uint32_t my_ob[2], my_me[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const uint32_t m = 8 * (2 * quad + h) + lane / 4;
-      my_me_a[h] = swz_out(tile_e(col0, m, ga), ga);
-      my_me_b[h] = swz_out<4>(tile_e(col0, m, gb), gb);
+      my_ob[h] = opb_off(tile_e(col0, m, ga), gb);
+      my_me[h] = swz_out<4>(tile_e(col0, m, gb), gb);
     }
     const float inv = a.inv_scale;
     float sout_s = 0.f, sout_c = 0.f;
@@ -1301,10 +1323,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint64_t i;
       bool is_b;
       tc2_job(k, T, &i, &is_b);
-      const int acc = int(k % kNA2);
-      const int b = int(k % kNB2);
-      const bool bad = !mbar_wait(&acc_full[acc], uint32_t(k / kNA2) & 1, flag,
-                                  a.wait_cycles);
+      const int acc = int(k % kNAcc2);
+      const int bb = int(i % kNBB2);
+      const bool bad = !mbar_wait(&acc_full[acc], uint32_t(k / kNAcc2) & 1,
+                                  flag, a.wait_cycles);
       if (bar_or(2, kEpiThreads, bad)) break;
       tc_fence_after();
       uint32_t v[32];
@@ -1316,35 +1338,53 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_before();
       bar_sync(2, kEpiThreads);
       if (et == 0) mbar_arrive(&acc_free[acc]);
-      float2* stage = reinterpret_cast<float2*>(smem + kOffOp2 + b * kOpBytes);
-      const uint32_t* ge = tab_ge + (is_b ? kGroups : 0);
-      const float f = is_b ? inv : 1.f;  // A's result stays scaled (mid)
+      unsigned char* bufb = smem + kOffOpB2 + bb * kOpBytes;
+      if (!is_b) {
+        // A's result (scaled by sigma) as B's FP16 hi / lo operand.  The
+        // buffer's previous tile, B(i - kNBB2), was stored by these threads
+        // before this job (the bar_sync ending that job).
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const float re = __uint_as_float(v[16 * h + 4 * x + e]);
+              const float im = __uint_as_float(v[16 * h + 4 * x + 2 + e]);
+              const __half2 hh = __floats2half2_rn(re, im);
+              const float2 hf = __half22float2(hh);
+              const uint32_t o = my_ob[h] ^ tab_ob[8 * x + e];
+              *reinterpret_cast<uint32_t*>(bufb + o) =
+                  *reinterpret_cast<const uint32_t*>(&hh);
+              *reinterpret_cast<uint32_t*>(bufb + kBImgBytes + o) =
+                  pack_half2(re - hf.x, im - hf.y);
+            }
+        fence_async_smem();
+        bar_sync(2, kEpiThreads);
+        if (et == 0) mbar_arrive(&opb_full[bb]);
+        continue;
+      }
+      // B's result: stage in B's buffer (its MMAs have completed), store.
+      float2* stage = reinterpret_cast<float2*>(bufb);
       float fo = 0.f;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const uint32_t me = is_b ? my_me_b[h] : my_me_a[h];
+      for (int h = 0; h < 2; ++h)
 #pragma unroll
         for (int x = 0; x < 4; ++x)
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
-            const float re = __uint_as_float(v[16 * h + 4 * x + e]) * f;
-            const float im = __uint_as_float(v[16 * h + 4 * x + 2 + e]) * f;
-            stage[me ^ ge[8 * x + e]] = make_float2(re, im);
-            if (is_b) fo = fmaf(re, re, fmaf(im, im, fo));
+            const float re = __uint_as_float(v[16 * h + 4 * x + e]) * inv;
+            const float im = __uint_as_float(v[16 * h + 4 * x + 2 + e]) * inv;
+            stage[my_me[h] ^ tab_ge[8 * x + e]] = make_float2(re, im);
+            fo = fmaf(re, re, fmaf(im, im, fo));
           }
-      }
-      bar_sync(2, kEpiThreads);
-      if (!is_b) {
-        // The mid tile is complete: B's split may read it.
-        if (et == 0) mbar_arrive(&mid_full[i & 1]);
-        continue;
-      }
       {
         const float y = fo - sout_c;
         const float t2 = sout_s + y;
         sout_c = (t2 - sout_s) - y;
         sout_s = t2;
       }
+      bar_sync(2, kEpiThreads);
       const uint64_t base = expand_outer_tc(t0 + i * step, ga);
       float4* gp = reinterpret_cast<float4*>(st + (base | my_g));
       const float4* so = reinterpret_cast<const float4*>(stage);
@@ -1355,8 +1395,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (sidx & 1) w = make_float4(w.z, w.w, w.x, w.y);
         gp[tab_g[j] >> 1] = w;
       }
-      bar_sync(2, kEpiThreads);
-      if (et == 0) mbar_arrive(&op_free[b]);  // staging buffer free
+      bar_sync(2, kEpiThreads);  // the buffer may take the next B operand
     }
     if (a.out) {
       double sum_out = double(sout_s) - double(sout_c);
@@ -1372,19 +1411,24 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint64_t i;
       bool is_b;
       tc2_job(k, T, &i, &is_b);
-      const int b = int(k % kNB2);
-      const int acc = int(k % kNA2);
-      if (!mbar_wait(&op_full[b], uint32_t(k / kNB2) & 1, flag, a.wait_cycles))
-        break;
+      const int acc = int(k % kNAcc2);
+      const int ba = int(i % kNA2), bb = int(i % kNBB2);
+      const bool ok =
+          is_b ? mbar_wait(&opb_full[bb], uint32_t(i / kNBB2) & 1, flag,
+                           a.wait_cycles)
+               : mbar_wait(&opa_full[ba], uint32_t(i / kNA2) & 1, flag,
+                           a.wait_cycles);
+      if (!ok) break;
       if (k == 0) {
         if (!mbar_wait(gate_ready, 0, flag, a.wait_cycles)) break;
-      } else if (k >= kNA2) {
-        if (!mbar_wait(&acc_free[acc], uint32_t((k - kNA2) / kNA2) & 1, flag,
-                       a.wait_cycles))
+      } else if (k >= kNAcc2) {
+        if (!mbar_wait(&acc_free[acc], uint32_t((k - kNAcc2) / kNAcc2) & 1,
+                       flag, a.wait_cycles))
           break;
       }
       tc_fence_after();
-      const uint32_t obuf = kOffOp2 + b * kOpBytes;
+      const uint32_t obuf =
+          is_b ? kOffOpB2 + bb * kOpBytes : kOffOpA2 + ba * kOpBytes;
       const uint32_t d = tmem + kTmemD2 + 64 * acc;
       const uint32_t gbase = tmem + (is_b ? kTmemGateB : 0);
       const uint64_t dhi = make_desc(sbase + obuf, kLBO, kSBOB);
@@ -1397,6 +1441,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_f16_ts(d, gbase + kTmemAlo + 8 * kk, dhi + ko, 1);
       }
       mma_commit(&acc_full[acc]);
+      // The A operand buffer is free once these MMAs have read it.
+      if (!is_b) mma_commit(&opa_free[ba]);
     }
   }
 
@@ -1426,13 +1472,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Geometry of a pair: the 12 tile bits are the union `u` of the two gates'
+// Geometry of a pair.  The 12 tile bits are the union `u` of the two gates'
 // (padded) targets, completed with the lowest other qubits; both geometries
-// share the tile-bit -> state-bit map and differ in member / group roles.
-// A's staging swizzle is the layout of the mid tile, which A's epilogue
-// writes and B's split reads: it is solved for both access patterns.
+// share the tile-bit -> state-bit map.  Tile bits are of four kinds: a
+// target of both gates (TT), of A only (TG), of B only (GT), of neither
+// (GG); with s TT bits there are 6 - s TG, 6 - s GT and s GG bits.  Five
+// tile bits L, a TT, 3 - a TG, 2 - a GT and a GG ones, become A's member
+// bits 0..2 (TT, TG), A's group bits 1, 2 (GT, GG), B's member bits 0, 1
+// (TT, GT) and B's group bits 0..2 (TG, GG): then the lanes of a warp in
+// A's drain (A member bits 0..2, A group bits 1, 2) write B's operand at 32
+// distinct banks (B member bits 0, 1 and group bits 0..2 are the bank).
+// Identical target sets (s = 6) admit no such L; false then.  pa[j] (pb[j])
+// is the sorted-target index of the qubit of member bit j.
 static bool plan_tc2(unsigned n, const unsigned* qa6, const unsigned* qb6,
-                     TcGeom& ga, TcGeom& gb) {
+                     TcGeom& ga, TcGeom& gb, uint32_t* pa, uint32_t* pb) {
   std::vector<unsigned> u(qa6, qa6 + kK);
   for (unsigned j = 0; j < kK; ++j)
     if (std::find(u.begin(), u.end(), qb6[j]) == u.end()) u.push_back(qb6[j]);
@@ -1452,27 +1505,95 @@ static bool plan_tc2(unsigned n, const unsigned* qa6, const unsigned* qb6,
   // Tile bit 0 must be state bit 0: the kernel moves amplitudes in pairs of
   // neighbours (16-byte units).
   if (h > kTileBits || b < 1) return false;
+  uint64_t bitpos[kTileBits];
+  for (unsigned j = 0; j < b; ++j) bitpos[j] = j;
+  for (unsigned i = 0; i < h; ++i) bitpos[b + i] = u[kTileBits - h + i];
+  auto in = [](const unsigned* q6, uint64_t sb) {
+    return std::find(q6, q6 + kK, unsigned(sb)) != q6 + kK;
+  };
+  std::vector<unsigned> tt, tg, gt, gg;
+  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
+    const bool ia = in(qa6, bitpos[j]), ib = in(qb6, bitpos[j]);
+    (ia ? (ib ? tt : tg) : (ib ? gt : gg)).push_back(j);
+  }
+  const int s = int(tt.size());
+  // a TT bits in L; prefer the choice that puts tile bit 0 (qubit 0, if a
+  // target of A) on A's member bit 0, for the producers' 16-byte reads.
+  // (tt and tg list tile bits in ascending order: tile bit 0, when one of
+  // them holds it, is their first element and is picked for any quota >= 1.)
+  int na = -1;
+  for (int a = std::max(0, s - 3); a <= std::min(2, s); ++a) {
+    if (3 - a > 6 - s || 2 - a > 6 - s) continue;
+    const bool zero_in = (!tt.empty() && tt[0] == 0 && a >= 1) ||
+                         (!tg.empty() && tg[0] == 0 && 3 - a >= 1);
+    if (na < 0 || zero_in) na = a;
+    if (zero_in) break;
+  }
+  if (na < 0) return false;
+  std::vector<unsigned> l_tt(tt.begin(), tt.begin() + na);
+  std::vector<unsigned> l_tg(tg.begin(), tg.begin() + (3 - na));
+  std::vector<unsigned> l_gt(gt.begin(), gt.begin() + (2 - na));
+  std::vector<unsigned> l_gg(gg.begin(), gg.begin() + na);
+  auto rest = [](const std::vector<unsigned>& all,
+                 std::vector<unsigned> pick) {
+    std::vector<unsigned> r;
+    for (unsigned j : all)
+      if (std::find(pick.begin(), pick.end(), j) == pick.end()) r.push_back(j);
+    return r;
+  };
+  auto cat = [](std::vector<unsigned> x, const std::vector<unsigned>& y) {
+    x.insert(x.end(), y.begin(), y.end());
+    return x;
+  };
+  // A: member bits 0..2 = L's TT + TG bits (tile bit 0 first when there),
+  // 3..5 the other A targets; group bit 0 an A group outside L, 1, 2 = L's
+  // GT + GG bits, 3..5 the rest.
+  std::vector<unsigned> at = cat(l_tt, l_tg);
+  std::sort(at.begin(), at.end());
+  std::vector<unsigned> a_targets = cat(tt, tg);
+  std::sort(a_targets.begin(), a_targets.end());
+  std::vector<unsigned> tord_a = cat(at, rest(a_targets, at));
+  std::vector<unsigned> ag = cat(l_gt, l_gg);
+  std::sort(ag.begin(), ag.end());
+  std::vector<unsigned> a_groups = cat(gt, gg);
+  std::sort(a_groups.begin(), a_groups.end());
+  std::vector<unsigned> ag_rest = rest(a_groups, ag);
+  if (ag_rest.empty()) return false;
+  std::vector<unsigned> gord_a = {ag_rest[0], ag[0], ag[1]};
+  for (size_t i = 1; i < ag_rest.size(); ++i) gord_a.push_back(ag_rest[i]);
+  // B: member bits 0, 1 = L's TT + GT bits, 2..5 the other B targets;
+  // group bits 0..2 = L's TG + GG bits, 3..5 the rest.
+  std::vector<unsigned> bt = cat(l_tt, l_gt);
+  std::sort(bt.begin(), bt.end());
+  std::vector<unsigned> b_targets = cat(tt, gt);
+  std::sort(b_targets.begin(), b_targets.end());
+  std::vector<unsigned> tord_b = cat(bt, rest(b_targets, bt));
+  std::vector<unsigned> bg = cat(l_tg, l_gg);
+  std::sort(bg.begin(), bg.end());
+  std::vector<unsigned> b_groups = cat(tg, gg);
+  std::sort(b_groups.begin(), b_groups.end());
+  std::vector<unsigned> gord_b = cat(bg, rest(b_groups, bg));
+  if (tord_a.size() != 6 || gord_a.size() != 6 || tord_b.size() != 6 ||
+      gord_b.size() != 6)
+    return false;
   for (int gi = 0; gi < 2; ++gi) {
     TcGeom& g = gi ? gb : ga;
     std::memset(&g, 0, sizeof(g));
     g.b = b;
-    for (unsigned j = 0; j < b; ++j) g.bitpos_state[j] = j;
-    for (unsigned i = 0; i < h; ++i) g.bitpos_state[b + i] = u[kTileBits - h + i];
-    if (!tc_roles(g, gi ? qb6 : qa6)) return false;
+    for (unsigned j = 0; j < unsigned(kTileBits); ++j) g.bitpos_state[j] = bitpos[j];
+    // B's operand comes from A's drain, not from a raw tile.
+    if (!tc_roles_ordered(g, (gi ? tord_b : tord_a).data(),
+                          (gi ? gord_b : gord_a).data(), gi == 0))
+      return false;
     g.n_ins = h;
     for (unsigned i = 0; i < h; ++i) g.ins_pos[i] = u[kTileBits - h + i];
     g.num_tiles = uint64_t{1} << (n - kTileBits);
   }
-  unsigned gpa[6], tpa[6], gpb[6], tpb[6];
-  for (unsigned j = 0; j < unsigned(kTileBits); ++j) {
-    if (ga.tile_is_target[j]) tpa[ga.target_slot[j]] = j;
-    else gpa[ga.group_slot[j]] = j;
-    if (gb.tile_is_target[j]) tpb[gb.target_slot[j]] = j;
-    else gpb[gb.group_slot[j]] = j;
+  for (unsigned m = 0; m < unsigned(kK); ++m) {
+    pa[m] = unsigned(std::find(qa6, qa6 + kK, unsigned(bitpos[tord_a[m]])) - qa6);
+    pb[m] = unsigned(std::find(qb6, qb6 + kK, unsigned(bitpos[tord_b[m]])) - qb6);
   }
-  return solve_swizzle({{tpa[0], tpa[1], gpa[1], gpa[2]},
-                        {gpb[0], gpb[1], gpb[2], tpb[2]}},
-                       0xF, ga.out_src, ga.out_msk, &ga.out_n);
+  return true;
 }
 
 }  // namespace tc
@@ -1643,7 +1764,7 @@ int apply_gate_tc2_carry(qsg_ctx* ctx, float* state, unsigned n,
                          double* out) {
   using namespace tc;
   Tc2Args a;
-  if (!plan_tc2(n, qa6, qb6, a.ga, a.gb)) {
+  if (!plan_tc2(n, qa6, qb6, a.ga, a.gb, a.pa, a.pb)) {
     set_error("two-gate tensor-core pass: targets do not fit one 12-qubit "
               "tile (n = %u)", n);
     return QSG_ERR_UNSUPPORTED;
@@ -1676,7 +1797,8 @@ int apply_gate_tc2_carry(qsg_ctx* ctx, float* state, unsigned n,
 // the tile), or -1 if the pair does not fit a two-gate pass.
 int tc2_run_bits(unsigned n, const unsigned* qa6, const unsigned* qb6) {
   tc::TcGeom ga, gb;
-  if (!tc::plan_tc2(n, qa6, qb6, ga, gb)) return -1;
+  uint32_t pa[tc::kK], pb[tc::kK];
+  if (!tc::plan_tc2(n, qa6, qb6, ga, gb, pa, pb)) return -1;
   return int(ga.b);
 }
 
@@ -1691,10 +1813,27 @@ int apply_gate_tc2_host(qsg_ctx* ctx, float* state, unsigned n,
   std::vector<float> ma6, mb6;
   pad_to_6(n, qa, ka, ma, qa6, ma6);
   pad_to_6(n, qb, kb, mb, qb6, mb6);
+  if (std::equal(qa6, qa6 + 6, qb6)) {
+    // The same six qubits: one pass of the product B A (FP64 on the host).
+    std::vector<float> prod(2 * kD * kD);
+    for (unsigned r = 0; r < unsigned(kD); ++r)
+      for (unsigned c = 0; c < unsigned(kD); ++c) {
+        double re = 0, im = 0;
+        for (unsigned j = 0; j < unsigned(kD); ++j) {
+          const double br = mb6[2 * (r * kD + j)], bi = mb6[2 * (r * kD + j) + 1];
+          const double ar = ma6[2 * (j * kD + c)], ai = ma6[2 * (j * kD + c) + 1];
+          re += br * ar - bi * ai;
+          im += br * ai + bi * ar;
+        }
+        prod[2 * (r * kD + c)] = float(re);
+        prod[2 * (r * kD + c) + 1] = float(im);
+      }
+    return apply_gate_tc_host(ctx, state, n, qa6, 6, prod.data());
+  }
   if (tc2_run_bits(n, qa6, qb6) < 1) {
     set_error("two-gate tensor-core pass: the padded targets of the two "
-              "gates span more than 12 qubits, or a 12-qubit tile of them "
-              "does not start at qubit 0");
+              "gates span 12 qubits without qubit 0 (no tile of them starts "
+              "at qubit 0)");
     return QSG_ERR_UNSUPPORTED;
   }
   int rc = tc_ring_init(ctx);

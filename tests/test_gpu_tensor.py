@@ -194,7 +194,9 @@ def tc2_cases(rng, n):
     include qubit 0."""
     cases = [([0, 1, 2, 3, 4, 5], [6, 7, 8, 9, 10, 11]),
              ([0, 2, 4, 6, 8, 10], [1, 3, 5, 7, 9, 11]),
-             ([3, 4, 5, 6, 7, 8], [3, 4, 5, 6, 7, 8]),
+             ([3, 4, 5, 6, 7, 8], [3, 4, 5, 6, 7, 8]),       # one product pass
+             ([1, 2, 3, 4, 5, 7], [1, 2, 3, 4, 6, 7]),       # five shared qubits
+             ([2, 5, 7, n - 3, n - 2, n - 1], [0, 5, 7, 9, n - 2, n - 1]),
              ([0, 1, 2, 3, 4, 5], [3, 4, 5, 6, 7, 8]),
              (list(range(n - 6, n)), [0, 1, 2] + list(range(n - 3, n))),
              ([0, n - 1], [1, 5, n - 2]),
