@@ -47,8 +47,9 @@ METRIC = "30q d20 circuit s/run: tensor-core+learned fusion vs plain, F>=1-1e-6;
 UNIT = "s/run"
 GRID = dict(rows=5, cols=6, extra=0, cycles=20, seed=1)
 # Two-gate tensor-core passes for consecutive blocks whose 12-qubit tile has
-# >= 3 run bits (measured 0.89-0.92 of two one-gate passes at 30 qubits).
-TC_PAIR_BITS = 3
+# >= 2 run bits (measured 0.78-0.95 of two one-gate passes at 30 qubits; the
+# planner pairs by the measured saving per run-bit count).
+TC_PAIR_BITS = 2
 WORKLOAD = "grid5x6 (30 qubits) random circuit depth 20, seed 1, complex64, from |0>"
 
 

@@ -251,7 +251,8 @@ class Plan:
                  tensor_path: bool = False, tc_min_k: int = 5, seeds: int = 0,
                  cost_model=None, unfused: bool = False, tc_pairs: int = 0):
         """tc_pairs: minimum run bits of two-gate tensor-core passes (0: one
-        pass per block; 3 is where a pair measured faster than two passes)."""
+        pass per block; from 2 run bits up a pair measured faster than two
+        passes, and the planner weighs pairs by their measured saving)."""
         self.circuit = circuit
         h = C.c_void_p()
         if unfused:

@@ -131,11 +131,17 @@ struct FuseOptions {
 };
 
 // Measured cost of a two-gate tensor-core pass relative to the two one-gate
-// passes it replaces (0.89 - 0.92 on GB300 at >= 3 run bits, 30 qubits).
-constexpr double kTcPairCostFactor = 0.9;
+// passes it replaces, by the run bits of its tile (GB300, 30 qubits, ten
+// launches each, best of three): 1.11 at 1 run bit, 0.95 at 2, 0.87 at 3,
+// 0.78-0.82 at 4 or more.
+inline double tc_pair_cost_factor(int run_bits) {
+  return run_bits >= 4 ? 0.80 : run_bits == 3 ? 0.87 : run_bits == 2 ? 0.95
+                                                                      : 1.11;
+}
 // Marks pairs of consecutive tensor-core ops (tc_pair_next) that fit a
-// two-gate pass with >= `bits` run bits, the most pairs possible; returns
-// their number.
+// two-gate pass with >= `bits` run bits and are predicted faster than two
+// passes, choosing the set of pairs with the largest predicted saving;
+// returns their number.
 size_t pair_tensor_ops(Plan& plan, unsigned bits);
 
 Plan fuse(const Circuit& c, const FuseOptions& opt);

@@ -494,7 +494,7 @@ class MemoCost : public CostModel {
 };
 
 // Predicted time of a plan; a two-gate tensor-core pass costs
-// kTcPairCostFactor of its two blocks' one-gate passes.
+// tc_pair_cost_factor(run bits) of its two blocks' one-gate passes.
 double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
   double t = 0;
   for (size_t i = 0; i < p.ops.size(); ++i) {
@@ -504,7 +504,7 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
     if (op.tc_pair_next) {
       const auto& nx = p.ops[i + 1];
       ti += m.cost_us(c.num_qubits, nx.qs, unsigned(nx.cqs.size()), nx.path);
-      ti *= kTcPairCostFactor;
+      ti *= tc_pair_cost_factor(tile_run_bits(c.num_qubits, op.qs, nx.qs));
       ++i;
     }
     t += ti;
@@ -512,11 +512,22 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
   return t;
 }
 
-// Passes over the state: ops minus the ones that share a two-gate pass.
-size_t plan_passes(const Plan& p) {
-  size_t n = 0;
-  for (const auto& op : p.ops) n += op.kind != OpKind::kMeasure && !op.tc_pair_next;
-  return n;
+// Passes over the state in units of one pass: a two-gate pass counts
+// 2 tc_pair_cost_factor(run bits).
+double plan_passes(const Plan& p) {
+  double t = 0;
+  for (size_t i = 0; i < p.ops.size(); ++i) {
+    const auto& op = p.ops[i];
+    if (op.kind == OpKind::kMeasure) continue;
+    if (op.tc_pair_next) {
+      t += 2.0 * tc_pair_cost_factor(
+                     tile_run_bits(p.num_qubits, op.qs, p.ops[i + 1].qs));
+      ++i;
+    } else {
+      t += 1.0;
+    }
+  }
+  return t;
 }
 
 }  // namespace
@@ -614,22 +625,29 @@ size_t pair_tensor_ops(Plan& plan, unsigned bits) {
     return op.kind == OpKind::kGate && op.path == Path::kTensor &&
            op.qs.size() == 6 && op.cqs.empty();
   };
-  // ok[i]: ops i, i + 1 fit one pass.  best[i]: most pairs among ops >= i.
-  std::vector<char> ok(n, 0);
-  for (size_t i = 0; i + 1 < n; ++i)
-    ok[i] = tensor6(plan.ops[i]) && tensor6(plan.ops[i + 1]) &&
-            tile_run_bits(plan.num_qubits, plan.ops[i].qs,
-                          plan.ops[i + 1].qs) >= int(bits) &&
-            tc2_run_bits(plan.num_qubits, plan.ops[i].qs.data(),
-                         plan.ops[i + 1].qs.data()) >= int(bits);
-  std::vector<size_t> best(n + 2, 0);
+  // gain[i] > 0: ops i, i + 1 fit one pass, predicted faster than two (in
+  // units of one pass).  best[i]: the largest total gain among ops >= i.
+  std::vector<double> gain(n, 0.0);
+  for (size_t i = 0; i + 1 < n; ++i) {
+    if (!tensor6(plan.ops[i]) || !tensor6(plan.ops[i + 1])) continue;
+    const int rb = tile_run_bits(plan.num_qubits, plan.ops[i].qs,
+                                 plan.ops[i + 1].qs);
+    if (rb < int(bits)) continue;
+    const double g = 2.0 * (1.0 - tc_pair_cost_factor(rb));
+    if (g <= 0) continue;
+    if (tc2_run_bits(plan.num_qubits, plan.ops[i].qs.data(),
+                     plan.ops[i + 1].qs.data()) < int(bits))
+      continue;
+    gain[i] = g;
+  }
+  std::vector<double> best(n + 2, 0.0);
   for (size_t i = n; i-- > 0;) {
     best[i] = best[i + 1];
-    if (ok[i]) best[i] = std::max(best[i], 1 + best[i + 2]);
+    if (gain[i] > 0) best[i] = std::max(best[i], gain[i] + best[i + 2]);
   }
   size_t pairs = 0;
   for (size_t i = 0; i < n;) {
-    if (ok[i] && 1 + best[i + 2] >= best[i + 1]) {
+    if (gain[i] > 0 && gain[i] + best[i + 2] >= best[i + 1]) {
       plan.ops[i].tc_pair_next = true;
       ++pairs;
       i += 2;
@@ -654,7 +672,7 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
     // std::async futures carry a worker's exception (bad_alloc, say) to
     // get() on this thread, and their destructors wait for the worker, so
     // an exception here never leaves a joinable thread behind.
-    // With two-gate passes the count is of passes (pairs count once).
+    // With two-gate passes a pair counts as its measured cost in passes.
     std::vector<Plan> plans(windows.size());
     std::vector<std::future<Plan>> pool;
     for (size_t i = 1; i < windows.size(); ++i) {
@@ -707,6 +725,11 @@ Plan fuse(const Circuit& c, const FuseOptions& opt) {
           if (w == 3u && (opt.seeds == 3u || ff < 5)) continue;
           cands.push_back({ff, w, pg, ex != 0});
         }
+        // The gate-count rule at the full block size also from the other
+        // start windows of the fixed tensor-core planner.
+        if (opt.tensor_path && ff == f && f >= 5 && !pg)
+          for (unsigned w : kStartWindows)
+            if (w != opt.seeds && w != 3u) cands.push_back({ff, w, pg, ex != 0});
       }
     }
   }
