@@ -609,7 +609,9 @@ typedef struct qsg_hybrid_options {
   unsigned num_prefix_gatexs;
   unsigned num_root_gatexs;
   unsigned max_fused_size;   /* 0: 4 */
-  int tensor_path;           /* fused blocks of >= 5 qubits on tcgen05 */
+  int tensor_path;           /* fused blocks of >= 5 qubits on tcgen05,
+                                consecutive ones in two-gate passes where
+                                their tile allows (tc_pair_bits 2) */
   unsigned max_batch_bits;   /* 0: by free memory */
 } qsg_hybrid_options;
 typedef struct qsg_hybrid_info {

@@ -69,7 +69,6 @@ constexpr int kReal = 2 * kD;          // real dimension (128) = M = K
 constexpr int kGroups = 64;            // N
 constexpr int kTileBits = 12;          // 64 groups x 64 members
 constexpr int kTileAmps = 1 << kTileBits;
-constexpr uint32_t kAWords = kReal / 2;                 // FP16 pairs per A row
 // Operands in memory: the padded 64 x 64 complex FP32 gate, row-major
 // interleaved; the kernel converts it to the FP16 A images itself.
 constexpr uint32_t kOperandBytes = kD * kD * 8;          // 32 KiB
@@ -538,7 +537,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float2* raw = reinterpret_cast<const float2*>(smem + kOffRaw + rs * kTileBytes);
       const uint32_t obuf = kOffOp + s * kOpBytes;
       float tile_in = 0.f;
-#pragma unroll
       // All raw reads of the tile first, then the splits and the operand
       // stores: the stores go to another buffer, but the compiler cannot
       // move a later shared-memory load above an earlier store, so
@@ -1037,7 +1035,7 @@ struct Tc2Args {
 };
 
 // Job k of a CTA with T tiles: its tile index i and whether it is gate B.
-__device__ __forceinline__ void tc2_job(uint64_t k, uint64_t T, uint64_t* i,
+__device__ __forceinline__ void tc2_job(uint32_t k, uint32_t T, uint32_t* i,
                                         bool* is_b) {
   if (k == 0) {
     *i = 0;
@@ -1143,11 +1141,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // Tile and job counters fit 32 bits: at most 2^(40 - 12) tiles.
   const uint64_t step = gridDim.x;
   const uint64_t t0 = blockIdx.x;
-  const uint64_t T =
-      t0 < ga.num_tiles ? (ga.num_tiles - t0 + step - 1) / step : 0;
-  const uint64_t jobs = 2 * T;
+  const uint32_t T =
+      t0 < ga.num_tiles ? uint32_t((ga.num_tiles - t0 + step - 1) / step) : 0;
+  const uint32_t jobs = 2 * T;
 
   if (warp < kProdWarps) {
     // ======================== producers (A splits) =======================
@@ -1180,10 +1179,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     const float sc = a.scale * carry;
     float sin_s = 0.f, sin_c = 0.f;
-    auto issue_loads = [&](uint64_t i) {
+    auto issue_loads = [&](uint32_t i) {
       if (i < T) {
         const float4* gp = reinterpret_cast<const float4*>(
-            st + (expand_outer_tc(t0 + i * step, ga) | my_g));
+            st + (expand_outer_tc(t0 + uint64_t(i) * step, ga) | my_g));
         const uint32_t sdst = sbase + kOffRaw + (i % kRawStages) * kTileBytes;
 #pragma unroll
         for (int j = 0; j < kUnitsPerRole; ++j)
@@ -1192,7 +1191,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       cp_commit();
     };
     for (int q = 0; q < kRawStages; ++q) issue_loads(q);
-    for (uint64_t i = 0; i < T; ++i) {
+    for (uint32_t i = 0; i < T; ++i) {
       const int ba = int(i % kNA2);
       cp_wait<kRawStages - 1>();
       bool bad = false;
@@ -1319,8 +1318,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     const float inv = a.inv_scale;
     float sout_s = 0.f, sout_c = 0.f;
-    for (uint64_t k = 0; k < jobs; ++k) {
-      uint64_t i;
+    for (uint32_t k = 0; k < jobs; ++k) {
+      uint32_t i;
       bool is_b;
       tc2_job(k, T, &i, &is_b);
       const int acc = int(k % kNAcc2);
@@ -1385,7 +1384,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         sout_s = t2;
       }
       bar_sync(2, kEpiThreads);
-      const uint64_t base = expand_outer_tc(t0 + i * step, ga);
+      const uint64_t base = expand_outer_tc(t0 + uint64_t(i) * step, ga);
       float4* gp = reinterpret_cast<float4*>(st + (base | my_g));
       const float4* so = reinterpret_cast<const float4*>(stage);
 #pragma unroll
@@ -1407,8 +1406,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (lane == 0) {
     // ======================== MMA issuer =================================
-    for (uint64_t k = 0; k < jobs; ++k) {
-      uint64_t i;
+    for (uint32_t k = 0; k < jobs; ++k) {
+      uint32_t i;
       bool is_b;
       tc2_job(k, T, &i, &is_b);
       const int acc = int(k % kNAcc2);

@@ -386,7 +386,15 @@ int qsg_unitary_run_plan(qsg_ctx* ctx, qsg_plan* p, float* u, unsigned n) {
     const PlanOp& op = rt.plan.ops[i];
     if (op.kind == OpKind::kMeasure)
       return invalid("qsg_unitary_run_plan: plans with measurements");
-    if (op.kind == OpKind::kGate && op.path == Path::kTensor) {
+    if (op.kind == OpKind::kGate && op.path == Path::kTensor &&
+        op.tc_pair_next) {
+      // Two blocks in one pass (their tile fits the n low qubits' union,
+      // the same on the 2n-qubit view).
+      rc = apply_gate_tc2_carry(ctx, u, 2 * n, op.qs.data(), rt.tc_operands(i),
+                                rt.plan.ops[i + 1].qs.data(),
+                                rt.tc_operands(i + 1), nullptr, 0, nullptr);
+      ++i;
+    } else if (op.kind == OpKind::kGate && op.path == Path::kTensor) {
       rc = apply_gate_tc(ctx, u, 2 * n, op.qs.data(), op.qs.size(),
                          op.m32.data(), rt.tc_operands(i));
     } else {

@@ -342,6 +342,9 @@ int qsg_hybrid_run(qsg_ctx* ctx, const qsg_circuit* c, const unsigned* parts,
   if (fo.max_fused_size > 6)
     return fail(QSG_ERR_INVALID, "max_fused_size must be 1..6");
   fo.tensor_path = o->tensor_path != 0;
+  // On the tensor cores, consecutive blocks share two-gate passes where
+  // their tile allows (from 2 run bits, weighed by the measured saving).
+  fo.tc_pair_bits = fo.tensor_path ? 2 : 0;
 
   // Suffix gates batched on the device: the first ones whose bits fit.
   unsigned cap = o->max_batch_bits;

@@ -114,18 +114,21 @@ def test_gpu_identity_entries_and_zeros(uc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,f,tc", [(5, 4, False), (7, 3, False),
-                                    (12, 6, True)])
-def test_gpu_unitary_from_fused_plan(uc, oracle, n, f, tc):
+@pytest.mark.parametrize("n,f,tc,pairs", [(5, 4, False, 0), (7, 3, False, 0),
+                                          (12, 6, True, 0), (12, 6, True, 1)])
+def test_gpu_unitary_from_fused_plan(uc, oracle, n, f, tc, pairs):
     """A fused plan applied to the unitary (tensor-core blocks on tcgen05
-    for the 12-qubit circuit: a 2^24-entry unitary) equals the unfused
-    oracle unitary."""
+    for the 12-qubit circuit: a 2^24-entry unitary; with `pairs`, blocks
+    two at a time in two-gate passes) equals the unfused oracle unitary."""
     us, calc, ctx = uc
     from qsim_gb300 import engine as E
     c = E.Circuit.chain(n, 4, 30 + n) if n < 12 else E.Circuit.grid(3, 4, 0, 3, 5)
-    plan = E.Plan(c, max_fused_size=f, tensor_path=tc, tc_min_k=2)
+    plan = E.Plan(c, max_fused_size=f, tensor_path=tc, tc_min_k=2,
+                  tc_pairs=pairs)
     if tc:
         assert plan.info()["num_tensor_ops"] > 0
+    if pairs:
+        assert plan.info()["num_tc_pairs"] > 0
     u = us.CreateUnitary(n)
     us.SetIdentity(u)
     calc.RunPlan(plan, u)
