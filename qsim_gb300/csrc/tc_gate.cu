@@ -471,8 +471,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // Tile counters fit 32 bits: at most 2^(40 - 12) tiles.
   const uint64_t step = gridDim.x;
   const uint64_t t0 = blockIdx.x;
+  const uint32_t T =
+      t0 < g.num_tiles ? uint32_t((g.num_tiles - t0 + step - 1) / step) : 0;
 
   if (warp < kProdWarps) {
     // ======================== producers ==================================
@@ -509,10 +512,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     // sum |input|^2 over this thread's items (unscaled): FP32 per tile,
     // Kahan-compensated FP32 across tiles (FP64 issue is scarce on GB300).
     float sin_s = 0.f, sin_c = 0.f;
-    auto issue_loads = [&](uint64_t t, int stage) {
-      if (t < g.num_tiles) {
+    auto issue_loads = [&](uint32_t i, int stage) {
+      if (i < T) {
         const float4* gp = reinterpret_cast<const float4*>(
-            st + (expand_outer_tc(t, g) | my_g));
+            st + (expand_outer_tc(t0 + uint64_t(i) * step, g) | my_g));
         const uint32_t sdst = sbase + kOffRaw + stage * kTileBytes;
 #pragma unroll
         for (int j = 0; j < kUnitsPerRole; ++j)
@@ -520,9 +523,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       cp_commit();
     };
-    for (int q = 0; q < kRawStages; ++q) issue_loads(t0 + q * step, q);
-    int i = 0;
-    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+    for (int q = 0; q < kRawStages; ++q) issue_loads(q, q);
+    for (uint32_t i = 0; i < T; ++i) {
       const int rs = i % kRawStages;
       const int s = i % kNB;
       cp_wait<kRawStages - 1>();
@@ -597,7 +599,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       fence_async_smem();
       bar_sync(1, kProdThreads);
       if (rt == 0) mbar_arrive(&op_full[s]);
-      issue_loads(t + kRawStages * step, rs);  // raw[rs] is consumed
+      issue_loads(i + kRawStages, rs);  // raw[rs] is consumed
     }
     cp_wait<0>();
     if (a.out) {
@@ -661,8 +663,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // sum |output|^2 over this thread's outputs: FP32 per tile, Kahan FP32
     // across tiles.
     float sout_s = 0.f, sout_c = 0.f;
-    int i = 0;
-    for (uint64_t t = t0; t < g.num_tiles; t += step, ++i) {
+    for (uint32_t i = 0; i < T; ++i) {
       const int s = i % kNB;
       const bool bad =
           !mbar_wait(&acc_full[s], (i / kNB) & 1, flag, a.wait_cycles);
@@ -696,7 +697,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         sout_s = t2;
       }
       bar_sync(2, kEpiThreads);
-      const uint64_t base = expand_outer_tc(t, g);
+      const uint64_t base = expand_outer_tc(t0 + uint64_t(i) * step, g);
       float4* gp = reinterpret_cast<float4*>(st + (base | my_g));
       const float4* so = reinterpret_cast<const float4*>(stage);
 #pragma unroll
@@ -719,11 +720,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (lane == 0) {
     // ======================== MMA issuer =================================
-    int i = 0;
     // Test hook: a wait that nothing ends; it gives up after the budget and
     // sets the flag, and the loop below then issues nothing.
     const bool stalled = a.stall && !mbar_wait(never, 0, flag, a.wait_cycles);
-    for (uint64_t t = t0; !stalled && t < g.num_tiles; t += step, ++i) {
+    for (uint32_t i = 0; !stalled && i < T; ++i) {
       const int s = i % kNB;
       if (!mbar_wait(&op_full[s], (i / kNB) & 1, flag, a.wait_cycles)) break;
       // The gate must be in tensor memory before the first MMA, and

@@ -93,7 +93,9 @@ int PlanRuntime::upload(qsg_ctx* c) {
   for (size_t i = 0; i < plan.ops.size(); ++i) {
     const auto& op = plan.ops[i];
     if (op.kind == OpKind::kMeasure) continue;
-    if (op.qs.size() >= 6) {
+    // k = 6 matrices of CUDA-core passes (tensor-core passes read their own
+    // operands, prepare_tc).
+    if (op.qs.size() >= 6 && op.path != Path::kTensor) {
       dmat_off[i] = total;
       total += op.m32.size();
     }
