@@ -452,7 +452,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (tid < kGroups) tab_ge[tid] = swz_out<4>(tile_e(tid, 0, g), g);
   if (tid == 0) {
-    for (uint32_t i = 0; i < kNumBars; ++i) mbar_init(&bars[i], 1);
+    // Accumulators and operand buffers are released by each epilogue warp
+    // (eight arrivals), the rest by one thread.
+    for (uint32_t i = 0; i < kNumBars; ++i) {
+      const bool per_warp = (i >= kNB && i < 2 * kNB) || (i >= 3 * kNB && i < 4 * kNB);
+      mbar_init(&bars[i], per_warp ? kEpiWarps : 1);
+    }
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -675,8 +680,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       tmem_ld16x256_x4(taddr + (16u << 16), v + 16);
       tmem_wait_ld();
       tc_fence_before();
-      bar_sync(2, kEpiThreads);
-      if (et == 0) mbar_arrive(&acc_free[s]);  // accumulator s drained
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_free[s]);  // this warp's part drained
       float2* stage = reinterpret_cast<float2*>(smem + kOffOp + s * kOpBytes);
       float fo = 0.f;
 #pragma unroll
@@ -707,8 +712,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (sidx & 1) w = make_float4(w.z, w.w, w.x, w.y);
         gp[tab_g[j] >> 1] = w;
       }
-      bar_sync(2, kEpiThreads);
-      if (et == 0) mbar_arrive(&op_free[s]);  // operand buffer s free
+      // This warp has read its part of the staging: one of the eight
+      // arrivals that free operand buffer s.
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&op_free[s]);
     }
     if (a.out) {
       double sum_out = double(sout_s) - double(sout_c);
@@ -1122,7 +1129,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     tab_ob[tid] = opb_off(tile_e(tid, 0, ga), gb);
   }
   if (tid == 0) {
-    for (uint32_t i = 0; i < kNumBars2; ++i) mbar_init(&bars[i], 1);
+    // B operands and accumulators are released by each epilogue warp
+    // (eight arrivals), the rest by one thread.
+    for (uint32_t i = 0; i < kNumBars2; ++i) {
+      const uint64_t* b = &bars[i];
+      const bool per_warp = (b >= opb_full && b < opb_full + kNBB2) ||
+                            (b >= acc_free && b < acc_free + kNAcc2);
+      mbar_init(&bars[i], per_warp ? kEpiWarps : 1);
+    }
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -1335,13 +1349,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       tmem_ld16x256_x4(taddr + (16u << 16), v + 16);
       tmem_wait_ld();
       tc_fence_before();
-      bar_sync(2, kEpiThreads);
-      if (et == 0) mbar_arrive(&acc_free[acc]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_free[acc]);  // this warp's part drained
       unsigned char* bufb = smem + kOffOpB2 + bb * kOpBytes;
       if (!is_b) {
         // A's result (scaled by sigma) as B's FP16 hi / lo operand.  The
         // buffer's previous tile, B(i - kNBB2), was stored by these threads
-        // before this job (the bar_sync ending that job).
+        // in an earlier job (the barrier that starts every job orders it).
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
@@ -1359,8 +1373,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                   pack_half2(re - hf.x, im - hf.y);
             }
         fence_async_smem();
-        bar_sync(2, kEpiThreads);
-        if (et == 0) mbar_arrive(&opb_full[bb]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&opb_full[bb]);  // one of eight arrivals
         continue;
       }
       // B's result: stage in B's buffer (its MMAs have completed), store.
@@ -1394,7 +1408,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (sidx & 1) w = make_float4(w.z, w.w, w.x, w.y);
         gp[tab_g[j] >> 1] = w;
       }
-      bar_sync(2, kEpiThreads);  // the buffer may take the next B operand
+      // The buffer takes B(i + kNBB2)'s operand in a later job, after the
+      // barrier that starts every job.
     }
     if (a.out) {
       double sum_out = double(sout_s) - double(sout_c);
