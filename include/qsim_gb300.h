@@ -221,6 +221,15 @@ int qsg_apply_gate_tc(qsg_ctx* ctx, float* state, unsigned n,
 int qsg_apply_gate_tc2(qsg_ctx* ctx, float* state, unsigned n,
                        const unsigned* qa, unsigned ka, const float* ma,
                        const unsigned* qb, unsigned kb, const float* mb);
+/* ExpectationValue on the tensor cores: <s| M_qs |s> for k <= 6 targets
+ * (padded to 6 with the identity), n >= 12, |s_i| <= 4; the state is read
+ * once and each tile's (M s) is multiplied by conj(s) in the epilogue, FP64
+ * partials.  qsg_expectation_value takes this path for dense operators
+ * where it is faster; this entry forces it.  The reference computes
+ * ExpectationValue on CUDA cores (lib/simulator_cuda.h:216-260). */
+int qsg_expectation_value_tc(qsg_ctx* ctx, const float* state, unsigned n,
+                             const unsigned* qs, unsigned k,
+                             const float* matrix, double* out_re_im);
 /* Reads and clears the tensor-core kernels' error flag: 1 if a bounded
  * device-side wait gave up (the kernel then skipped its remaining tiles). */
 int qsg_tc_error(qsg_ctx* ctx, int* out);

@@ -76,6 +76,7 @@ SIGNATURES = {
     "qsg_apply_gate_tc": (i32, [vp, vp, u32, P_u32, u32, P_f32]),
     "qsg_apply_gate_tc2": (i32, [vp, vp, u32, P_u32, u32, P_f32, P_u32, u32,
                                  P_f32]),
+    "qsg_expectation_value_tc": (i32, [vp, vp, u32, P_u32, u32, P_f32, P_f64]),
     "qsg_tc_error": (i32, [vp, C.POINTER(C.c_int)]),
     "qsg_tc_stall_test": (i32, [vp, vp, u32, C.c_longlong]),
     "qsg_simd_register_size": (u32, []),

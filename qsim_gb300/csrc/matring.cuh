@@ -17,6 +17,13 @@ int matring_upload(qsg_ctx* ctx, const float* host_matrix, size_t nfloats,
 int reduce_partials_d2(qsg_ctx* ctx, const double2* partial, uint64_t count,
                        double* out_re_im);
 
+// <psi| M |psi> of a k <= 6-qubit operator on the tensor cores (n >= 12;
+// tc_gate.cu).  *overflow: an amplitude was too large for the split (the
+// result is then not valid; use the CUDA-core path).
+int expectation_tc(qsg_ctx* ctx, const float* state, unsigned n,
+                   const unsigned* qs, unsigned k, const float* m32,
+                   double* out_re_im, bool* overflow);
+
 // Releases the ring buffers of a context.
 void matring_release(qsg_ctx* ctx);
 // Releases the tensor-core operand ring of a context (tc_gate.cu).

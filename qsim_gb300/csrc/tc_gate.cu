@@ -50,6 +50,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "matring.cuh"
 
 namespace qsg {
 
@@ -148,6 +149,11 @@ struct TcArgs {
   // wait runs out before any MMA is issued and every role takes the error
   // exit (the state is left as it was).
   int stall;
+  // Expectation-value launches: per-CTA sum of conj(psi_i) (M psi)_i, and
+  // a flag set when an amplitude times sigma left the FP16 range (the
+  // result is then not used).
+  double2* ev_partial;
+  int* ev_overflow;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -413,6 +419,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
   return true;
 }
 
+// EV = false: apply the gate (read and write the state).  EV = true:
+// <psi| M |psi> (ExpectationValue): the state is only read; the epilogue
+// multiplies each output amplitude (M psi)_i by conj(psi_i), psi_i taken
+// back from the tile's FP16 hi + lo operand images, and nothing is stored.
+template <bool EV>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gate_kernel(float2* __restrict__ st, const __grid_constant__ TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -517,6 +528,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // sum |input|^2 over this thread's items (unscaled): FP32 per tile,
     // Kahan-compensated FP32 across tiles (FP64 issue is scarce on GB300).
     float sin_s = 0.f, sin_c = 0.f;
+    bool ovf = false;  // EV: an amplitude times sigma beyond FP16's range
     auto issue_loads = [&](uint32_t i, int stage) {
       if (i < T) {
         const float4* gp = reinterpret_cast<const float4*>(
@@ -590,6 +602,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           const float2 hf = __half22float2(hh);
           hp[c] = *reinterpret_cast<const uint32_t*>(&hh);
           lp[c] = pack_half2(x[2 * c] - hf.x, x[2 * c + 1] - hf.y);
+          if constexpr (EV)
+            ovf |= fmaxf(fabsf(x[2 * c]), fabsf(x[2 * c + 1])) > 65504.f;
         }
         const uint32_t o = my_so | tso[j];
         *reinterpret_cast<uint4*>(smem + obuf + o) = h;
@@ -607,6 +621,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       issue_loads(i + kRawStages, rs);  // raw[rs] is consumed
     }
     cp_wait<0>();
+    if constexpr (EV) {
+      if (__any_sync(0xffffffffu, ovf) && lane == 0) atomicOr(a.ev_overflow, 1);
+    }
     if (a.out) {
       // The input this pass applies the gate to is carry * input.
       double sum_in = (double(sin_s) - double(sin_c)) * double(carry) *
@@ -668,6 +685,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     // sum |output|^2 over this thread's outputs: FP32 per tile, Kahan FP32
     // across tiles.
     float sout_s = 0.f, sout_c = 0.f;
+    // EV: this thread's sum of conj(psi) (M psi), FP32 per tile, FP64
+    // across tiles; my_xo[h] is the operand-image byte offset of its
+    // amplitude (member 8 (2 quad + h) + lane / 4, group col0): group bit 0
+    // adds 16 bytes, group bits 3, 4 add 2 KiB each step.
+    double ev_re = 0, ev_im = 0;
+    uint32_t my_xo[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t m = 8 * (2 * quad + h) + lane / 4;
+      my_xo[h] = op_off(col0, m >> 2) + (m & 3) * 4;
+    }
     for (uint32_t i = 0; i < T; ++i) {
       const int s = i % kNB;
       const bool bad =
@@ -682,6 +710,33 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_free[s]);  // this warp's part drained
+      if constexpr (EV) {
+        const unsigned char* ob = smem + kOffOp + s * kOpBytes;
+        float pr = 0.f, pi = 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const float yr = __uint_as_float(v[16 * h + 4 * x + e]) * inv;
+              const float yi = __uint_as_float(v[16 * h + 4 * x + 2 + e]) * inv;
+              const uint32_t o = my_xo[h] + 16u * e + kSBOB * uint32_t(x);
+              const float2 ph = __half22float2(
+                  *reinterpret_cast<const __half2*>(ob + o));
+              const float2 pl = __half22float2(
+                  *reinterpret_cast<const __half2*>(ob + kBImgBytes + o));
+              const float xr = (ph.x + pl.x) * inv, xi = (ph.y + pl.y) * inv;
+              pr = fmaf(xr, yr, fmaf(xi, yi, pr));
+              pi = fmaf(xr, yi, fmaf(-xi, yr, pi));
+            }
+        ev_re += double(pr);
+        ev_im += double(pi);
+        // This warp has read its part of the operand images.
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&op_free[s]);
+        continue;
+      }
       float2* stage = reinterpret_cast<float2*>(smem + kOffOp + s * kOpBytes);
       float fo = 0.f;
 #pragma unroll
@@ -717,7 +772,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&op_free[s]);
     }
-    if (a.out) {
+    if constexpr (EV) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ev_re += __shfl_xor_sync(0xffffffffu, ev_re, o);
+        ev_im += __shfl_xor_sync(0xffffffffu, ev_im, o);
+      }
+      if (lane == 0) {
+        reinterpret_cast<double*>(smem + kOffNorm)[ew] = ev_re;
+        reinterpret_cast<double*>(smem + kOffNorm)[kEpiWarps + ew] = ev_im;
+      }
+    }
+    if (!EV && a.out) {
       double sum_out = double(sout_s) - double(sout_c);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
@@ -763,7 +829,16 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   // ---- tear-down -----------------------------------------------------------
   __syncthreads();
-  if (a.out && tid == 0) {
+  if (EV && tid == 0) {
+    const double* nsum = reinterpret_cast<const double*>(smem + kOffNorm);
+    double sr = 0, si = 0;
+    for (int w = 0; w < kEpiWarps; ++w) {
+      sr += nsum[w];
+      si += nsum[kEpiWarps + w];
+    }
+    a.ev_partial[blockIdx.x] = make_double2(sr, si);
+  }
+  if (!EV && a.out && tid == 0) {
     const double* nsum = reinterpret_cast<const double*>(smem + kOffNorm);
     double si = 0, so = 0;
     for (int w = 0; w < kProdWarps; ++w) si += nsum[w];
@@ -1653,6 +1728,29 @@ static int tc_ring_init(qsg_ctx* ctx) {
   return QSG_OK;
 }
 
+// Uploads a padded 6-qubit gate (m6, 64 x 64 complex FP32) through a pinned
+// staging slot of the context's operand ring; *dev is its device copy.
+static int tc_ring_upload(qsg_ctx* ctx, const std::vector<float>& m6,
+                          const void** dev) {
+  using namespace tc;
+  constexpr size_t kSlot = (kOperandBytes + 1023) & ~size_t(1023);
+  int rc = tc_ring_init(ctx);
+  if (rc) return rc;
+  const int slot = ctx->tc_ring_next;
+  ctx->tc_ring_next = (slot + 1) % qsg_ctx::kTcRingSlots;
+  if (ctx->tc_ring_used[slot])
+    QSG_CUDA(cudaEventSynchronize(ctx->tc_ring_ev[slot]));
+  unsigned char* h = ctx->tc_ring_host + slot * kSlot;
+  unsigned char* d = ctx->tc_ring_dev + slot * kSlot;
+  std::memcpy(h, m6.data(), kOperandBytes);
+  QSG_CUDA(cudaMemcpyAsync(d, h, kOperandBytes, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  QSG_CUDA(cudaEventRecord(ctx->tc_ring_ev[slot], ctx->stream));
+  ctx->tc_ring_used[slot] = true;
+  *dev = d;
+  return QSG_OK;
+}
+
 int apply_gate_tc_host(qsg_ctx* ctx, float* state, unsigned n,
                        const unsigned* qs, unsigned k, const float* m32) {
   using namespace tc;
@@ -1689,6 +1787,7 @@ void tcring_release(qsg_ctx* ctx) {
 }
 
 static int* g_tc_err = nullptr;
+static int* g_tc_ovf = nullptr;  // EV overflow flag
 // Wait budget and test stall of the next launches; changed only for the
 // duration of qsg_tc_stall_test on the calling thread.
 static thread_local long long g_tc_wait_cycles = tc::kWaitCycles;
@@ -1700,7 +1799,12 @@ int tc_setup() {
   if (!g_tc_err) {
     QSG_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
     QSG_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
-    QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate_kernel,
+    QSG_CUDA(cudaMalloc(&g_tc_ovf, sizeof(int)));
+    QSG_CUDA(cudaMemset(g_tc_ovf, 0, sizeof(int)));
+    QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate_kernel<false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(tc::kSmemBytes)));
+    QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate_kernel<true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(tc::kSmemBytes)));
     QSG_CUDA(cudaFuncSetAttribute(tc::tc_gate2_kernel,
@@ -1762,7 +1866,8 @@ int apply_gate_tc_carry(qsg_ctx* ctx, float* state, unsigned n,
   a.wait_cycles = g_tc_wait_cycles;
   a.stall = g_tc_stall;
   const uint64_t grid = std::min<uint64_t>(a.g.num_tiles, ctx->num_sms);
-  tc_gate_kernel<<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
+  a.ev_partial = nullptr;
+  tc_gate_kernel<false><<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
       reinterpret_cast<float2*>(state), a);
   QSG_LAUNCHED(ctx);
   (void)m32;
@@ -1882,6 +1987,57 @@ int tc_check_error(qsg_ctx* ctx, int* out) {
   return QSG_OK;
 }
 
+// <psi| M |psi> of a k-qubit operator (k <= 6, padded to 6 targets with the
+// identity, which leaves the value unchanged) on the tensor cores: one read
+// of the state, per-CTA FP64 partials summed in a fixed order.
+int expectation_tc(qsg_ctx* ctx, const float* state, unsigned n,
+                   const unsigned* qs, unsigned k, const float* m32,
+                   double* out_re_im, bool* overflow) {
+  using namespace tc;
+  *overflow = false;
+  if (n < unsigned(kTileBits) || k > unsigned(kK)) {
+    set_error("tensor-core expectation values need n >= %d, k <= 6",
+              kTileBits);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  unsigned qs6[6];
+  std::vector<float> m6;
+  pad_to_6(n, qs, k, m32, qs6, m6);
+  TcArgs a;
+  std::memset(&a, 0, sizeof(a));
+  if (!plan_tc(n, qs6, a.g)) {
+    set_error("tensor-core path needs n >= %d qubits (n = %u)", kTileBits, n);
+    return QSG_ERR_UNSUPPORTED;
+  }
+  const void* dev = nullptr;
+  int rc = tc_ring_upload(ctx, m6, &dev);
+  if (rc) return rc;
+  rc = tc_setup();
+  if (rc) return rc;
+  a.operands = static_cast<const float2*>(dev);
+  const int e = std::min(int(n / 2), 14);
+  a.scale = std::ldexp(1.0f, e);
+  a.inv_scale = std::ldexp(1.0f, -e);
+  a.error = g_tc_err;
+  a.wait_cycles = g_tc_wait_cycles;
+  const uint64_t grid = std::min<uint64_t>(a.g.num_tiles, ctx->num_sms);
+  void* p = nullptr;
+  rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
+  if (rc) return rc;
+  a.ev_partial = static_cast<double2*>(p);
+  a.ev_overflow = g_tc_ovf;
+  QSG_CUDA(cudaMemsetAsync(g_tc_ovf, 0, sizeof(int), ctx->stream));
+  tc_gate_kernel<true><<<unsigned(grid), kThreads, kSmemBytes, ctx->stream>>>(
+      const_cast<float2*>(reinterpret_cast<const float2*>(state)), a);
+  QSG_LAUNCHED(ctx);
+  rc = reduce_partials_d2(ctx, a.ev_partial, grid, out_re_im);  // synchronises
+  if (rc) return rc;
+  int ovf = 0;
+  QSG_CUDA(cudaMemcpy(&ovf, g_tc_ovf, sizeof(int), cudaMemcpyDeviceToHost));
+  *overflow = ovf != 0;
+  return QSG_OK;
+}
+
 void set_error_msg(const char* msg) { set_error("%s", msg); }
 
 }  // namespace qsg
@@ -1922,6 +2078,24 @@ int qsg_apply_gate_tc2(qsg_ctx* ctx, float* state, unsigned n,
     return QSG_ERR_UNSUPPORTED;
   }
   return apply_gate_tc2_host(ctx, state, n, qa, ka, ma, qb, kb, mb);
+}
+
+int qsg_expectation_value_tc(qsg_ctx* ctx, const float* state, unsigned n,
+                             const unsigned* qs, unsigned k,
+                             const float* matrix, double* out_re_im) {
+  QSG_CHECK_ARG(ctx && state && matrix && out_re_im,
+                "qsg_expectation_value_tc: null argument");
+  QSG_CHECK_ARG(k >= 1 && k <= 6 && valid_qubits(qs, k, n),
+                "qsg_expectation_value_tc: bad qubits");
+  bool overflow = false;
+  const int rc = expectation_tc(ctx, state, n, qs, k, matrix, out_re_im,
+                                &overflow);
+  if (rc == QSG_OK && overflow) {
+    set_error("qsg_expectation_value_tc: an amplitude exceeds the range of "
+              "the tensor-core split (|psi_i| > 4)");
+    return QSG_ERR_UNSUPPORTED;
+  }
+  return rc;
 }
 
 int qsg_tc_error(qsg_ctx* ctx, int* out) {
