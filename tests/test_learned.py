@@ -1,5 +1,6 @@
 """Learned fusion planner: the cost-model network and the planner that uses
-it (no counterpart in the reference; its fixed-size fuser is the judge).
+it (no counterpart in the reference; its fixed-size fuser is the baseline
+the learned plans are measured against).
 
 CPU: the FP64 oracle of the network (oracle/mlp_oracle.py) is checked
 against finite differences; the engine's host inference matches it; the
