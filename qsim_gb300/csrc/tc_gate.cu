@@ -349,8 +349,8 @@ __host__ __device__ __forceinline__ uint32_t op_off(uint32_t n, uint32_t q) {
   return (n / 8) * kSBOB + q * kLBO + (n % 8) * 16;
 }
 
-// N: the most entries a swizzle can have (4 for one access pattern, 8 for
-// the two-gate mid tile).
+// N: the most entries a swizzle can have (4 for one access pattern; one
+// solved for two patterns at once can have up to 8).
 template <int N = 8>
 __host__ __device__ __forceinline__ uint32_t swz_x(uint32_t e, const uint32_t* src,
                                           const uint32_t* msk, uint32_t n) {
