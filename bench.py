@@ -701,10 +701,12 @@ EXPECT = dict(n=28, layers=40, controlled=8, seed=3, strings=64, weight=6,
 def bench_expectations(ctx, ss, dist):
     """28-qubit layered circuit (U3 on every qubit, CZ/CNOT on random
     disjoint pairs, 8 gates with 1-2 controls per layer, 40 layers) and 64
-    Pauli strings of weight 1..6: seconds per circuit run (plain f = 4 plan
-    from a CUDA graph) and per expectation value, on the one-pass monomial
-    kernel and, for comparison, on the dense tile kernel (the same operator
-    with one off-pattern entry of 1e-30, which the monomial test rejects)."""
+    Pauli strings of weight 1..6: seconds per circuit run (the learned
+    tensor-core plan with two-gate passes, and the plain f = 4 plan, from
+    CUDA graphs) and per expectation value, on the one-pass monomial kernel
+    and, for comparison, on the dense path (the same operator with one
+    off-pattern entry of 1e-30, which the monomial test rejects: tile kernel
+    for k <= 3, tensor cores for k >= 4)."""
     import numpy as np
     from qsim_gb300 import engine as E
     import qsim_gb300 as q
@@ -719,20 +721,30 @@ def bench_expectations(ctx, ss, dist):
             m = np.kron(paulis[p], m)
         return m
 
+    from qsim_gb300 import learned as L
     c = E.Circuit.layered_u3(EXPECT["n"], EXPECT["layers"], EXPECT["controlled"],
                              EXPECT["seed"])
     n = c.num_qubits
     st = ss.Create(n)
-    plan = E.Plan(c, max_fused_size=4)
-    plan.capture(ctx, st)
-    ss.SetStateZero(st)
-    plan.replay(ctx)
-    ctx.sync()
-    barrier(dist)
-    ctx.timer_start()
-    ss.SetStateZero(st)
-    plan.replay(ctx)
-    circuit_s = max_over_ranks(dist, ctx.timer_stop() / 1e3)
+    # The circuit by the engine's fastest form (learned fusion on the tensor
+    # cores with two-gate passes) and by the plain f = 4 plan; the Pauli sums
+    # are taken on the former's state.
+    circuit = {}
+    for name, plan in (("plain_f4", E.Plan(c, max_fused_size=4)),
+                       ("learned_tc_f6_pairs",
+                        E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=2,
+                               cost_model=L.CostMLP.load(),
+                               tc_pairs=TC_PAIR_BITS))):
+        plan.capture(ctx, st)
+        ss.SetStateZero(st)
+        plan.replay(ctx)
+        ctx.sync()
+        barrier(dist)
+        ctx.timer_start()
+        ss.SetStateZero(st)
+        plan.replay(ctx)
+        circuit[name] = max_over_ranks(dist, ctx.timer_stop() / 1e3)
+        ctx.sync()
     strings = E.pauli_sum(n, EXPECT["strings"], EXPECT["weight"],
                           EXPECT["pauli_seed"])
     mats = []
@@ -757,7 +769,10 @@ def bench_expectations(ctx, ss, dist):
         "workload": f"layered U3 ({n} qubits) 40 layers, 8 controlled gates "
                     f"per layer, seed 3; {len(mats)} Pauli strings of weight "
                     "1..6",
-        "circuit_s_per_run": circuit_s, "passes": len(plan),
+        "circuit_s_per_run": circuit["learned_tc_f6_pairs"],
+        "circuit_form": "learned_tc_f6_pairs",
+        "circuit_plain_f4_s": circuit["plain_f4"],
+        "passes": len(plan) - int(plan.tc_pair_next().sum()),
         "ev": out,
         "ev_speedup": out["dense"]["s_per_ev"] / out["monomial"]["s_per_ev"],
     }
@@ -1005,6 +1020,24 @@ def bench_unitary(ctx, dist, cpu: bool):
 LEARN_GRID = dict(rows=5, cols=6, extra=2, cycles=24, seed=1)
 
 
+def pair_cost_factor(n, a, b):
+    """Cost of a two-gate tensor-core pass relative to two one-gate passes,
+    as the planner weighs it: the pair's 12-qubit tile is the union of both
+    target sets completed with the lowest other qubits, its run bits the
+    length of the prefix 0, 1, ... it holds, and the factor the one measured
+    for that many run bits (0.80 at >= 4, 0.87 at 3, 0.95 at 2, 1.11 else)."""
+    u = set(a) | set(b)
+    q = 0
+    while len(u) < 12 and q < n:
+        u.add(q)
+        q += 1
+    run = 0
+    while run in u:
+        run += 1
+    return (0.80 if run >= 4 else 0.87 if run == 3 else 0.95 if run == 2
+            else 1.11)
+
+
 def bench_learned_planner(ctx, ss, model, dist):
     """Seconds per run of the 32-qubit 5x6+2 grid depth-24 circuit for the
     learned plan and the fixed-size plans (CUDA-core f = 4, 5, 6 and
@@ -1049,15 +1082,17 @@ def bench_learned_planner(ctx, ss, model, dist):
             runs.append(ctx.timer_stop() / 1e3)
         times[name] = max_over_ranks(dist, statistics.median(runs))
         spread[name] = [min(runs), max(runs)]
-        # Predicted time as the planner scores it: a two-gate pass costs
-        # 0.9 of its two blocks (the C++ planner's kTcPairCostFactor).
+        # Predicted time as the planner scores it: a two-gate pass costs its
+        # two blocks times the measured pair factor of its tile's run bits.
         pn = p.tc_pair_next()
+        ops = p.ops()
         costs = [model.cost_us(n, o["qs"], len(o["cqs"]), o["path"])
-                 if o["kind"] != 2 else 0.0 for o in p.ops()]
+                 if o["kind"] != 2 else 0.0 for o in ops]
         pred, i = 0.0, 0
         while i < len(costs):
             if pn[i]:
-                pred += 0.9 * (costs[i] + costs[i + 1])
+                pred += (pair_cost_factor(n, ops[i]["qs"], ops[i + 1]["qs"])
+                         * (costs[i] + costs[i + 1]))
                 i += 2
             else:
                 pred += costs[i]
@@ -1097,9 +1132,10 @@ def bench_learned_controlled(ctx, ss, model, dist):
     f = 4, 5, 6 and tensor-core f = 6) pass the 320 controlled gates through
     unfused, as the reference's MultiQubitGateFuser does; the learned
     planner may absorb them into blocks, and its predicted times choose.
-    Seconds per run (median of 5 graph replays each, min/max beside), host
-    fusion time per plan, and the learned plan's fidelity against the plain
-    f = 4 plan's state."""
+    Each tensor-core form also with two-gate passes.  Seconds per run
+    (median of 5 graph replays each, min/max beside), host fusion time per
+    plan, and the fidelity of the learned plan with two-gate passes against
+    the plain f = 4 plan's state."""
     from qsim_gb300 import engine as E
     from qsim_gb300 import _native as N
     c = E.Circuit.layered_u3(EXPECT["n"], EXPECT["layers"],
@@ -1112,6 +1148,11 @@ def bench_learned_controlled(ctx, ss, model, dist):
         "tc_f6": dict(max_fused_size=6, tensor_path=True, tc_min_k=5),
         "learned_tc_f6": dict(max_fused_size=6, tensor_path=True, tc_min_k=2,
                               cost_model=model),
+        "tc_f6_pairs": dict(max_fused_size=6, tensor_path=True, tc_min_k=5,
+                            tc_pairs=TC_PAIR_BITS),
+        "learned_tc_f6_pairs": dict(max_fused_size=6, tensor_path=True,
+                                    tc_min_k=2, cost_model=model,
+                                    tc_pairs=TC_PAIR_BITS),
     }
     forms, fuse_s = {}, {}
     for name, o in opts.items():
@@ -1140,18 +1181,25 @@ def bench_learned_controlled(ctx, ss, model, dist):
     N.check(N.lib.qsg_inner_product(ctx.h, ref.get(), st.get(), n, r))
     fid = (r[0] ** 2 + r[1] ** 2) / (ss.Norm(ref) * ss.Norm(st))
     del st, ref
-    fixed = {k: v for k, v in times.items() if k != "learned_tc_f6"}
-    best_fixed = min(fixed, key=fixed.get)
+    fixed = {k: v for k, v in times.items() if not k.startswith("learned")}
+    fixed_np = {k: v for k, v in fixed.items() if not k.endswith("_pairs")}
+    best_fixed = min(fixed_np, key=fixed_np.get)
+    best_fixed_any = min(fixed, key=fixed.get)
     return {
         "workload": f"layered U3 ({n} qubits) 40 layers, CZ/CNOT pairs, 8 "
                     "controlled U3 gates (1-2 controls) per layer, seed 3",
         "unit": "s/run", "forms_s": times, "forms_min_max_s": spread,
-        "fuse_s": fuse_s, "passes": {k: len(v) for k, v in forms.items()},
+        "fuse_s": fuse_s,
+        "passes": {k: len(v) - int(v.tc_pair_next().sum())
+                   for k, v in forms.items()},
         "controlled_passes": {k: sum(1 for o in v.ops() if o["kind"] == 1)
                               for k, v in forms.items()},
         "learned_vs_best_fixed": times[best_fixed] / times["learned_tc_f6"],
         "best_fixed": best_fixed,
-        "learned_vs_plain_f4": times["plain_f4"] / times["learned_tc_f6"],
+        "learned_pairs_vs_best_fixed": (times[best_fixed_any]
+                                        / times["learned_tc_f6_pairs"]),
+        "best_fixed_with_pairs": best_fixed_any,
+        "learned_vs_plain_f4": times["plain_f4"] / times["learned_tc_f6_pairs"],
         "fidelity_learned_vs_plain_f4": fid,
     }
 

@@ -154,8 +154,12 @@ def test_gpu_learned_plan_same_state_and_timed(ctx):
     plans = {f"f{f}" + ("_tc" if tc else ""): E.Plan(c, max_fused_size=f,
                                                      tensor_path=tc, tc_min_k=5)
              for f in (4, 5, 6) for tc in (False, True) if tc or f < 6}
+    plans["f6_tc_pairs"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                                  tc_min_k=5, tc_pairs=2)
     plans["learned"] = E.Plan(c, max_fused_size=6, tensor_path=True,
                               tc_min_k=2, cost_model=m)
+    plans["learned_pairs"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                                    tc_min_k=2, cost_model=m, tc_pairs=2)
     states, times = {}, {}
     for name, p in plans.items():
         ss.SetStateZero(st)
@@ -189,7 +193,9 @@ def test_gpu_learned_plan_gains_on_controlled_circuit(ctx, oracle):
     planner may absorb them into blocks, and its predicted times choose the
     candidate.  Its state equals the FP64 oracle's (relative L2 <= 1e-5,
     fidelity >= 1 - 1e-6), and it is faster than every fixed plan by at
-    least 20 % (best of 5 runs each; run-to-run spread ~1 %)."""
+    least 20 % (best of 5 runs each; run-to-run spread ~1 %).  The same
+    holds with two-gate tensor-core passes on both sides (each tensor-core
+    form also paired)."""
     import qsim_gb300 as q
     ss = q.StateSpace(ctx=ctx)
     m = L.CostMLP.load(WEIGHTS)
@@ -200,8 +206,12 @@ def test_gpu_learned_plan_gains_on_controlled_circuit(ctx, oracle):
     plans = {f"f{f}" + ("_tc" if tc else ""): E.Plan(c, max_fused_size=f,
                                                      tensor_path=tc, tc_min_k=5)
              for f in (4, 5, 6) for tc in (False, True) if tc or f < 6}
+    plans["f6_tc_pairs"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                                  tc_min_k=5, tc_pairs=2)
     plans["learned"] = E.Plan(c, max_fused_size=6, tensor_path=True,
                               tc_min_k=2, cost_model=m)
+    plans["learned_pairs"] = E.Plan(c, max_fused_size=6, tensor_path=True,
+                                    tc_min_k=2, cost_model=m, tc_pairs=2)
     times = {}
     for name, p in plans.items():
         ss.SetStateZero(st)
@@ -219,7 +229,10 @@ def test_gpu_learned_plan_gains_on_controlled_circuit(ctx, oracle):
             p.replay(ctx)
             runs.append(ctx.timer_stop())
         times[name] = min(runs)
-    best_fixed = min(v for k, v in times.items() if k != "learned")
+    best_fixed = min(v for k, v in times.items()
+                     if not k.startswith("learned") and not k.endswith("pairs"))
+    best_any = min(v for k, v in times.items() if not k.startswith("learned"))
     print("plan times (ms):", {k: round(v, 3) for k, v in times.items()},
           "passes:", {k: len(p) for k, p in plans.items()})
     assert times["learned"] * 1.2 <= best_fixed
+    assert times["learned_pairs"] * 1.2 <= best_any
