@@ -1023,19 +1023,28 @@ LEARN_GRID = dict(rows=5, cols=6, extra=2, cycles=24, seed=1)
 def pair_cost_factor(n, a, b):
     """Cost of a two-gate tensor-core pass relative to two one-gate passes,
     as the planner weighs it: the pair's 12-qubit tile is the union of both
-    target sets completed with the lowest other qubits, its run bits the
-    length of the prefix 0, 1, ... it holds, and the factor the one measured
-    for that many run bits (0.80 at >= 4, 0.87 at 3, 0.95 at 2, 1.11 else)."""
+    target sets completed with the lowest other qubits, its run bits rb the
+    length of the prefix 0, 1, ... it holds; 0.80 at rb >= 4; shorter runs
+    by the tile's other qubits below 12 (near) and in 12..20 (mid)."""
     u = set(a) | set(b)
     q = 0
     while len(u) < 12 and q < n:
         u.add(q)
         q += 1
-    run = 0
-    while run in u:
-        run += 1
-    return (0.80 if run >= 4 else 0.87 if run == 3 else 0.95 if run == 2
-            else 1.11)
+    rb = 0
+    while rb in u:
+        rb += 1
+    if rb >= 4:
+        return 0.80
+    near = sum(1 for x in u if rb <= x < 12)
+    mid = sum(1 for x in u if 12 <= x < 21)
+    if rb == 3:
+        return 0.87 if near >= 1 else 1.28
+    if rb == 2:
+        if near >= 2 or (near == 1 and mid >= 2):
+            return 0.95
+        return 1.28 if near == 1 else 2.49
+    return 1.11 if rb == 1 else 2.49
 
 
 def bench_learned_planner(ctx, ss, model, dist):
@@ -1413,10 +1422,74 @@ def kernel_case(spec: str, n: int, reps: int):
                       "norm": ss.Norm(st)}))
 
 
+def pair_shapes(n: int, reps: int):
+    """Two-gate tensor-core pass against two one-gate passes by tile shape,
+    on a uniform n-qubit state: for run bits rb = 2, 3, 4 the tile holds
+    qubits 0..rb-1, one qubit j (or none) and the rest on the highest
+    qubits from 20 up; gate A takes qubit 0 and every other tile qubit, B
+    the rest.  CUDA events on the context stream, `reps` launches, best of
+    two; one JSON line per shape (milliseconds per launch)."""
+    import numpy as np
+    import qsim_gb300 as q
+    from qsim_gb300 import _native as N
+    ctx = q.Context(0)
+    ss = q.StateSpace(ctx=ctx)
+    st = ss.Create(n)
+    ss.SetStateUniform(st)
+    rng = np.random.default_rng(0)
+    mats = []
+    for _ in range(2):
+        u, _ = np.linalg.qr(rng.normal(size=(64, 64)) +
+                            1j * rng.normal(size=(64, 64)))
+        mats.append(np.ascontiguousarray(u.astype(np.complex64)).view(np.float32))
+    ma, mb = mats
+    for rb in (2, 3, 4):
+        for j in [rb + 1, 6, 8, 10, 11, 12, 14, 16, None]:
+            tile = list(range(rb)) + ([j] if j is not None else [])
+            tile += [x for x in range(n - 1, 19, -1) if x not in tile][
+                :12 - len(tile)]
+            tile = sorted(tile)
+            if len(set(tile)) != 12:
+                continue
+            qa, qb = tile[0::2], tile[1::2]
+
+            def one(qs, mat):
+                N.check(N.lib.qsg_apply_gate_tc(ctx.h, st.get(), n,
+                                                N.u32_array(qs), 6,
+                                                mat.ctypes.data_as(N.P_f32)))
+
+            def pair():
+                N.check(N.lib.qsg_apply_gate_tc2(
+                    ctx.h, st.get(), n, N.u32_array(qa), 6,
+                    ma.ctypes.data_as(N.P_f32), N.u32_array(qb), 6,
+                    mb.ctypes.data_as(N.P_f32)))
+
+            one(qa, ma), one(qb, mb), pair()
+            ctx.sync()
+            out = {}
+            for label, fn in (("two_passes_ms", lambda: (one(qa, ma),
+                                                         one(qb, mb))),
+                              ("pair_ms", pair)):
+                ts = []
+                for _ in range(2):
+                    ctx.timer_start()
+                    for _ in range(reps):
+                        fn()
+                    ts.append(ctx.timer_stop() / reps)
+                out[label] = min(ts)
+            print(json.dumps({"n": n, "run_bits": rb, "j": j, "qa": qa, "qb": qb,
+                              **out, "ratio": out["pair_ms"] / out["two_passes_ms"],
+                              "planner_factor": pair_cost_factor(n, qa, qb)}),
+                  flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel-case", default=None,
                     help='profiling case "gate:q,..." or "tc:q,..."')
+    ap.add_argument("--pair-shapes", action="store_true",
+                    help="two-gate pass against two passes by tile shape "
+                         "(--qubits, --reps), then exit")
     ap.add_argument("--qubits", type=int, default=26)
     ap.add_argument("--reps", type=int, default=4)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1447,6 +1520,9 @@ def main():
     args = ap.parse_args()
     if args.kernel_case:
         kernel_case(args.kernel_case, args.qubits, args.reps)
+        return
+    if args.pair_shapes:
+        pair_shapes(args.qubits, args.reps)
         return
     if args.hybrid_case:
         hybrid_case(args.hybrid_case == "tc")

@@ -131,12 +131,27 @@ struct FuseOptions {
 };
 
 // Measured cost of a two-gate tensor-core pass relative to the two one-gate
-// passes it replaces, by the run bits of its tile (GB300, 30 qubits, ten
-// launches each, best of three): 1.11 at 1 run bit, 0.95 at 2, 0.87 at 3,
-// 0.78-0.82 at 4 or more.
-inline double tc_pair_cost_factor(int run_bits) {
-  return run_bits >= 4 ? 0.80 : run_bits == 3 ? 0.87 : run_bits == 2 ? 0.95
-                                                                      : 1.11;
+// passes it replaces, by the shape of its 12-qubit tile (`tile`: the mask of
+// its qubits; GB300, 30 and 32 qubits, CUDA events, best of several runs).
+// With run bits b (tile qubits 0..b-1) of 4 or more: 0.78-0.82.  Shorter
+// runs depend on the tile's other low qubits, `near` = those in [b, 12):
+// b = 3 with near >= 1 0.87-0.88, with near = 0 1.28; b = 2 with near >= 2,
+// or near = 1 and >= 2 tile qubits in [12, 21), 0.84-1.03 (0.95 taken),
+// near = 1 and the rest of the tile above 20 1.28, near = 0 2.0-2.5; b = 1
+// 1.11.
+inline double tc_pair_cost_factor(uint64_t tile) {
+  int b = 0;
+  while (b < 64 && ((tile >> b) & 1)) ++b;
+  if (b >= 4) return 0.80;
+  const uint64_t low12 = (uint64_t{1} << 12) - 1;
+  const int near = __builtin_popcountll(tile & low12 & ~((uint64_t{1} << b) - 1));
+  const int mid = __builtin_popcountll(tile & (((uint64_t{1} << 21) - 1) & ~low12));
+  if (b == 3) return near >= 1 ? 0.87 : 1.28;
+  if (b == 2) {
+    if (near >= 2 || (near == 1 && mid >= 2)) return 0.95;
+    return near == 1 ? 1.28 : 2.49;
+  }
+  return b == 1 ? 1.11 : 2.49;
 }
 // Marks pairs of consecutive tensor-core ops (tc_pair_next) that fit a
 // two-gate pass with >= `bits` run bits and are predicted faster than two

@@ -113,24 +113,29 @@ uint64_t qmask(const std::vector<unsigned>& qs) {
   return m;
 }
 
-// Run bits of the 12-qubit tile of two sorted 6-qubit target sets (their
-// union completed with the lowest other qubits; tile bits 0..b-1 are
-// qubits 0..b-1), without the kernel geometry: a quick filter before
+// The 12-qubit tile of two sorted 6-qubit target sets: the mask of their
+// union completed with the lowest other qubits (0 when the union has more
+// than 12), without the kernel geometry: a quick filter before
 // tc2_run_bits, which also builds the geometry and its swizzles.
-int tile_run_bits(unsigned n, const std::vector<unsigned>& a,
-                  const std::vector<unsigned>& b) {
+uint64_t pair_tile(unsigned n, const std::vector<unsigned>& a,
+                   const std::vector<unsigned>& b) {
   uint64_t u = 0;
   for (unsigned q : a) u |= uint64_t{1} << q;
   for (unsigned q : b) u |= uint64_t{1} << q;
   int cnt = __builtin_popcountll(u);
-  if (cnt > 12) return -1;
+  if (cnt > 12) return 0;
   for (unsigned q = 0; cnt < 12 && q < n; ++q)
     if (!((u >> q) & 1)) {
       u |= uint64_t{1} << q;
       ++cnt;
     }
+  return u;
+}
+
+// Run bits of a tile mask: the length of its prefix of qubits 0, 1, ...
+int tile_run_bits(uint64_t tile) {
   int run = 0;
-  while (run < 64 && ((u >> run) & 1)) ++run;
+  while (run < 64 && ((tile >> run) & 1)) ++run;
   return run;
 }
 
@@ -494,7 +499,7 @@ class MemoCost : public CostModel {
 };
 
 // Predicted time of a plan; a two-gate tensor-core pass costs
-// tc_pair_cost_factor(run bits) of its two blocks' one-gate passes.
+// tc_pair_cost_factor(tile) of its two blocks' one-gate passes.
 double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
   double t = 0;
   for (size_t i = 0; i < p.ops.size(); ++i) {
@@ -504,7 +509,7 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
     if (op.tc_pair_next) {
       const auto& nx = p.ops[i + 1];
       ti += m.cost_us(c.num_qubits, nx.qs, unsigned(nx.cqs.size()), nx.path);
-      ti *= tc_pair_cost_factor(tile_run_bits(c.num_qubits, op.qs, nx.qs));
+      ti *= tc_pair_cost_factor(pair_tile(c.num_qubits, op.qs, nx.qs));
       ++i;
     }
     t += ti;
@@ -513,7 +518,7 @@ double plan_cost(const Circuit& c, const Plan& p, const CostModel& m) {
 }
 
 // Passes over the state in units of one pass: a two-gate pass counts
-// 2 tc_pair_cost_factor(run bits).
+// 2 tc_pair_cost_factor(tile).
 double plan_passes(const Plan& p) {
   double t = 0;
   for (size_t i = 0; i < p.ops.size(); ++i) {
@@ -521,7 +526,7 @@ double plan_passes(const Plan& p) {
     if (op.kind == OpKind::kMeasure) continue;
     if (op.tc_pair_next) {
       t += 2.0 * tc_pair_cost_factor(
-                     tile_run_bits(p.num_qubits, op.qs, p.ops[i + 1].qs));
+                     pair_tile(p.num_qubits, op.qs, p.ops[i + 1].qs));
       ++i;
     } else {
       t += 1.0;
@@ -630,10 +635,10 @@ size_t pair_tensor_ops(Plan& plan, unsigned bits) {
   std::vector<double> gain(n, 0.0);
   for (size_t i = 0; i + 1 < n; ++i) {
     if (!tensor6(plan.ops[i]) || !tensor6(plan.ops[i + 1])) continue;
-    const int rb = tile_run_bits(plan.num_qubits, plan.ops[i].qs,
-                                 plan.ops[i + 1].qs);
-    if (rb < int(bits)) continue;
-    const double g = 2.0 * (1.0 - tc_pair_cost_factor(rb));
+    const uint64_t tile = pair_tile(plan.num_qubits, plan.ops[i].qs,
+                                    plan.ops[i + 1].qs);
+    if (!tile || tile_run_bits(tile) < int(bits)) continue;
+    const double g = 2.0 * (1.0 - tc_pair_cost_factor(tile));
     if (g <= 0) continue;
     if (tc2_run_bits(plan.num_qubits, plan.ops[i].qs.data(),
                      plan.ops[i + 1].qs.data()) < int(bits))

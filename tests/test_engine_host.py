@@ -236,10 +236,55 @@ def run_bits(a, b):
     return 12 - h if 12 - h >= 1 else -1
 
 
-def pair_factor(rb):
+def pair_tile(a, b):
+    """The two-gate tile of two padded 6-qubit target sets: their union
+    completed with the lowest other qubits to 12."""
+    u = set(a) | set(b)
+    q = 0
+    while len(u) < 12:
+        u.add(q)
+        q += 1
+    return u
+
+
+def pair_factor(a, b):
     """Measured cost of a two-gate pass relative to two one-gate passes by
-    run bits (the planner's table)."""
-    return 0.80 if rb >= 4 else 0.87 if rb == 3 else 0.95 if rb == 2 else 1.11
+    the shape of its tile (the planner's table): run bits rb, and for short
+    runs the tile's other qubits below 12 (near) and in 12..20 (mid)."""
+    u = pair_tile(a, b)
+    rb = 0
+    while rb in u:
+        rb += 1
+    if rb >= 4:
+        return 0.80
+    near = sum(1 for q in u if rb <= q < 12)
+    mid = sum(1 for q in u if 12 <= q < 21)
+    if rb == 3:
+        return 0.87 if near >= 1 else 1.28
+    if rb == 2:
+        if near >= 2 or (near == 1 and mid >= 2):
+            return 0.95
+        return 1.28 if near == 1 else 2.49
+    return 1.11 if rb == 1 else 2.49
+
+
+def test_pair_factor_by_tile_shape(E):
+    """The planner's pair cost by tile shape, at the geometries measured on
+    the GB300: long runs 0.80 whatever the rest of the tile; 64-byte runs
+    (3 run bits) need another tile qubit below 12, 32-byte runs (2) two of
+    them or one and a spread of middle qubits; otherwise the pass costs more
+    than two (1.28-2.49) and is never chosen."""
+    hi = [21, 22, 23, 24, 25, 26, 27, 28, 29]
+    assert pair_factor([0, 2, 5, 24, 26, 28], [1, 3, 23, 25, 27, 29]) == 0.80
+    assert pair_factor([0, 2, 22, 24, 26, 28], [1, 3, 23, 25, 27, 29]) == 0.80
+    assert pair_factor([0, 2, 22, 24, 26, 28], [1, 9, 23, 25, 27, 29]) == 0.87
+    assert pair_factor([0, 2, 22, 24, 26, 28], [1, 12, 23, 25, 27, 29]) == 1.28
+    assert pair_factor([0, 6] + hi[:4], [1] + hi[4:]) == 1.28
+    assert pair_factor([0, 12] + hi[:4], [1] + hi[4:]) == 2.49
+    assert pair_factor([12, 13, 14, 15, 16, 17], [0, 6, 12, 18, 24, 30]) == 0.95
+    assert pair_factor([0, 4, 10, 16, 22, 28], [4, 5, 11, 17, 23, 29]) == 0.95
+    # The 32-qubit pair that ran at 2.0x two passes in a learned plan.
+    assert pair_factor([24, 25, 26, 27, 28, 29], [12, 18, 24, 25, 30, 31]) > 2
 
 
 @pytest.mark.parametrize("bits", [1, 3, 5])
@@ -264,7 +309,8 @@ def test_two_gate_pass_pairing(E, bits):
                 and len(ops[i]["qs"]) == 6 and len(ops[i + 1]["qs"]) == 6):
             rb = run_bits(ops[i]["qs"], ops[i + 1]["qs"])
             if rb >= bits:
-                gain[i] = max(0.0, 2 * (1 - pair_factor(rb)))
+                gain[i] = max(0.0, 2 * (1 - pair_factor(ops[i]["qs"],
+                                                        ops[i + 1]["qs"])))
     cost = 0.0
     i = 0
     while i < len(ops):
