@@ -135,7 +135,7 @@ int qsg_norm(qsg_ctx* ctx, const float* state, unsigned n, double* out);
  * the reduction may need at most 4096 partial sums (8 per SM; any GPU with
  * up to 512 SMs) and larger requests fail with QSG_ERR_INVALID.  The first
  * call on a device looks up the array's device address (with that device
- * made current), so make that call before any stream capture.  The call
+ * made current).  The call
  * makes the context's device current for its duration and restores the
  * caller's device afterwards.  There is one array per device: calls that
  * overlap in time on the same device (from several threads or streams) race
