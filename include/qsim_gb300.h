@@ -323,9 +323,11 @@ typedef struct qsg_fuse_options {
   const void* cost_model;   /* a qsg_mlp* (NULL: gate-count rule) */
   /* Two-gate tensor-core passes (qsg_apply_gate_tc2): consecutive
    * tensor-core blocks share one pass over the state when their 12-qubit
-   * tile has at least this many run bits (low qubits 0..b-1 in the tile);
-   * the most such pairs are taken, and plans are compared by passes.
-   * 0: one pass per block.  No counterpart in the reference. */
+   * tile has at least this many run bits (low qubits 0..b-1 in the tile)
+   * and a pass of that tile shape measured faster than two; the set of
+   * pairs with the largest predicted saving is taken, and plans are
+   * compared by passes (a pair at its measured cost).  0: one pass per
+   * block.  No counterpart in the reference. */
   unsigned tc_pair_bits;
 } qsg_fuse_options;
 int qsg_plan_create(const qsg_circuit* c, const qsg_fuse_options* opts,

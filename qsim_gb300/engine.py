@@ -251,8 +251,10 @@ class Plan:
                  tensor_path: bool = False, tc_min_k: int = 5, seeds: int = 0,
                  cost_model=None, unfused: bool = False, tc_pairs: int = 0):
         """tc_pairs: minimum run bits of two-gate tensor-core passes (0: one
-        pass per block; from 2 run bits up a pair measured faster than two
-        passes, and the planner weighs pairs by their measured saving)."""
+        pass per block).  The planner weighs each pair by the saving
+        measured for its tile's shape (run bits, and for short runs the
+        tile's other low qubits) and takes only pairs predicted faster than
+        two passes."""
         self.circuit = circuit
         h = C.c_void_p()
         if unfused:
