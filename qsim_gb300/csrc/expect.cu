@@ -16,8 +16,8 @@
 // unit (two amplitudes)
 // and, when X flips qubits above qubit 0, its partner unit, and adds both
 // units' terms, so every amplitude is read once (8 N bytes).  Products are
-// FP32; partial sums FP32 over a thread's units of one step, FP64 across
-// steps and threads, as in the other reductions here.
+// FP32; partial sums FP32 over a thread's units of one step, compensated
+// (Kahan) FP32 across steps, FP64 across threads.
 
 #include <algorithm>
 #include <cstring>
@@ -78,7 +78,10 @@ __global__ void __launch_bounds__(kEvThreads)
     mono_ev_kernel(const float4* __restrict__ s, uint64_t work,
                    const __grid_constant__ MonoArgs a,
                    double2* __restrict__ partial) {
-  double ar = 0, ai = 0;
+  // FP32 sums per step, accumulated across steps in FP32 with Kahan
+  // compensation (s - c) and converted to FP64 once: an FP64 add per step
+  // would load GB300's narrow FP64 pipe.
+  float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
   const uint64_t tile = uint64_t(kEvThreads) * kEvUnroll;
   for (uint64_t b0 = blockIdx.x * tile; b0 < work;
        b0 += uint64_t(gridDim.x) * tile) {
@@ -123,9 +126,14 @@ __global__ void __launch_bounds__(kEvThreads)
         term(fr, fi, r1, dval<SIGNED>(k0 + 1, a), v1);
       }
     }
-    ar += double(fr);
-    ai += double(fi);
+    const float yr = fr - cr, tr = sr + yr;
+    cr = (tr - sr) - yr;
+    sr = tr;
+    const float yi = fi - ci, ti = si + yi;
+    ci = (ti - si) - yi;
+    si = ti;
   }
+  double ar = double(sr) - double(cr), ai = double(si) - double(ci);
   __shared__ double red[2][kEvThreads / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

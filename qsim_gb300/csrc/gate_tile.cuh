@@ -286,6 +286,11 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
     }
   };
 
+  // MODE 1: this thread's sum over its tiles, FP32 with Kahan compensation
+  // (s - c), added to (er, ei) in FP64 once at the end: an FP64 add per
+  // tile costs GB300's narrow FP64 pipe as much as the pass's loads.
+  float ksr = 0.f, kcr = 0.f, ksi = 0.f, kci = 0.f;
+
   // Pipeline: tiles t0 .. t0 + (STAGES-1) step are in flight on entry.
   uint64_t t = t0;
 #pragma unroll
@@ -368,8 +373,7 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
 
     if constexpr (MODE == 1) {
       // v^dagger (M v) over this item's rows: FP32 products and item sum,
-      // FP64 accumulation across items and tiles (FP64 issue is scarce on
-      // GB300).
+      // compensated FP32 accumulation across tiles, FP64 across threads.
       if (active) {
         float fr = 0.f, fi = 0.f;
         if constexpr (PAIR) {
@@ -391,8 +395,12 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
                   fmaf(v.z, acc[r + 1][1], -v.w * acc[r + 1][0]);
           }
         }
-        er += double(fr);
-        ei += double(fi);
+        const float yr = fr - kcr, tr = ksr + yr;
+        kcr = (tr - ksr) - yr;
+        ksr = tr;
+        const float yi = fi - kci, ti = ksi + yi;
+        kci = (ti - ksi) - yi;
+        ksi = ti;
       }
     } else if (active) {
       // Controlled rows keep their input where the control test fails, so
@@ -428,6 +436,10 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
     stage = stage + 1 == STAGES ? 0 : stage + 1;
   }
   cp_async_wait<0>();
+  if constexpr (MODE == 1) {
+    er += double(ksr) - double(kcr);
+    ei += double(ksi) - double(kci);
+  }
 }
 
 // MODE 0: apply, MODE 1: expectation value.
