@@ -206,6 +206,35 @@ def test_monomial_expectation_values(eng, oracle):
                 assert abs(ev - evd) < 1e-5 * max(1.0, abs(ref)), (n, k, xm)
 
 
+@pytest.mark.parametrize("n", [13, 20])
+def test_pauli_string_kernel_forms(eng, oracle, n):
+    """Pauli strings over whole tiles of work take the kernel that derives
+    a thread's units and signs from one base unit: without a partner unit
+    (Z only, or X on qubit 0), with a near partner (flipped qubits 1..10)
+    and with a far one (a flipped qubit >= 11, paired on the highest; also
+    with flips of qubits 9 and 10, whose unit bits 8, 9 are the thread's
+    own unit offsets).  Each against the FP64 oracle and against the same
+    operator with a 1e-30 off-pattern entry (the dense path)."""
+    q, ss, sim = eng
+    rng = np.random.default_rng(21 + n)
+    s0 = random_state(rng, n)
+    st = ss.Create(n)
+    ss.from_numpy(s0, st)
+    cases = [([2, 5], "ZZ"), ([0, 7], "XZ"), ([0, 3, 6], "YIZ"),
+             ([3], "X"), ([0, 5, 8], "XYZ"), ([1, 10], "YX"),
+             ([9, 10, 12], "XYZ"), ([0, 2, 9, 12], "YZXX"),
+             ([4, 11], "ZY"), ([0, 1, 6, 9, 10, 12], "XYZXYZ")]
+    for qs, word in cases:
+        m = pauli_matrix(word)
+        ref = oracle.expectation_value(c64_to_c128(s0), n, qs, m)
+        ev = sim.ExpectationValue(qs, mat32(m), st)
+        assert abs(ev - ref) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
+        md = m.copy()
+        md[0, 1 if md[0, 1] == 0 else 0] += 1e-30
+        evd = sim.ExpectationValue(qs, mat32(md), st)
+        assert abs(ev - evd) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
+
+
 def test_norm_inner_product_add_multiply(eng):
     q, ss, sim = eng
     rng = np.random.default_rng(5)
