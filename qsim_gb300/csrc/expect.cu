@@ -42,6 +42,10 @@ struct MonoArgs {
   uint32_t x0;         // bit 0 of X (qubit 0 flipped)
   uint64_t ux;         // X >> 1: partner unit offset (0: the unit itself)
   uint32_t ub;         // lowest set bit of ux (when ux != 0)
+  // Table form in mono_fast_kernel: rows of amplitude offsets 2 j
+  // kEvThreads (rj), of offset 1 (r1) and of 2 ux (rx).
+  uint32_t rj[4];
+  uint32_t r1, rx;
 };
 
 __device__ __forceinline__ uint32_t row_of(uint64_t i, const MonoArgs& a) {
@@ -155,33 +159,43 @@ __global__ void __launch_bounds__(kEvThreads)
   }
 }
 
-// Pauli-type operators (d[r] = c0 (-1)^popcount(r & zm)) with whole tiles
-// of work: S = sum_i (-1)^par(i) conj(psi_i) psi_(i ^ X), par(i) the
-// parity of i & zmask, and c0 S per block.  The per-amplitude form above
-// spends its issue on 64-bit index and sign arithmetic (the integer pipe
-// 79 % busy, DRAM 57 %, at 27 qubits); here a thread derives its kEvUnroll
-// units per step from one base unit u0 (unit j is u0 + j kEvThreads, bits
-// 8..9 of u0 clear) and the signs from one parity: par(2 (u0 + j kEvThreads))
-// = par(2 u0) ^ par(2 j kEvThreads), the unit's second amplitude adds bit 0
-// of zmask, the partner unit u ^ ux adds par(2 ux).  FORM 0: no partner
-// unit (X on qubit 0 at most).  FORM 1: the partner is far (a set bit of ux
-// at or above bit 10, `ub` the highest): work items are the units with bit
-// ub clear, each with its partner, every amplitude once.  FORM 2: the
-// partner is near (ux < 1024, inside the same tile of 1024 units): every
-// unit takes its own two terms and reads its partner, which the tile's
-// other threads read too (a cache hit, DRAM still reads each byte once).
-template <int FORM, bool X0>
+// Monomial operators over whole tiles of work, one thread deriving its
+// kEvUnroll units per step from one base unit u0 (unit j is u0 + j
+// kEvThreads, bits 8..9 of u0 clear).  The per-amplitude form above spends
+// its issue on 64-bit index and sign arithmetic (the integer pipe 79 %
+// busy, DRAM 57 %, at 27 qubits).  SIGNED (Pauli-type, d[r] = c0
+// (-1)^popcount(r & zm)): S = sum_i (-1)^par(i) conj(psi_i) psi_(i ^ X),
+// par(i) the parity of i & zmask, and c0 S per block; par(2 (u0 + j
+// kEvThreads)) = par(2 u0) ^ par(2 j kEvThreads), the unit's second
+// amplitude adds bit 0 of zmask, the partner unit u ^ ux adds par(2 ux).
+// Table form: the row r(i) of amplitude i (its target bits) is r(2 u0)
+// | rj[j] for unit j, | r1 for the unit's second amplitude, ^ rx for the
+// partner unit; d[r] from shared memory.  FORM 0: no partner unit (X on
+// qubit 0 at most).  FORM 1: the partner is far (a set bit of ux at or
+// above bit 10, `ub` the highest): work items are the units with bit ub
+// clear, each with its partner, every amplitude once.  FORM 2: the partner
+// is near (ux < 1024, inside the same tile of 1024 units): every unit takes
+// its own two terms and reads its partner, which the tile's other threads
+// read too (a cache hit, DRAM still reads each byte once).
+template <int FORM, bool X0, bool SIGNED>
 __global__ void __launch_bounds__(kEvThreads)
-    mono_sign_kernel(const float4* __restrict__ s, uint64_t work,
+    mono_fast_kernel(const float4* __restrict__ s, uint64_t work,
                      const __grid_constant__ MonoArgs a,
                      double2* __restrict__ partial) {
   constexpr uint64_t kTile = uint64_t(kEvThreads) * kEvUnroll;
   static_assert(kTile == 1024, "unit offsets j kEvThreads use bits 8..9");
+  static_assert(kEvUnroll == 4, "rj holds four rows");
   const uint32_t tid = threadIdx.x;
+  __shared__ float2 dtab[SIGNED ? 1 : 64];
+  if constexpr (!SIGNED) {
+    if (tid < 64) dtab[tid] = a.d[tid];
+    __syncthreads();
+  }
   uint32_t pj[kEvUnroll];
 #pragma unroll
   for (int j = 0; j < kEvUnroll; ++j)
-    pj[j] = __popcll((uint64_t(2 * j) * kEvThreads) & a.zmask) & 1u;
+    pj[j] = SIGNED ? __popcll((uint64_t(2 * j) * kEvThreads) & a.zmask) & 1u
+                   : a.rj[j];
   // Signs as floats: bit 0 of zmask (second amplitude of a unit), the
   // partner unit's parity.
   const float f_z0 = (a.zmask & 1) ? -1.f : 1.f;
@@ -193,6 +207,13 @@ __global__ void __launch_bounds__(kEvThreads)
     er = fmaf(sg, tr, er);
     ei = fmaf(sg, ti, ei);
   };
+  // conj(p) d q.
+  auto acc_d = [](float& er, float& ei, float2 d, float2 p, float2 q) {
+    const float qr = fmaf(d.x, q.x, -d.y * q.y);
+    const float qi = fmaf(d.x, q.y, d.y * q.x);
+    er = fmaf(p.x, qr, fmaf(p.y, qi, er));
+    ei = fmaf(p.x, qi, fmaf(-p.y, qr, ei));
+  };
   for (uint64_t b0 = blockIdx.x * kTile; b0 < work;
        b0 += uint64_t(gridDim.x) * kTile) {
     const uint64_t w = b0 + tid;
@@ -201,7 +222,8 @@ __global__ void __launch_bounds__(kEvThreads)
       const uint64_t lo = w & ((uint64_t{1} << a.ub) - 1);
       u0 = lo | ((w ^ lo) << 1);
     }
-    const uint32_t par0 = __popcll((2 * u0) & a.zmask) & 1u;
+    const uint32_t par0 =
+        SIGNED ? __popcll((2 * u0) & a.zmask) & 1u : row_of(2 * u0, a);
     const float4* sp = s + u0;
     const uint64_t v0 = u0 ^ a.ux;
     float4 x[kEvUnroll], y[kEvUnroll];
@@ -213,10 +235,28 @@ __global__ void __launch_bounds__(kEvThreads)
     float fr = 0.f, fi = 0.f;
 #pragma unroll
     for (int j = 0; j < kEvUnroll; ++j) {
-      const float sa = __int_as_float(0x3f800000u | ((par0 ^ pj[j]) << 31));
-      const float sb = sa * f_z0;
       const float2 p0 = make_float2(x[j].x, x[j].y);
       const float2 p1 = make_float2(x[j].z, x[j].w);
+      if constexpr (!SIGNED) {
+        const uint32_t ra = par0 | pj[j], rb = ra | a.r1;
+        if constexpr (FORM == 0) {
+          acc_d(fr, fi, dtab[ra], p0, X0 ? p1 : p0);
+          acc_d(fr, fi, dtab[rb], p1, X0 ? p0 : p1);
+        } else {
+          const float2 r0 = make_float2(y[j].x, y[j].y);
+          const float2 r1 = make_float2(y[j].z, y[j].w);
+          acc_d(fr, fi, dtab[ra], p0, X0 ? r1 : r0);
+          acc_d(fr, fi, dtab[rb], p1, X0 ? r0 : r1);
+          if constexpr (FORM == 1) {
+            const uint32_t rc = ra ^ a.rx, rd = rc | a.r1;
+            acc_d(fr, fi, dtab[rc], r0, X0 ? p1 : p0);
+            acc_d(fr, fi, dtab[rd], r1, X0 ? p0 : p1);
+          }
+        }
+        continue;
+      }
+      const float sa = __int_as_float(0x3f800000u | ((par0 ^ pj[j]) << 31));
+      const float sb = sa * f_z0;
       if constexpr (FORM == 0) {
         acc(fr, fi, sa, p0, X0 ? p1 : p0);
         acc(fr, fi, sb, p1, X0 ? p0 : p1);
@@ -257,7 +297,7 @@ __global__ void __launch_bounds__(kEvThreads)
       sr2 += red[0][i];
       si2 += red[1][i];
     }
-    const double c0r = a.c0.x, c0i = a.c0.y;
+    const double c0r = SIGNED ? a.c0.x : 1.0, c0i = SIGNED ? a.c0.y : 0.0;
     partial[blockIdx.x] =
         make_double2(c0r * sr2 - c0i * si2, c0r * si2 + c0i * sr2);
   }
@@ -323,11 +363,11 @@ int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
   const uint64_t units = n == 0 ? 1 : (uint64_t{1} << (n - 1));
   uint64_t work = a.ux ? units / 2 : units;
   const uint64_t per_block = uint64_t(kEvThreads) * kEvUnroll;
-  // Pauli-type operators over whole tiles take mono_sign_kernel: FORM 0
-  // without a partner unit, 2 with a near one (ux < one tile), 1 with a far
-  // one (paired on the highest bit of ux).
+  // Whole tiles of work take mono_fast_kernel: FORM 0 without a partner
+  // unit, 2 with a near one (ux < one tile), 1 with a far one (paired on
+  // the highest bit of ux).
   int form = -1;
-  if (signed_form) {
+  {
     const uint64_t wf = a.ux == 0 || a.ux < per_block ? units : units / 2;
     if (wf % per_block == 0) {
       form = a.ux == 0 ? 0 : a.ux < per_block ? 2 : 1;
@@ -335,6 +375,15 @@ int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
       if (form == 1) a.ub = 63u - unsigned(__builtin_clzll(a.ux));
     }
   }
+  auto row = [&](uint64_t i) {
+    uint32_t r = 0;
+    for (unsigned j = 0; j < k; ++j) r |= uint32_t((i >> qs[j]) & 1) << j;
+    return r;
+  };
+  for (int j = 0; j < kEvUnroll; ++j)
+    a.rj[j] = row(uint64_t(2 * j) * kEvThreads);
+  a.r1 = row(1);
+  a.rx = row(2 * a.ux);
   uint64_t grid = (work + per_block - 1) / per_block;
   grid = std::min<uint64_t>(grid, uint64_t(ctx->num_sms) * 8);
   if (grid < 1) grid = 1;
@@ -344,19 +393,29 @@ int expectation_monomial(qsg_ctx* ctx, const float* state, unsigned n,
   double2* partial = static_cast<double2*>(p);
   const float4* sv = reinterpret_cast<const float4*>(state);
   const unsigned gb = unsigned(grid);
-  switch (form < 0 ? -1 : 2 * form + (a.x0 ? 1 : 0)) {
-    case 0: mono_sign_kernel<0, false><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
-    case 1: mono_sign_kernel<0, true><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
-    case 2: mono_sign_kernel<1, false><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
-    case 3: mono_sign_kernel<1, true><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
-    case 4: mono_sign_kernel<2, false><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
-    case 5: mono_sign_kernel<2, true><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial); break;
+#define QSG_MONO(F, X, S)                                                   \
+  mono_fast_kernel<F, X, S><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, \
+                                                               partial)
+  switch (form < 0 ? -1 : 4 * form + 2 * (a.x0 ? 1 : 0) + (signed_form ? 1 : 0)) {
+    case 0: QSG_MONO(0, false, false); break;
+    case 1: QSG_MONO(0, false, true); break;
+    case 2: QSG_MONO(0, true, false); break;
+    case 3: QSG_MONO(0, true, true); break;
+    case 4: QSG_MONO(1, false, false); break;
+    case 5: QSG_MONO(1, false, true); break;
+    case 6: QSG_MONO(1, true, false); break;
+    case 7: QSG_MONO(1, true, true); break;
+    case 8: QSG_MONO(2, false, false); break;
+    case 9: QSG_MONO(2, false, true); break;
+    case 10: QSG_MONO(2, true, false); break;
+    case 11: QSG_MONO(2, true, true); break;
     default:
       if (signed_form)
         mono_ev_kernel<true><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial);
       else
         mono_ev_kernel<false><<<gb, kEvThreads, 0, ctx->stream>>>(sv, work, a, partial);
   }
+#undef QSG_MONO
   QSG_LAUNCHED(ctx);
   return reduce_partials_d2(ctx, partial, grid, out_re_im);
 }

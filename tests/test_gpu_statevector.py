@@ -207,14 +207,16 @@ def test_monomial_expectation_values(eng, oracle):
 
 
 @pytest.mark.parametrize("n", [13, 20])
-def test_pauli_string_kernel_forms(eng, oracle, n):
-    """Pauli strings over whole tiles of work take the kernel that derives
-    a thread's units and signs from one base unit: without a partner unit
-    (Z only, or X on qubit 0), with a near partner (flipped qubits 1..10)
-    and with a far one (a flipped qubit >= 11, paired on the highest; also
-    with flips of qubits 9 and 10, whose unit bits 8, 9 are the thread's
-    own unit offsets).  Each against the FP64 oracle and against the same
-    operator with a 1e-30 off-pattern entry (the dense path)."""
+def test_monomial_kernel_forms(eng, oracle, n):
+    """Monomial operators over whole tiles of work take the kernel that
+    derives a thread's units, signs and table rows from one base unit:
+    without a partner unit (Z only, or X on qubit 0), with a near partner
+    (flipped qubits 1..10) and with a far one (a flipped qubit >= 11,
+    paired on the highest; also with flips of qubits 9 and 10, whose unit
+    bits 8, 9 are the thread's own unit offsets).  Each Pauli string (sign
+    form) and a monomial with random entries on the same pattern (table
+    form) against the FP64 oracle, and against the same operator with a
+    1e-30 off-pattern entry (the dense path)."""
     q, ss, sim = eng
     rng = np.random.default_rng(21 + n)
     s0 = random_state(rng, n)
@@ -225,14 +227,20 @@ def test_pauli_string_kernel_forms(eng, oracle, n):
              ([9, 10, 12], "XYZ"), ([0, 2, 9, 12], "YZXX"),
              ([4, 11], "ZY"), ([0, 1, 6, 9, 10, 12], "XYZXYZ")]
     for qs, word in cases:
-        m = pauli_matrix(word)
-        ref = oracle.expectation_value(c64_to_c128(s0), n, qs, m)
-        ev = sim.ExpectationValue(qs, mat32(m), st)
-        assert abs(ev - ref) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
-        md = m.copy()
-        md[0, 1 if md[0, 1] == 0 else 0] += 1e-30
-        evd = sim.ExpectationValue(qs, mat32(md), st)
-        assert abs(ev - evd) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
+        pm = pauli_matrix(word)
+        dim = len(pm)
+        xm = int(np.flatnonzero(pm[0])[0])
+        tm = np.zeros_like(pm)
+        for r in range(dim):
+            tm[r, r ^ xm] = complex(rng.normal(), rng.normal())
+        for m in (pm, tm):
+            ref = oracle.expectation_value(c64_to_c128(s0), n, qs, c64_to_c128(m))
+            ev = sim.ExpectationValue(qs, mat32(m), st)
+            assert abs(ev - ref) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
+            md = m.copy()
+            md[0, 1 if md[0, 1] == 0 else 0] += 1e-30
+            evd = sim.ExpectationValue(qs, mat32(md), st)
+            assert abs(ev - evd) < 1e-5 * max(1.0, abs(ref)), (n, qs, word)
 
 
 def test_norm_inner_product_add_multiply(eng):
