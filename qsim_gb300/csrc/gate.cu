@@ -161,7 +161,7 @@ static int launch_tile(qsg_ctx* ctx, float* state, unsigned n,
   if (grid < 1) grid = 1;
 
   double2* partial = nullptr;
-  if (MODE == 1) {
+  if (MODE >= 1) {
     void* p = nullptr;
     int rc = get_scratch(ctx, (grid + 1) * sizeof(double2), &p);
     if (rc) return rc;
@@ -171,7 +171,7 @@ static int launch_tile(qsg_ctx* ctx, float* state, unsigned n,
       reinterpret_cast<float4*>(state), a, partial);
   QSG_LAUNCHED(ctx);
 
-  if (MODE == 1) {
+  if (MODE >= 1) {
     return reduce_partials_d2(ctx, partial, grid, out_re_im);
   }
   return QSG_OK;
@@ -209,6 +209,43 @@ static int dispatch(qsg_ctx* ctx, float* state, unsigned n,
 #undef QSG_CASE
   set_error("gates on %u qubits are not supported (maximum 6)", k);
   return QSG_ERR_UNSUPPORTED;
+}
+
+// ExpectationValue of a Hermitian matrix on 1..3 qubits: the tile kernel's
+// MODE 2 (the upper triangle of the matrix, half the products of MODE 1).
+static int dispatch_hermitian_ev(qsg_ctx* ctx, const float* state, unsigned n,
+                                 const unsigned* qs, unsigned k,
+                                 const float* matrix, double* out) {
+  float* s = const_cast<float*>(state);
+  const bool pair = qs[0] != 0;
+#define QSG_HCASE(KK)                                                          \
+  case KK:                                                                     \
+    return pair ? launch_tile<KK, true, 2>(ctx, s, n, qs, nullptr, 0, 0,        \
+                                           matrix, nullptr, out)               \
+                : launch_tile<KK, false, 2>(ctx, s, n, qs, nullptr, 0, 0,       \
+                                            matrix, nullptr, out);
+  switch (k) {
+    QSG_HCASE(1)
+    QSG_HCASE(2)
+    QSG_HCASE(3)
+    default:
+      break;
+  }
+#undef QSG_HCASE
+  set_error("Hermitian expectation values take 1..3 qubits (got %u)", k);
+  return QSG_ERR_UNSUPPORTED;
+}
+
+// m == m^dagger exactly (FP32 entries).
+static bool is_hermitian(const float* m, unsigned k) {
+  const unsigned d = 1u << k;
+  for (unsigned r = 0; r < d; ++r)
+    for (unsigned c = r; c < d; ++c) {
+      const float* a = m + 2 * (r * d + c);
+      const float* b = m + 2 * (c * d + r);
+      if (a[0] != b[0] || a[1] != -b[1]) return false;
+    }
+  return true;
 }
 
 int apply_gate_prepare(unsigned k, bool pair, int mode) {
@@ -323,6 +360,9 @@ int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
                                   &overflow);
     if (rc != QSG_OK || !overflow) return rc;
   }
+  // Hermitian operators of <= 3 qubits (observables): half the products.
+  if (k <= 3 && is_hermitian(matrix, k))
+    return dispatch_hermitian_ev(ctx, state, n, qs, k, matrix, out_re_im);
   return dispatch<1>(ctx, const_cast<float*>(state), n, qs, k, nullptr, 0, 0,
                      matrix, out_re_im);
 }

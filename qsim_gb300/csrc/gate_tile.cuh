@@ -209,7 +209,10 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float2 m, float vr,
 
 // One CTA's share of a gate pass: tiles t0, t0 + step, ... of geometry g,
 // pipelined through STAGES shared-memory tile buffers (cp.async).  MODE 0
-// applies the matrix, MODE 1 accumulates <s|M|s> into (er, ei).  SMAT: the
+// applies the matrix, MODE 1 accumulates <s|M|s> into (er, ei), MODE 2 (a
+// Hermitian M, k <= 3: one thread holds every row) accumulates it as
+// sum_r M_rr |v_r|^2 + 2 Re conj(v_r) sum_(c > r) M_rc v_c, half the
+// products, with ei = 0.  SMAT: the
 // matrix is read column-major from `smat` (2^k x 2^k float2, staged by the
 // caller); otherwise from the accessor M.  PRE: the tile-invariant parts of
 // every load and store address are computed once per pass and kept in
@@ -348,9 +351,11 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
       } else if constexpr (PAIR) {
 #pragma unroll
         for (int c = 0; c < D; ++c) {
+          if (MODE == 2 && c == 0) continue;
           const float4 v = cur[((e | g.moff[c]) >> 1) ^ swe];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
+            if (MODE == 2 && r >= c) continue;
             const float2 m = M(r, c);
             cmac(acc[r][0], acc[r][1], m, v.x, v.y);
             cmac(acc[r][2], acc[r][3], m, v.z, v.w);
@@ -362,16 +367,50 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
           const float4 v = cur[((e | g.moff[2 * p]) >> 1) ^ swe];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const float2 m0 = M(r, 2 * p);
-            const float2 m1 = M(r, 2 * p + 1);
-            cmac(acc[r][0], acc[r][1], m0, v.x, v.y);
-            cmac(acc[r][0], acc[r][1], m1, v.z, v.w);
+            if (MODE != 2 || r < 2 * p) {
+              const float2 m0 = M(r, 2 * p);
+              cmac(acc[r][0], acc[r][1], m0, v.x, v.y);
+            }
+            if (MODE != 2 || r < 2 * p + 1) {
+              const float2 m1 = M(r, 2 * p + 1);
+              cmac(acc[r][0], acc[r][1], m1, v.z, v.w);
+            }
           }
         }
       }
     }
 
-    if constexpr (MODE == 1) {
+    if constexpr (MODE == 2) {
+      // Hermitian: diagonal |v_r|^2 terms plus twice the real part of
+      // conj(v_r) times the upper-triangle sums.
+      if (active) {
+        float fr = 0.f;
+        if constexpr (PAIR) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float4 v = cur[((e | g.moff[r]) >> 1) ^ swe];
+            const float d = M(r, r).x;
+            const float n2 = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w)));
+            const float o = fmaf(v.x, acc[r][0], fmaf(v.y, acc[r][1],
+                            fmaf(v.z, acc[r][2], v.w * acc[r][3])));
+            fr = fmaf(d, n2, fmaf(2.f, o, fr));
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; r += 2) {
+            const float4 v = cur[((e | g.moff[r]) >> 1) ^ swe];
+            const float d0 = M(r, r).x, d1 = M(r + 1, r + 1).x;
+            const float o = fmaf(v.x, acc[r][0], fmaf(v.y, acc[r][1],
+                            fmaf(v.z, acc[r + 1][0], v.w * acc[r + 1][1])));
+            fr = fmaf(d0, fmaf(v.x, v.x, v.y * v.y),
+                      fmaf(d1, fmaf(v.z, v.z, v.w * v.w), fmaf(2.f, o, fr)));
+          }
+        }
+        const float yr = fr - kcr, tr = ksr + yr;
+        kcr = (tr - ksr) - yr;
+        ksr = tr;
+      }
+    } else if constexpr (MODE == 1) {
       // v^dagger (M v) over this item's rows: FP32 products and item sum,
       // compensated FP32 accumulation across tiles, FP64 across threads.
       if (active) {
@@ -436,13 +475,14 @@ __device__ __forceinline__ void tile_pass(float4* __restrict__ st,
     stage = stage + 1 == STAGES ? 0 : stage + 1;
   }
   cp_async_wait<0>();
-  if constexpr (MODE == 1) {
+  if constexpr (MODE >= 1) {
     er += double(ksr) - double(kcr);
     ei += double(ksi) - double(kci);
   }
 }
 
-// MODE 0: apply, MODE 1: expectation value.
+// MODE 0: apply, MODE 1: expectation value, MODE 2: expectation value of a
+// Hermitian matrix (k <= 3).
 // k = 4 keeps its addresses in registers (PRE) at four CTAs per SM: 15 %
 // faster than five CTAs without (3.40 against 4.1 ms per 30-qubit pass).
 template <int K, bool PAIR, int MODE>
@@ -470,7 +510,7 @@ __global__ void __launch_bounds__(kTileThreads, K <= 4 ? 4 : 5)
   tile_pass<K, PAIR, MODE, SH::SMEM_MAT, SH::STAGES, K == 4>(
       st, a.g, MatAccess<K>{a}, smat, smem, blockIdx.x, gridDim.x, er, ei);
 
-  if constexpr (MODE == 1) {
+  if constexpr (MODE >= 1) {
     // Block reduction of (er, ei) in FP64, fixed order.
     __shared__ double red[2][kTileThreads / 32];
 #pragma unroll

@@ -177,6 +177,38 @@ def test_expectation_values_random(eng, oracle):
                 assert abs(ev - ref) < 1e-5 * max(1.0, abs(ref)), (n, qs)
 
 
+def test_hermitian_expectation_values(eng, oracle):
+    """Hermitian operators of 1..3 qubits take the tile kernel's Hermitian
+    mode (the diagonal and twice the real part of the upper triangle, half
+    the products): against the FP64 oracle, with and without qubit 0 among
+    the targets, and against the general mode on the same matrix made
+    non-Hermitian by a 1e-30 imaginary part on one diagonal entry."""
+    q, ss, sim = eng
+    rng = np.random.default_rng(13)
+    for n in (3, 9, 14, 20):
+        s0 = random_state(rng, n)
+        st = ss.Create(n)
+        ss.from_numpy(s0, st)
+        for k in (1, 2, 3):
+            for with0 in (True, False):
+                if k + (0 if with0 else 1) > n:
+                    continue
+                pool = list(range(n)) if with0 else list(range(1, n))
+                qs = sorted(rng.choice(pool, size=k, replace=False).tolist())
+                if with0 and 0 not in qs:
+                    qs = sorted([0] + qs[1:])
+                z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+                h = c64_to_c128((z + z.conj().T) / 2)
+                ref = oracle.expectation_value(c64_to_c128(s0), n, qs, h)
+                ev = sim.ExpectationValue(qs, mat32(h), st)
+                assert abs(ev - ref) < 1e-5 * max(1.0, abs(ref)), (n, k, qs)
+                assert ev.imag == 0.0
+                g = h.copy()
+                g[0, 0] += 1e-30j
+                evg = sim.ExpectationValue(qs, mat32(g), st)
+                assert abs(ev - evg) < 1e-5 * max(1.0, abs(ref)), (n, k, qs)
+
+
 def test_monomial_expectation_values(eng, oracle):
     """Monomial operators (one nonzero per row at column r ^ xm: Pauli
     strings, diagonal gates, phased permutations) take the one-pass kernel;
