@@ -103,6 +103,10 @@ struct PlanOp {
   // Tensor-core ops only: this op and the next one run as one two-gate
   // tensor-core pass (one read and one write of the state).
   bool tc_pair_next = false;
+  // Every member gate is unitary (M^dagger M = 1 within 1e-5 per entry),
+  // so the block is: set when the op is built from its members; the
+  // runner's norm carry needs it.
+  bool unitary = false;
 };
 
 struct Plan {

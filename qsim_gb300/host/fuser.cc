@@ -16,6 +16,7 @@
 // (cost of the block) per block, i.e. the most time saved.
 
 #include <algorithm>
+#include <cmath>
 #include <future>
 #include <unordered_map>
 #include <utility>
@@ -139,7 +140,27 @@ int tile_run_bits(uint64_t tile) {
   return run;
 }
 
+// M^dagger M = 1 within 1e-5 per entry (M row-major, d x d).
+bool unitary_matrix(const std::vector<cplx>& m) {
+  const size_t d = size_t(std::sqrt(double(m.size())) + 0.5);
+  for (size_t r = 0; r < d; ++r)
+    for (size_t c = r; c < d; ++c) {
+      cplx a = 0;
+      for (size_t j = 0; j < d; ++j) a += std::conj(m[j * d + r]) * m[j * d + c];
+      if (std::abs(a - (r == c ? 1.0 : 0.0)) > 1e-5) return false;
+    }
+  return true;
+}
+
 void finish(const Circuit& c, PlanOp& p) {
+  // A block is unitary when every member gate is: the members are small
+  // (usually 1-2 qubits), the block up to 64 x 64.
+  p.unitary = p.kind != OpKind::kMeasure && !p.members.empty();
+  for (int mi : p.members)
+    if (!unitary_matrix(c.ops[mi].m)) {
+      p.unitary = false;
+      break;
+    }
   if (p.kind == OpKind::kGate) {
     if (p.members.size() == 1 && c.ops[p.members[0]].qs == p.qs) {
       p.m = c.ops[p.members[0]].m;

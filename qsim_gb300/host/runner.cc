@@ -49,21 +49,6 @@ void PlanRuntime::release() {
   tc_ready = false;
 }
 
-namespace {
-
-bool is_unitary(const std::vector<cplx>& m) {
-  const size_t d = size_t(std::sqrt(double(m.size())) + 0.5);
-  for (size_t r = 0; r < d; ++r)
-    for (size_t c = 0; c < d; ++c) {
-      cplx a = 0;
-      for (size_t j = 0; j < d; ++j) a += std::conj(m[j * d + r]) * m[j * d + c];
-      if (std::abs(a - (r == c ? 1.0 : 0.0)) > 1e-5) return false;
-    }
-  return true;
-}
-
-}  // namespace
-
 int PlanRuntime::upload(qsg_ctx* c) {
   if (uploaded) return QSG_OK;
   ctx = c;
@@ -74,8 +59,11 @@ int PlanRuntime::upload(qsg_ctx* c) {
     if (op.kind == OpKind::kGate && op.path == Path::kTensor) tc = true;
   }
   if (tc && unitary) {
+    // Known from the member gates (set at fusion), not recomputed here:
+    // a 64 x 64 product check per block cost ~0.3 ms of host time per
+    // tensor-core op on every run of a new plan.
     for (const auto& op : plan.ops)
-      if (!is_unitary(op.m)) {
+      if (!op.unitary) {
         unitary = false;
         break;
       }

@@ -249,6 +249,46 @@ def test_tc2_rejects_pairs_that_do_not_fit(eng):
     assert tc_error(N, ctx) == 0
 
 
+def test_tc_plan_with_a_non_unitary_gate(eng, oracle):
+    """A tensor-core plan whose circuit holds one non-unitary gate runs
+    without the norm carry (a block is unitary only when all its member
+    gates are, known from fusion): the oracle's state, norm included;
+    the same circuit without that gate keeps the carry and its norm."""
+    q, E, N, ctx, ss, sim = eng
+    rng = np.random.default_rng(31)
+    n = 14
+
+    def circuit(with_bad):
+        c = E.Circuit(n)
+        t = 0
+        for layer in range(10):
+            for a in range(layer % 2, n - 1, 2):
+                z = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+                u, _ = np.linalg.qr(z)
+                c.add_gate(t, [a, a + 1], u)
+            t += 1
+            if with_bad and layer == 4:
+                c.add_gate(t, [3, 4], np.diag([1.0, 0.6, 0.9, 1.3]).astype(complex))
+                t += 1
+        return c
+
+    for with_bad in (True, False):
+        c = circuit(with_bad)
+        plan = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=1,
+                      tc_pairs=2)
+        want = oracle.zero_state(n)
+        for o in c.ops():
+            oracle.apply_gate(want, n, o["qs"], o["m"])
+        st = ss.Create(n)
+        ss.SetStateZero(st)
+        plan.run(ctx, st)
+        got = ss.to_numpy(st)
+        assert rel_l2(got, want) < 1e-5, with_bad
+        if not with_bad:
+            assert abs(np.linalg.norm(got) - 1) < 1e-6
+    assert tc_error(N, ctx) == 0
+
+
 @pytest.mark.parametrize("bits", [1, 3])
 def test_tc2_plans_match_oracle(eng, oracle, bits):
     """Plans whose consecutive tensor-core blocks share two-gate passes
