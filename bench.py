@@ -1483,10 +1483,73 @@ def pair_shapes(n: int, reps: int):
                   flush=True)
 
 
+def ev_shapes(n: int, reps: int):
+    """ExpectationValue per call (CUDA events on the context stream, the
+    reduction and the read-back of the result included) on a uniform
+    n-qubit state, one JSON line per operator: dense Hermitian and general
+    matrices of 1..3 qubits (CUDA-core tile kernel), Pauli strings and
+    phased permutations (the monomial kernels, every partner form)."""
+    import ctypes as Cx
+    import numpy as np
+    import qsim_gb300 as q
+    from qsim_gb300 import _native as N
+    ctx = q.Context(0)
+    ss = q.StateSpace(ctx=ctx)
+    st = ss.Create(n)
+    ss.SetStateUniform(st)
+    rng = np.random.default_rng(0)
+    pauli = {"I": np.eye(2), "X": np.array([[0, 1], [1, 0]]),
+             "Y": np.array([[0, -1j], [1j, 0]]), "Z": np.diag([1, -1])}
+    cases = []
+    for qs in ([0], [17], [0, 1], [5, 23], [0, 9, 28], [4, 12, 20]):
+        d = 1 << len(qs)
+        z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+        cases.append(("hermitian", qs, (z + z.conj().T) / 2))
+        cases.append(("general", qs, z))
+    for qs, word in (([0, 5, 9], "ZZZ"), ([0, 3, 6], "XYZ"),
+                     ([0, 5, 11], "XZY"), ([1, 7, 13, 20, 26, 29], "XYZXYZ")):
+        m = np.eye(1)
+        for ch in word:
+            m = np.kron(pauli[ch], m)
+        cases.append(("pauli " + word, qs, m))
+    for qs, xm in (([0, 5, 9], 0), ([3, 8], 1), ([2, 3, 19, 27], 0b1100)):
+        d = 1 << len(qs)
+        m = np.zeros((d, d), complex)
+        for r in range(d):
+            m[r, r ^ xm] = np.exp(1j * rng.uniform(0, 2 * np.pi))
+        cases.append(("monomial", qs, m))
+    out = (Cx.c_double * 2)()
+    for kind, qs, mat in cases:
+        qs = [x for x in qs if x < n]
+        if len(qs) != int(np.log2(len(mat))):
+            continue
+        m32 = np.ascontiguousarray(mat.astype(np.complex64)).view(np.float32)
+
+        def f():
+            N.check(N.lib.qsg_expectation_value(
+                ctx.h, st.get(), n, N.u32_array(qs), len(qs),
+                m32.ctypes.data_as(N.P_f32), out))
+
+        f(), f()
+        ts = []
+        for _ in range(3):
+            ctx.timer_start()
+            for _ in range(reps):
+                f()
+            ts.append(ctx.timer_stop() / reps)
+        ms = min(ts)
+        print(json.dumps({"n": n, "operator": kind, "qs": qs, "ms": ms,
+                          "alg_gbs": 8 * (1 << n) / (ms * 1e-3) / 1e9,
+                          "ev": [out[0], out[1]]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel-case", default=None,
                     help='profiling case "gate:q,..." or "tc:q,..."')
+    ap.add_argument("--ev-shapes", action="store_true",
+                    help="ExpectationValue per call by operator kind "
+                         "(--qubits, --reps), then exit")
     ap.add_argument("--pair-shapes", action="store_true",
                     help="two-gate pass against two passes by tile shape "
                          "(--qubits, --reps), then exit")
@@ -1523,6 +1586,9 @@ def main():
         return
     if args.pair_shapes:
         pair_shapes(args.qubits, args.reps)
+        return
+    if args.ev_shapes:
+        ev_shapes(args.qubits, args.reps)
         return
     if args.hybrid_case:
         hybrid_case(args.hybrid_case == "tc")
