@@ -191,6 +191,8 @@ __global__ void __launch_bounds__(kEvThreads)
     if (tid < 64) dtab[tid] = a.d[tid];
     __syncthreads();
   }
+  // Per unit offset j: its parity (SIGNED) or its table-row bits; par0
+  // below is likewise the base unit's parity or table row.
   uint32_t pj[kEvUnroll];
 #pragma unroll
   for (int j = 0; j < kEvUnroll; ++j)
