@@ -5,7 +5,7 @@ MultiQubitGateFuser, and the synthetic workload generators."""
 import numpy as np
 import pytest
 
-from conftest import load_golden, rel_l2
+from conftest import ROOT, load_golden, rel_l2
 
 
 @pytest.fixture(scope="module")
@@ -285,6 +285,28 @@ def test_pair_factor_by_tile_shape(E):
     assert pair_factor([0, 4, 10, 16, 22, 28], [4, 5, 11, 17, 23, 29]) == 0.95
     # The 32-qubit pair that ran at 2.0x two passes in a learned plan.
     assert pair_factor([24, 25, 26, 27, 28, 29], [12, 18, 24, 25, 30, 31]) > 2
+
+
+def test_bench_pair_factor_is_the_planners():
+    """bench.py predicts plan times with the planner's pair table: its
+    mirror agrees with this file's on random pairs of 6-qubit target sets
+    (whose planner consistency test_two_gate_pass_pairing checks)."""
+    import importlib
+    import sys
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    rng = np.random.default_rng(3)
+    n = 30
+    seen = set()
+    for _ in range(400):
+        a = sorted(rng.choice(n, 6, replace=False).tolist())
+        b = sorted(rng.choice(n, 6, replace=False).tolist())
+        if len(set(a) | set(b)) > 12:
+            continue
+        f = pair_factor(a, b)
+        assert bench.pair_cost_factor(n, a, b) == f, (a, b)
+        seen.add(f)
+    assert len(seen) >= 3
 
 
 @pytest.mark.parametrize("bits", [1, 3, 5])
