@@ -198,7 +198,14 @@ int qsg_apply_controlled_gate(qsg_ctx* ctx, float* state, unsigned n,
                               const unsigned* qs, unsigned k,
                               const unsigned* cqs, unsigned c, uint64_t cvals,
                               const float* matrix);
-/* ExpectationValue (:216-260): <s| M_qs |s> in FP64 -> out_re_im[2]. */
+/* ExpectationValue (:216-260): <s| M_qs |s> in FP64 -> out_re_im[2].
+ * One read of the state for every operator: monomial operators (one
+ * nonzero per row: Pauli strings, diagonal and phased-permutation
+ * operators) take a one-pass kernel; dense Hermitian operators of 1..3
+ * qubits sum the diagonal and twice the real part of the upper triangle
+ * (out_re_im[1] is then 0); other dense operators of 1..3 qubits take the
+ * CUDA-core tile kernel and of 4..6 qubits the tensor cores (CUDA cores
+ * when an amplitude exceeds the FP16 split's range). */
 int qsg_expectation_value(qsg_ctx* ctx, const float* state, unsigned n,
                           const unsigned* qs, unsigned k, const float* matrix,
                           double* out_re_im);
