@@ -287,6 +287,30 @@ def test_pair_factor_by_tile_shape(E):
     assert pair_factor([24, 25, 26, 27, 28, 29], [12, 18, 24, 25, 30, 31]) > 2
 
 
+def test_pairs_only_where_the_tile_shape_pays(E):
+    """Two consecutive 6-qubit tensor-core blocks share a pass only when
+    their tile's shape was measured faster than two passes: qubits 0..11
+    pair; a tile of qubits 0, 1, 12, 18, 24..31 (two run bits, no other
+    tile qubit below 12: 2.0x two passes on the GB300) does not."""
+    rng = np.random.default_rng(4)
+
+    def u64():
+        z = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
+        return np.linalg.qr(z)[0]
+
+    for qa, qb, pairs in (([0, 1, 2, 3, 4, 5], [6, 7, 8, 9, 10, 11], 1),
+                          ([24, 25, 26, 27, 28, 29], [12, 18, 24, 25, 30, 31], 0),
+                          ([0, 2, 22, 24, 26, 28], [1, 9, 23, 25, 27, 29], 1),
+                          ([0, 2, 22, 24, 26, 28], [1, 12, 23, 25, 27, 29], 0)):
+        c = E.Circuit(32)
+        c.add_gate(0, qa, u64())
+        c.add_gate(1, qb, u64())
+        plan = E.Plan(c, max_fused_size=6, tensor_path=True, tc_min_k=5,
+                      tc_pairs=2)
+        assert len(plan) == 2
+        assert plan.info()["num_tc_pairs"] == pairs, (qa, qb)
+
+
 def test_bench_pair_factor_is_the_planners():
     """bench.py predicts plan times with the planner's pair table: its
     mirror agrees with this file's on random pairs of 6-qubit target sets
