@@ -67,6 +67,12 @@
 //       `reps` times; prints one line per run: the wall seconds of Run
 //       (fusion + every fused gate, the state synchronised), then the
 //       seconds of FuseGates alone.
+//   trajbench <gates> <max_fused_size> <reps> <threads>
+//       QuantumTrajectorySimulator<IO, QSimRunner<IO, MultiQubitGateFuser,
+//       host SIMD simulator>>::RunBatch over the noisy gate list (gates and
+//       channels) in float with ParallelFor(threads): one warm-up
+//       repetition (r = 10^6), then repetitions r = 0..reps-1, one line of
+//       wall seconds each (each from |0...0>, lib/qtrajectory.h:141-180).
 //   measure <gates> <out-prefix> <seed> <reps> <k> <q...>
 //       From the f64 final state: `reps` rounds of Measure(qubits, rgen)
 //       with one std::mt19937(seed); writes bits per round (.bits) and the
@@ -587,6 +593,37 @@ static int CmdBench(int argc, char** argv) {
   return 0;
 }
 
+static int CmdTrajBench(int argc, char** argv) {
+  if (argc < 6) return 2;
+  unsigned n = 0;
+  auto specs = ReadGates(argv[2], n);
+  const unsigned fsize = std::atoi(argv[3]);
+  const unsigned reps = std::atoi(argv[4]);
+  Circuit<Operation<float>> circuit;
+  circuit.num_qubits = n;
+  for (const auto& g : specs) circuit.ops.push_back(ToOp<float>(g));
+  Factory32T factory;
+  factory.threads = std::atoi(argv[5]);
+  using Runner = QSimRunner<IO, MultiQubitGateFuser<IO>, Factory32T>;
+  using QTSim = QuantumTrajectorySimulator<IO, Runner>;
+  typename QTSim::Parameter param;
+  param.max_fused_size = fsize;
+  param.verbosity = 0;
+  auto ss = factory.CreateStateSpace();
+  auto sim = factory.CreateSimulator();
+  auto measure = [](uint64_t, const Factory32T::StateSpace::State&,
+                    const typename QTSim::Stat&) {};
+  if (!QTSim::RunBatch(param, circuit, 1000000, 1000001, ss, sim, measure))
+    return 1;
+  for (unsigned r = 0; r < reps; ++r) {
+    const double t0 = GetTime();
+    if (!QTSim::RunBatch(param, circuit, r, r + 1, ss, sim, measure)) return 1;
+    std::printf("%.6f\n", GetTime() - t0);
+    std::fflush(stdout);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   if (std::string(argv[1]) == "unitary") return CmdUnitary(argc, argv);
@@ -600,5 +637,6 @@ int main(int argc, char** argv) {
   if (cmd == "traj") return CmdTraj(argc, argv);
   if (cmd == "plan") return CmdPlan(argc, argv);
   if (cmd == "bench") return CmdBench(argc, argv);
+  if (cmd == "trajbench") return CmdTrajBench(argc, argv);
   return 2;
 }
